@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""Throughput of the probebwa mapping path on GB300.
+
+Workload (default): the paired-end configuration -- a synthetic 100 Mbp genome
+(25 x 4 Mbp, GC 41%, 5% segmental duplications of 1-10 kbp in 2-8 copies at
+95-99.5% identity, homopolymer runs of 6-15 bp at 1 per 2 kbp) and 1,000,000
+read pairs of 2 x 150 bp (insert N(350, 50), FR, 0.5% substitutions and
+0.05% indels enriched 5x in homopolymers, Phred N(35, 4) clipped to [2, 41]),
+mapped with the reference's default options. --config 0 selects the
+single-end configuration (1 Mbp genome with 20 planted 2 kbp repeat copies,
+10,000 x 120 bp reads). Data are generated from fixed seeds; no dataset is
+downloaded.
+
+One step maps the whole read set once. `value` is reads/s with the reads
+already in device memory (pbw_map_*_device-style timing from CUDA events on
+the pipeline's stream); `e2e` is the same metric through the public C ABI with
+pinned host buffers, host->device input copies and device->host record copies
+inside the timed region.
+
+--impl reference times the CPU restatement of the reference path (oracle/)
+on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = {0: 0x5EED0000, 1: 0x5EED0001}
+METRIC = "reads/s @1 GB300: plain vs ranked+batched (≤0.05% primaries changed); DP GCUPS"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def workload(cfg: int, cache: str, n_override: int | None = None):
+    from probebwa_gb300 import synth
+    os.makedirs(cache, exist_ok=True)
+    prefix = os.path.join(cache, f"cfg{cfg}")
+    seed = SEED[cfg]
+    if cfg == 0:
+        n = n_override or 10_000
+        meta = {"workload": "single-end 1 Mbp / 10,000 x 120 bp", "genome_bp": 1_000_000, "reads": n,
+                "read_len": 120, "paired": False}
+    else:
+        n = n_override or 1_000_000
+        meta = {"workload": "paired-end 100 Mbp (25 x 4 Mbp) / 1,000,000 pairs x 2 x 150 bp", "genome_bp": 100_000_000,
+                "pairs": n, "read_len": 150, "insert": "N(350,50)", "paired": True}
+    rpath = prefix + f".reads{n}.npz"
+    if not (os.path.exists(prefix + ".stidx") and os.path.exists(prefix + ".sthash") and os.path.exists(rpath)):
+        t = time.time()
+        if cfg == 0:
+            contigs = synth.genome_single(seed)
+        else:
+            contigs = synth.genome_paired(seed)
+        synth.write_index(prefix, contigs)
+        log(f"[bench] index for config {cfg}: {time.time() - t:.1f}s")
+        t = time.time()
+        if cfg == 0:
+            b, q, o = synth.reads_single_fast(seed + 17, contigs, n, L=120, sub=0.01, indel=0.001)
+            np.savez(rpath, b1=b, q1=q, o1=o)
+        else:
+            b1, q1, o1, b2, q2, o2 = synth.reads_paired_fast(seed + 17, contigs, n, L=150, mean=350.0, sd=50.0,
+                                                             sub=0.005, indel=0.0005)
+            np.savez(rpath, b1=b1, q1=q1, o1=o1, b2=b2, q2=q2, o2=o2)
+        log(f"[bench] reads for config {cfg}: {time.time() - t:.1f}s")
+    d = dict(np.load(rpath))
+    return prefix, d, meta
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev: int = 0):
+        self.dev = dev
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def pinned(a: np.ndarray) -> np.ndarray:
+    import torch
+    t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+    v = t.numpy().view(a.dtype).reshape(a.shape)
+    v[...] = a
+    v._keep = t  # noqa: keep the pinned tensor alive
+    return v
+
+
+def run_gpu(args, prefix, d, meta, rank, world):
+    import torch
+    import probebwa_gb300 as P
+    P.build()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    opts = P.MapperOptions(device=dev)
+    t0 = time.time()
+    m = P.Mapper(prefix, options=opts)
+    t_open = time.time() - t0
+    paired = meta["paired"]
+    R1 = P.Reads(pinned(d["b1"]), pinned(d["q1"]), pinned(d["o1"]))
+    R2 = P.Reads(pinned(d["b2"]), pinned(d["q2"]), pinned(d["o2"])) if paired else None
+    n_reads = R1.n * (2 if paired else 1)
+    # pinned outputs
+    def outs(R):
+        recs = P.alloc_records(R.n, len(R.bases))
+        return {k: pinned(v) for k, v in recs.items()}
+    O1 = outs(R1)
+    O2 = outs(R2) if paired else None
+    import ctypes as C
+    L = P.lib()
+
+    def step():
+        if paired:
+            mdl = P.InsertModelC(opts.insert_size_mean, opts.insert_size_sd, 0)
+            rc = L.pbw_map_paired(m.h, C.byref(mdl), C.byref(R1.c()), C.byref(R2.c()), C.byref(P.records_c(O1)),
+                                  C.byref(P.records_c(O2)))
+        else:
+            rc = L.pbw_map_single(m.h, C.byref(R1.c()), C.byref(P.records_c(O1)))
+        m._check(rc)
+        return m.stats()
+
+    for _ in range(args.warmup):
+        step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(dev)
+    clk.start()
+    stats = []
+    t_wall = time.time()
+    for _ in range(args.steps):
+        stats.append(step())
+    torch.cuda.synchronize()
+    t_wall = time.time() - t_wall
+    clocks = clk.stop()
+    # device time of a step: the pipeline's CUDA events, without the input copy
+    dev_ms = [s["ms_seed"] + s["ms_cluster"] + s["ms_align"] + s["ms_pair"] + s["ms_finalize"] + s["ms_d2h"]
+              for s in stats]
+    e2e_ms = [s["ms_total"] for s in stats]
+    mean_dev = statistics.mean(dev_ms) / 1e3
+    mean_e2e = statistics.mean(e2e_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([mean_dev, mean_e2e], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        mean_dev, mean_e2e = float(t[0]), float(t[1])
+    s0 = stats[-1]
+    value = n_reads * world / mean_dev
+    e2e = n_reads * world / mean_e2e
+    h2d = int(R1.bases.nbytes + R1.quals.nbytes + R1.offsets.nbytes)
+    if paired:
+        h2d += int(R2.bases.nbytes + R2.quals.nbytes + R2.offsets.nbytes)
+    rec_bytes = sum(int(v.nbytes) for k, v in O1.items() if k != "cigar") + int(O1["cigar_off"][-1]) * 4
+    if paired:
+        rec_bytes += sum(int(v.nbytes) for k, v in O2.items() if k != "cigar") + int(O2["cigar_off"][-1]) * 4
+    # roofline of the dominant kernel
+    phases = {"seed": s0["ms_seed"], "cluster": s0["ms_cluster"], "align_seeded": s0["ms_align"],
+              "pair": s0["ms_pair"], "finalize": s0["ms_finalize"]}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    L_read = meta["read_len"]
+    seed_bytes = (n_reads * ((L_read + 3) // 4 + L_read) + 8 * s0["seed_probes"] + 8 * s0["seed_entries"] +
+                  8 * s0["seed_hits"])
+    seed_gbs = seed_bytes / (s0["ms_seed"] / 1e3) / 1e9 if s0["ms_seed"] > 0 else 0.0
+    gcups = s0["dp_cells"] / (s0["ms_align"] / 1e3) / 1e9 if s0["ms_align"] > 0 else 0.0
+    roofline = {"kernel": "k_seed (K1 seeding)", "bound": "hbm", "achieved": round(seed_gbs, 1),
+                "peak": hbm_peak, "unit": "GB/s", "frac": round(seed_gbs / hbm_peak, 4),
+                "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": int(seed_bytes), "phase_ms": {k: round(v, 3) for k, v in phases.items()}}
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "reads/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(mean_dev * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded)",
+        "config": dict(meta, l2="inputs larger than L2: 4 GiB k-mer CSR + entries + genome + reads",
+                       index_load_s=round(t_open, 2), parallelism=f"replicas x{world}"),
+        "e2e": {"value": round(e2e, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": rec_bytes,
+                "ms_per_step": round(mean_e2e * 1e3, 3)},
+        "gpu_launches": int(s0["kernel_launches"]) * args.steps,
+        "dp_gcups": round(gcups, 2), "dp_cells_per_step": int(s0["dp_cells"]), "dp_jobs_per_step": int(s0["dp_jobs"]),
+        "roofline": roofline, "clocks": clocks, "wall_s_timed": round(t_wall, 3),
+    }
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU (reference path restatement)
+# ---------------------------------------------------------------------------
+def cpu_time(prefix, d, meta, n_sample: int, threads: int):
+    from oracle import pyoracle as O
+    O.build()
+    m = O.Mapper(prefix, threads=threads)
+    paired = meta["paired"]
+    o1 = d["o1"]
+    k = min(n_sample, len(o1) - 1)
+    R1 = O.Reads(d["b1"][:int(o1[k])], d["q1"][:int(o1[k])], o1[:k + 1])
+    if paired:
+        o2 = d["o2"]
+        R2 = O.Reads(d["b2"][:int(o2[k])], d["q2"][:int(o2[k])], o2[:k + 1])
+        t, _, _ = m.time_map_paired(R1, R2)
+        reads = 2 * k
+    else:
+        t, _ = m.time_map_single(R1)
+        reads = k
+    m.close()
+    return reads, t
+
+
+def cpu_baseline(prefix, d, meta):
+    threads = os.cpu_count() or 1
+    n = 40_000 if meta["paired"] else 10_000
+    reads, t = cpu_time(prefix, d, meta, n, threads)
+    return {"value": round(reads / t, 1), "unit": "reads/s", "cores": threads, "kind": "port",
+            "sample": f"first {reads} reads ({'pairs' if meta['paired'] else 'reads'} incl. the serial warm-up) "
+                      f"of the same workload, oracle/ C++ restatement, {threads} threads"}
+
+
+def run_reference(args, prefix, d, meta):
+    threads = os.cpu_count() or 1
+    n = 20_000 if meta["paired"] else 10_000
+    for _ in range(args.warmup):
+        cpu_time(prefix, d, meta, min(n, 2000), threads)
+    times, reads = [], 0
+    for _ in range(args.steps):
+        reads, t = cpu_time(prefix, d, meta, n, threads)
+        times.append(t)
+    v = reads / statistics.mean(times)
+    cb = {"value": round(v, 1), "unit": "reads/s", "cores": threads, "kind": "port",
+          "sample": f"first {reads} reads of the workload per step (oracle/ C++ restatement of the reference CPU path)"}
+    return {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "reads/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(times) * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+            "data": "synthetic (seeded)", "config": meta, "cpu_baseline": cb,
+            "e2e": {"value": round(v, 1), "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--n", type=int, default=None, help="override read / pair count")
+    ap.add_argument("--cache", default=os.environ.get("PBW_BENCH_CACHE", "/tmp/pbw_bench_cache"))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        prefix, d, meta = workload(args.config, args.cache, args.n)
+        print(json.dumps(run_reference(args, prefix, d, meta)), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    prefix, d, meta = workload(args.config, args.cache, args.n)
+    out = run_gpu(args, prefix, d, meta, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(prefix, d, meta)
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+/* probebwa_gpu.h -- C ABI of the GB300 (sm_103a) probebwa mapping path.
+ *
+ * Plain C types only: pointers, sizes and status codes. Every call returns
+ * PBW_OK (0) or a negative PBW_ERR_* code; pbw_last_error(h) (or
+ * pbw_last_error(NULL) for a failed pbw_open) describes the failure. No C++
+ * exception or CUDA error crosses this boundary.
+ *
+ * Each entry point names the reference interface it replaces
+ * (GUIBA-EX/probebwa, file:line).
+ *
+ * Threading: one handle owns one CUDA stream and its device buffers; calls on
+ * one handle must be serialised by the caller. Different handles are
+ * independent.
+ */
+#ifndef PROBEBWA_GPU_H
+#define PROBEBWA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBW_ABI_VERSION 1
+
+#define PBW_OK 0
+#define PBW_ERR_ARG -1        /* invalid argument */
+#define PBW_ERR_IO -2         /* cannot open / read an index file */
+#define PBW_ERR_FORMAT -3     /* malformed .stidx / .sthash */
+#define PBW_ERR_CUDA -4       /* CUDA runtime error */
+#define PBW_ERR_NOMEM -5      /* device or host allocation failed */
+#define PBW_ERR_LIMIT -6      /* input beyond a documented device limit */
+#define PBW_ERR_CAPACITY -7   /* caller-provided output array too small */
+#define PBW_ERR_DEVICE -8     /* a kernel reported an internal error */
+
+/* Longest read the device path maps (bases). Longer reads: PBW_ERR_LIMIT. */
+#define PBW_MAX_READ_LEN 1024
+
+typedef struct pbw_handle pbw_handle;
+
+/* MapperOptions (src/types.rs:207-249) plus device settings. */
+typedef struct {
+  double substitution_rate;   /* --substitution-rate, default 0.001 */
+  double insert_size_mean;    /* insert-size prior mean, default 250 */
+  double insert_size_sd;      /* insert-size prior sd, default 60 */
+  uint64_t max_indel_len;     /* seeded DP band, default 30 */
+  uint32_t gap_open_phred;    /* --gapopen, default 40 */
+  uint32_t gap_extend_phred;  /* --gapextend, default 3 */
+  double sv_prior_phred;      /* --svprior, default 55 */
+  /* SwissTable group width whose iteration order the candidate tie order
+   * follows: 16 = the reference built for x86_64 (SSE2), 8 = aarch64. */
+  int32_t group_width;
+  int32_t device;             /* CUDA device ordinal */
+  uint64_t chunk_reads;       /* reads per device chunk (0 = default) */
+} pbw_options;
+
+/* Reads as structure-of-arrays (Read, src/types.rs:79-84): concatenated
+ * sequence bytes (any case; uppercased like DnaSeq::from_ascii), Phred
+ * scores with the ASCII offset already removed (QualityScores::scores), and
+ * n+1 offsets shared by both arrays (sequence and quality have equal
+ * length). */
+typedef struct {
+  uint64_t n;
+  const uint8_t* bases;
+  const uint8_t* quals;
+  const uint64_t* offsets;
+} pbw_reads;
+
+/* Output records as structure-of-arrays (AlignmentRecord, src/types.rs:181-203).
+ * contig / mate_contig are indices into the genome's contigs (-1 = '*').
+ * pos and mate_pos are 1-based (0 = unmapped / none). flag is the SAM FLAG of
+ * src/io/sam.rs:126-143. log_lk = alignment_score, posterior =
+ * posterior_prob. as_score (the DP score the reference computes and drops,
+ * src/mapper/single.rs:128) and nm (edit distance) are derived fields.
+ * cigar holds (len << 4) | op with op 0=M 1=I 2=D 4=S; cigar_off has n+1
+ * entries; cigar_cap is the capacity of cigar (2*total_bases + 2*n always
+ * suffices). SEQ/QUAL are not copied: they are the input read, reverse-
+ * complemented and reversed when (flag & 0x10). */
+typedef struct {
+  uint64_t n;
+  int32_t* contig;
+  uint64_t* pos;
+  uint8_t* mapq;
+  uint16_t* flag;
+  int32_t* mate_contig;
+  uint64_t* mate_pos;
+  int64_t* tlen;
+  double* log_lk;
+  double* posterior;
+  int32_t* as_score;
+  int32_t* nm;
+  uint32_t* cigar_off;
+  uint32_t* cigar;
+  uint64_t cigar_cap;
+} pbw_records;
+
+/* InsertSizeDistribution (src/types.rs:266-270). */
+typedef struct {
+  double mean;
+  double sd;
+  uint64_t n_observed;
+} pbw_insert_model;
+
+/* Per-call device timing (milliseconds, CUDA events) and work counters. */
+typedef struct {
+  double ms_total;
+  double ms_h2d;
+  double ms_seed;
+  double ms_cluster;
+  double ms_align;
+  double ms_finalize;
+  double ms_pair;
+  double ms_d2h;
+  uint64_t seed_probes;       /* hash lookups */
+  uint64_t seed_entries;      /* bucket entries read */
+  uint64_t seed_hits;         /* hits that passed the similarity filter */
+  uint64_t dp_jobs;           /* alignments */
+  uint64_t dp_cells;          /* DP cells (smith_waterman.rs:191-203 bands) */
+  uint64_t kernel_launches;   /* kernels launched by the call */
+} pbw_stats;
+
+void pbw_default_options(pbw_options* opt);
+
+/* Open an index: replaces GenomeIndex::load (src/index/genome.rs:80-86) +
+ * HashTable::load (src/index/hashtable.rs:73-79) + the SingleEndMapper /
+ * PairedEndMapper constructors (src/mapper/single.rs:52-70,
+ * src/mapper/paired.rs:85-99). Reads <prefix>.stidx and <prefix>.sthash and
+ * uploads a 2-bit genome, an N mask and a dense k-mer CSR to the device. */
+int pbw_open(const char* genome_prefix, const char* hash_prefix, const pbw_options* opt, pbw_handle** out);
+void pbw_close(pbw_handle* h);
+const char* pbw_last_error(const pbw_handle* h);
+
+/* Index facts: contig count, total length, contig names / lengths. */
+uint64_t pbw_num_contigs(const pbw_handle* h);
+uint64_t pbw_total_length(const pbw_handle* h);
+const char* pbw_contig_name(const pbw_handle* h, uint64_t i);
+uint64_t pbw_contig_length(const pbw_handle* h, uint64_t i);
+
+/* Single-end mapping: replaces SingleEndMapper::map (src/mapper/single.rs:164-209)
+ * applied per read by map_reads_with_format (src/lib.rs:86-104). Host buffers
+ * in and out. */
+int pbw_map_single(pbw_handle* h, const pbw_reads* reads, pbw_records* out);
+
+/* Paired-end mapping: replaces map_paired (src/lib.rs:145-185), i.e.
+ * PairedEndMapper::map_pair for the first 500 pairs and
+ * PairedEndMapper::map_pairs_batch (src/mapper/paired.rs:127-146) for batches
+ * of 2000 after them. model is the insert-size model, read and updated. */
+int pbw_map_paired(pbw_handle* h, pbw_insert_model* model, const pbw_reads* r1, const pbw_reads* r2,
+                   pbw_records* o1, pbw_records* o2);
+
+/* Stage entry points for parity tests. */
+
+/* SmithWatermanAligner::new(band, gop, gep).align(read, qual, ref, hint)
+ * (src/align/smith_waterman.rs:113-255) for a batch of independent problems.
+ * reads/quals/refs are concatenated with n+1 offsets; outputs score, offset
+ * and CIGAR (packed as in pbw_records, cigar_off n+1). */
+int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8_t* quals,
+                    const uint64_t* read_off, const uint8_t* refs, const uint64_t* ref_off,
+                    const int64_t* hint, const uint64_t* band, int32_t* score, uint64_t* offset,
+                    uint32_t* cigar_off, uint32_t* cigar, uint64_t cigar_cap);
+
+/* find_seed_hits (src/mapper/seeds.rs:91-151) for a batch of reads: per read
+ * the hit count and, in emission order, hits packed as
+ * (strand << 63) | (contig << 40) | ref_pos with read_pos in hit_read_pos;
+ * repeat_prob per 15-mer window (n_windows = len - 14). hit_off (n+1) and
+ * win_off (n+1) are computed by the call. */
+int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uint64_t* hits,
+                   uint32_t* hit_read_pos, uint64_t hit_cap, uint64_t* win_off, double* repeat_prob,
+                   uint64_t win_cap);
+
+/* cluster_hits (src/mapper/candidates.rs:30-78) after seeding: per read the
+ * first max_per_read candidates in final order (contig, 0-based position,
+ * strand, score) and the full candidate count. */
+int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_read, uint32_t* n_cand,
+                      uint32_t* total_cand, uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,
+                      double* cand_score);
+
+/* Timing and counters of the last map call on this handle. */
+int pbw_last_stats(const pbw_handle* h, pbw_stats* st);
+
+/* Device-resident variant of pbw_map_single for throughput measurement:
+ * bases/quals/offsets are device pointers; records are written to host
+ * arrays as in pbw_map_single but no host-to-device input copy happens. */
+int pbw_map_single_device(pbw_handle* h, const pbw_reads* dev_reads, pbw_records* out);
+
+/* SAM text (src/io/sam.rs:69-108, format_sam :37-58) for records produced by
+ * a map call: header (@HD, @SQ per contig, @PG with command_line) then one
+ * line per record. read_ids[i] is the QNAME. Writes to path. */
+int pbw_write_sam(pbw_handle* h, const char* path, const char* command_line, const pbw_reads* reads,
+                  const char* const* read_ids, const pbw_records* recs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PROBEBWA_GPU_H */

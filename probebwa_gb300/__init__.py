@@ -1,0 +1,363 @@
+"""probebwa_gb300: the probebwa read-mapping hot path on a GB300 (sm_103a).
+
+Python mirror of the reference's mapper / align / mapq interface over the C
+ABI in include/probebwa_gpu.h (ctypes; plain pointers and sizes). The compute
+path is the CUDA library probebwa_gb300/_lib/libprobebwa_gb300.so; importing a
+mapping entry point without it raises instead of falling back to the CPU.
+
+Reference interfaces mirrored (GUIBA-EX/probebwa):
+  SingleEndMapper.map              src/mapper/single.rs:164-209
+  PairedEndMapper.map_pairs_batch  src/mapper/paired.rs:127-146 (+ lib.rs:145-185 schedule)
+  SmithWatermanAligner.align       src/align/smith_waterman.rs:113-255
+  find_seed_hits                   src/mapper/seeds.rs:91-151
+  cluster_hits                     src/mapper/candidates.rs:30-78
+  MapperOptions                    src/types.rs:207-249
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libprobebwa_gb300.so")
+
+PBW_OK = 0
+ERRORS = {-1: "invalid argument", -2: "I/O error", -3: "malformed index file", -4: "CUDA error",
+          -5: "out of memory", -6: "input beyond a device limit", -7: "output capacity too small",
+          -8: "device kernel error"}
+MAX_READ_LEN = 1024
+
+
+class PbwError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+class OptionsC(C.Structure):
+    _fields_ = [
+        ("substitution_rate", C.c_double),
+        ("insert_size_mean", C.c_double),
+        ("insert_size_sd", C.c_double),
+        ("max_indel_len", C.c_uint64),
+        ("gap_open_phred", C.c_uint32),
+        ("gap_extend_phred", C.c_uint32),
+        ("sv_prior_phred", C.c_double),
+        ("group_width", C.c_int32),
+        ("device", C.c_int32),
+        ("chunk_reads", C.c_uint64),
+    ]
+
+
+class ReadsC(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("bases", C.c_void_p), ("quals", C.c_void_p), ("offsets", C.c_void_p)]
+
+
+class RecordsC(C.Structure):
+    _fields_ = [("n", C.c_uint64)] + [(k, C.c_void_p) for k in (
+        "contig", "pos", "mapq", "flag", "mate_contig", "mate_pos", "tlen", "log_lk", "posterior", "as_score", "nm",
+        "cigar_off", "cigar")] + [("cigar_cap", C.c_uint64)]
+
+
+class InsertModelC(C.Structure):
+    _fields_ = [("mean", C.c_double), ("sd", C.c_double), ("n_observed", C.c_uint64)]
+
+
+class StatsC(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("ms_total", "ms_h2d", "ms_seed", "ms_cluster", "ms_align", "ms_finalize",
+                                           "ms_pair", "ms_d2h")] + \
+               [(k, C.c_uint64) for k in ("seed_probes", "seed_entries", "seed_hits", "dp_jobs", "dp_cells",
+                                          "kernel_launches")]
+
+
+_lib = None
+
+EXPORTS = ["pbw_default_options", "pbw_open", "pbw_close", "pbw_last_error", "pbw_num_contigs", "pbw_total_length",
+           "pbw_contig_name", "pbw_contig_length", "pbw_map_single", "pbw_map_paired", "pbw_align_batch",
+           "pbw_seed_batch", "pbw_cluster_batch", "pbw_last_stats", "pbw_map_single_device", "pbw_write_sam"]
+
+
+def build(verbose: bool = False) -> str:
+    from . import native_build as _b
+    return _b.build(verbose=verbose)
+
+
+def lib():
+    """Load the native library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"probebwa_gb300 native library missing: {LIB_PATH} (run probebwa_gb300.build())")
+        L = C.CDLL(LIB_PATH)
+        vp, u64, i64, u32, dbl, cp = C.c_void_p, C.c_uint64, C.c_int64, C.c_uint32, C.c_double, C.c_char_p
+        L.pbw_default_options.argtypes = [C.POINTER(OptionsC)]
+        L.pbw_open.argtypes = [cp, cp, C.POINTER(OptionsC), C.POINTER(vp)]
+        L.pbw_close.argtypes = [vp]
+        L.pbw_last_error.argtypes = [vp]
+        L.pbw_last_error.restype = cp
+        L.pbw_num_contigs.argtypes = [vp]
+        L.pbw_num_contigs.restype = u64
+        L.pbw_total_length.argtypes = [vp]
+        L.pbw_total_length.restype = u64
+        L.pbw_contig_name.argtypes = [vp, u64]
+        L.pbw_contig_name.restype = cp
+        L.pbw_contig_length.argtypes = [vp, u64]
+        L.pbw_contig_length.restype = u64
+        L.pbw_map_single.argtypes = [vp, C.POINTER(ReadsC), C.POINTER(RecordsC)]
+        L.pbw_map_single_device.argtypes = [vp, C.POINTER(ReadsC), C.POINTER(RecordsC)]
+        if hasattr(L, "pbw_map_paired"):
+            L.pbw_map_paired.argtypes = [vp, C.POINTER(InsertModelC), C.POINTER(ReadsC), C.POINTER(ReadsC),
+                                         C.POINTER(RecordsC), C.POINTER(RecordsC)]
+        L.pbw_align_batch.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u64]
+        L.pbw_seed_batch.argtypes = [vp, C.POINTER(ReadsC), vp, vp, vp, u64, vp, vp, u64]
+        L.pbw_cluster_batch.argtypes = [vp, C.POINTER(ReadsC), u32, vp, vp, vp, vp, vp, vp]
+        L.pbw_last_stats.argtypes = [vp, C.POINTER(StatsC)]
+        L.pbw_write_sam.argtypes = [vp, cp, cp, C.POINTER(ReadsC), C.POINTER(cp), C.POINTER(RecordsC)]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+@dataclass
+class MapperOptions:
+    """MapperOptions (src/types.rs:207-249) plus device settings."""
+    substitution_rate: float = 0.001
+    insert_size_mean: float = 250.0
+    insert_size_sd: float = 60.0
+    max_indel_len: int = 30
+    gap_open_phred: int = 40
+    gap_extend_phred: int = 3
+    sv_prior_phred: float = 55.0
+    group_width: int = 16
+    device: int = 0
+    chunk_reads: int = 0
+
+    def c(self) -> OptionsC:
+        return OptionsC(self.substitution_rate, self.insert_size_mean, self.insert_size_sd, self.max_indel_len,
+                        self.gap_open_phred, self.gap_extend_phred, self.sv_prior_phred, self.group_width,
+                        self.device, self.chunk_reads)
+
+
+class Reads:
+    """Reads as SoA numpy arrays: bases (uint8), Phred scores (uint8), n+1 offsets."""
+
+    def __init__(self, bases, quals, offsets, ids=None):
+        self.bases = np.ascontiguousarray(bases, dtype=np.uint8)
+        self.quals = np.ascontiguousarray(quals, dtype=np.uint8)
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self.ids = ids if ids is not None else [f"r{i}" for i in range(len(self.offsets) - 1)]
+
+    @property
+    def n(self) -> int:
+        return len(self.offsets) - 1
+
+    @staticmethod
+    def from_lists(seqs, quals=None, ids=None) -> "Reads":
+        seqs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+        if quals is None:
+            quals = [bytes([40] * len(s)) for s in seqs]
+        quals = [bytes(q) for q in quals]
+        offs = np.zeros(len(seqs) + 1, dtype=np.uint64)
+        if seqs:
+            offs[1:] = np.cumsum([len(s) for s in seqs])
+        b = np.frombuffer(b"".join(seqs) + b"\0", dtype=np.uint8)[:-1].copy()
+        q = np.frombuffer(b"".join(quals) + b"\0", dtype=np.uint8)[:-1].copy()
+        return Reads(b, q, offs, ids)
+
+    def c(self) -> ReadsC:
+        if self.bases.size == 0:
+            self._keep = (np.zeros(1, np.uint8), np.zeros(1, np.uint8))
+            return ReadsC(self.n, _ptr(self._keep[0]), _ptr(self._keep[1]), _ptr(self.offsets))
+        return ReadsC(self.n, _ptr(self.bases), _ptr(self.quals), _ptr(self.offsets))
+
+    def seq(self, i: int) -> bytes:
+        return self.bases[int(self.offsets[i]):int(self.offsets[i + 1])].tobytes()
+
+
+RECORD_FIELDS = (("contig", np.int32), ("pos", np.uint64), ("mapq", np.uint8), ("flag", np.uint16),
+                 ("mate_contig", np.int32), ("mate_pos", np.uint64), ("tlen", np.int64), ("log_lk", np.float64),
+                 ("posterior", np.float64), ("as_score", np.int32), ("nm", np.int32))
+
+
+def alloc_records(n: int, total_len: int) -> dict:
+    r = {k: np.zeros(max(n, 1), t)[:n] for k, t in RECORD_FIELDS}
+    r["cigar_off"] = np.zeros(n + 1, np.uint32)
+    r["cigar"] = np.zeros(2 * total_len + 2 * n + 16, np.uint32)
+    return r
+
+
+def records_c(r: dict) -> RecordsC:
+    n = len(r["contig"])
+    keep = [r[k] if r[k].size else np.zeros(1, r[k].dtype) for k, _ in RECORD_FIELDS]
+    r["_keep"] = keep
+    return RecordsC(n, *[_ptr(a) for a in keep], _ptr(r["cigar_off"]), _ptr(r["cigar"]), len(r["cigar"]))
+
+
+OPS = "MIDXSH"
+
+
+def cigar_strings(r: dict) -> list:
+    co, cg = r["cigar_off"], r["cigar"]
+    return ["".join(f"{int(w) >> 4}{OPS[int(w) & 15]}" for w in cg[co[i]:co[i + 1]])
+            for i in range(len(r["contig"]))]
+
+
+class Mapper:
+    """One device handle: index resident in HBM plus the mapping pipeline."""
+
+    def __init__(self, genome_prefix: str, hash_prefix: str | None = None, options: MapperOptions | None = None,
+                 **kw):
+        self.options = options or MapperOptions(**kw)
+        self._opt = self.options.c()
+        h = C.c_void_p()
+        rc = lib().pbw_open(genome_prefix.encode(), (hash_prefix or genome_prefix).encode(), C.byref(self._opt),
+                            C.byref(h))
+        if rc != PBW_OK:
+            raise PbwError(rc, lib().pbw_last_error(None).decode())
+        self.h = h
+
+    def _check(self, rc):
+        if rc != PBW_OK:
+            raise PbwError(rc, lib().pbw_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pbw_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def contigs(self):
+        L = lib()
+        return [(L.pbw_contig_name(self.h, i).decode(), L.pbw_contig_length(self.h, i))
+                for i in range(L.pbw_num_contigs(self.h))]
+
+    def map_single(self, reads: Reads) -> dict:
+        recs = alloc_records(reads.n, len(reads.bases))
+        self._check(lib().pbw_map_single(self.h, C.byref(reads.c()), C.byref(records_c(recs))))
+        return recs
+
+    def map_paired(self, r1: Reads, r2: Reads, mean=None, sd=None):
+        m = InsertModelC(self.options.insert_size_mean if mean is None else mean,
+                         self.options.insert_size_sd if sd is None else sd, 0)
+        o1 = alloc_records(r1.n, len(r1.bases))
+        o2 = alloc_records(r2.n, len(r2.bases))
+        self._check(lib().pbw_map_paired(self.h, C.byref(m), C.byref(r1.c()), C.byref(r2.c()),
+                                         C.byref(records_c(o1)), C.byref(records_c(o2))))
+        return o1, o2, (m.mean, m.sd, m.n_observed)
+
+    def stats(self) -> dict:
+        s = StatsC()
+        self._check(lib().pbw_last_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in StatsC._fields_}
+
+    def seed_batch(self, reads: Reads, hit_cap: int | None = None):
+        """find_seed_hits per read: (hit_off, packed hits, read_pos, win_off, repeat_prob)."""
+        n = reads.n
+        hit_cap = hit_cap or (4096 * max(n, 1))
+        hit_off = np.zeros(n + 1, np.uint64)
+        hits = np.zeros(hit_cap, np.uint64)
+        rpos = np.zeros(hit_cap, np.uint32)
+        win_cap = max(len(reads.bases), 1)
+        win_off = np.zeros(n + 1, np.uint64)
+        rep = np.zeros(win_cap, np.float64)
+        self._check(lib().pbw_seed_batch(self.h, C.byref(reads.c()), _ptr(hit_off), _ptr(hits), _ptr(rpos), hit_cap,
+                                         _ptr(win_off), _ptr(rep), win_cap))
+        return hit_off, hits[:hit_off[-1]], rpos[:hit_off[-1]], win_off, rep[:win_off[-1]]
+
+    def cluster_batch(self, reads: Reads, max_per_read: int = 64):
+        """cluster_hits per read: first max_per_read candidates and the full count."""
+        n = reads.n
+        nc = np.zeros(max(n, 1), np.uint32)
+        tc = np.zeros(max(n, 1), np.uint32)
+        cc = np.zeros(max(n, 1) * max_per_read, np.uint32)
+        cp = np.zeros(max(n, 1) * max_per_read, np.uint64)
+        cs = np.zeros(max(n, 1) * max_per_read, np.uint8)
+        sc = np.zeros(max(n, 1) * max_per_read, np.float64)
+        self._check(lib().pbw_cluster_batch(self.h, C.byref(reads.c()), max_per_read, _ptr(nc), _ptr(tc), _ptr(cc),
+                                            _ptr(cp), _ptr(cs), _ptr(sc)))
+        return nc[:n], tc[:n], cc.reshape(-1, max_per_read)[:n], cp.reshape(-1, max_per_read)[:n], \
+            cs.reshape(-1, max_per_read)[:n], sc.reshape(-1, max_per_read)[:n]
+
+    def align_batch(self, problems):
+        """SmithWatermanAligner::align for a list of (read, qual, ref, hint, band)."""
+        n = len(problems)
+        reads = [bytes(p[0]) for p in problems]
+        quals = [bytes(p[1]) for p in problems]
+        refs = [bytes(p[2]) for p in problems]
+        ro = np.zeros(n + 1, np.uint64)
+        fo = np.zeros(n + 1, np.uint64)
+        ro[1:] = np.cumsum([len(x) for x in reads])
+        fo[1:] = np.cumsum([len(x) for x in refs])
+        rb = np.frombuffer(b"".join(reads) + b"\0", np.uint8)[:-1].copy()
+        qb = np.frombuffer(b"".join(quals) + b"\0", np.uint8)[:-1].copy()
+        fb = np.frombuffer(b"".join(refs) + b"\0", np.uint8)[:-1].copy()
+        for a in ("rb", "qb", "fb"):
+            if locals()[a].size == 0:
+                pass
+        rb = rb if rb.size else np.zeros(1, np.uint8)
+        qb = qb if qb.size else np.zeros(1, np.uint8)
+        fb = fb if fb.size else np.zeros(1, np.uint8)
+        hint = np.array([p[3] for p in problems], np.int64)
+        band = np.array([p[4] for p in problems], np.uint64)
+        score = np.zeros(n, np.int32)
+        off = np.zeros(n, np.uint64)
+        cap = int(2 * ro[-1] + fo[-1] + 8 * n + 8)
+        co = np.zeros(n + 1, np.uint32)
+        cg = np.zeros(cap, np.uint32)
+        self._check(lib().pbw_align_batch(self.h, n, _ptr(rb), _ptr(qb), _ptr(ro), _ptr(fb), _ptr(fo), _ptr(hint),
+                                          _ptr(band), _ptr(score), _ptr(off), _ptr(co), _ptr(cg), cap))
+        out = []
+        for i in range(n):
+            cig = "".join(f"{int(w) >> 4}{OPS[int(w) & 15]}" for w in cg[co[i]:co[i + 1]])
+            out.append((int(score[i]), cig, int(off[i])))
+        return out
+
+    def write_sam(self, path: str, reads: Reads, recs: dict, command_line: str = "probebwa map"):
+        ids = (C.c_char_p * max(reads.n, 1))(*[i.encode() for i in reads.ids])
+        self._check(lib().pbw_write_sam(self.h, path.encode(), command_line.encode(), C.byref(reads.c()), ids,
+                                        C.byref(records_c(recs))))
+
+
+# ---- reference-shaped API ----
+
+class SingleEndMapper:
+    """SingleEndMapper (src/mapper/single.rs:33-209) over one device handle."""
+
+    def __init__(self, genome_prefix: str, hash_prefix: str | None = None, options: MapperOptions | None = None):
+        self.mapper = Mapper(genome_prefix, hash_prefix, options)
+
+    def map(self, reads: Reads) -> dict:
+        return self.mapper.map_single(reads)
+
+
+class PairedEndMapper:
+    """PairedEndMapper (src/mapper/paired.rs:76-146) with the map_paired schedule of src/lib.rs:145-185."""
+
+    def __init__(self, genome_prefix: str, hash_prefix: str | None = None, options: MapperOptions | None = None):
+        self.mapper = Mapper(genome_prefix, hash_prefix, options)
+        o = self.mapper.options
+        self.insert_model = (o.insert_size_mean, o.insert_size_sd, 0)
+
+    def map_pairs(self, r1: Reads, r2: Reads):
+        m, s, _ = self.insert_model
+        o1, o2, model = self.mapper.map_paired(r1, r2, m, s)
+        self.insert_model = model
+        return o1, o2

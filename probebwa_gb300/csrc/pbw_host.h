@@ -1,0 +1,42 @@
+// pbw_host.h -- glue-kernel argument blocks and launchers used by the host pipeline.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pbw_common.cuh"
+#include "pbw_kernels.h"
+
+namespace pbw {
+
+struct MakeJobsArgs {
+  DevGenome G;
+  const uint64_t* offs;
+  uint32_t r0, nr;
+  const Cand* cand;
+  const uint32_t* n_cand;
+  uint64_t right_pad;       // max(max_indel_len, 10)
+  uint32_t band;            // max_indel_len
+  int32_t gap_open, gap_extend;
+  AlnJob* jobs;
+  unsigned int* n_jobs;
+  AlnOut* out;
+  uint8_t mate;             // read set of the jobs (AlnJob::mate)
+};
+
+struct CigarGatherArgs {
+  const uint64_t* offs;
+  uint32_t r0, nr;
+  const int32_t* best;
+  const AlnOut* aln;
+  const uint32_t* cig_pool;
+  const uint32_t* cig_off;  // chunk-relative exclusive offsets (including the chunk base)
+  uint32_t* cigar;          // packed output for the whole call
+};
+
+void launch_make_jobs_single(const MakeJobsArgs& a, cudaStream_t st);
+void launch_cigar_gather(const CigarGatherArgs& a, cudaStream_t st);
+uint64_t scan_blocks(uint64_t n);
+void launch_scan_excl(unsigned int* a, uint64_t n, unsigned int* out, unsigned int* block_sums, unsigned int* total,
+                      const unsigned int* base_in, cudaStream_t st);
+
+}  // namespace pbw

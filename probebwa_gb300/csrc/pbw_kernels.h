@@ -1,0 +1,162 @@
+// pbw_kernels.h -- kernel argument blocks and launchers (host <-> device).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pbw_common.cuh"
+
+namespace pbw {
+
+// ---- K1 seeding ----
+struct SeedArgs {
+  DevGenome G;
+  DevIndex idx;
+  const uint8_t* bases;
+  const uint64_t* offs;
+  uint32_t r0, nr;          // reads [r0, r0+nr) of the offsets array
+  int lmax;                 // longest read in the chunk
+  unsigned long long* hits; // nr * hcap
+  uint32_t hcap;
+  uint32_t* hit_cnt;        // nr
+  uint8_t* overflow;        // nr
+  unsigned int* n_overflow; // 1
+  uint8_t* rep;             // nr * wcap: 0 none, 1 neighbour repetitive, 2 exact repetitive
+  uint32_t wcap;
+  uint16_t* hit_rpos;       // optional nr * hcap read positions (parity tests)
+  unsigned long long* counters;  // probes, entries, hits
+};
+__host__ __device__ inline size_t seed_smem_per_warp(int lmax) {
+  int W = lmax - KMER + 1 > 0 ? lmax - KMER + 1 : 1;
+  size_t s = (size_t)(4 * W + 1) * 4 + (size_t)lmax;
+  return (s + 15) & ~(size_t)15;
+}
+void launch_seed(const SeedArgs& a, int grid, cudaStream_t st);
+
+// ---- K2 clustering ----
+struct Cand {
+  unsigned long long pos;   // 0-based candidate position (candidates.rs:62-71)
+  uint32_t contig;
+  uint32_t score;           // cluster size
+  uint8_t strand;
+  uint8_t pad[7];
+};
+struct ClusterArgs {
+  const unsigned long long* hits;
+  const uint32_t* hit_cnt;
+  const uint8_t* overflow;
+  uint32_t hcap;
+  const uint64_t* offs;
+  uint32_t r0, nr;
+  int group_width;
+  uint32_t max_out;         // candidates kept per read (20 for mapping)
+  Cand* cand;               // nr * max_out
+  uint32_t* n_cand;         // nr: kept
+  uint32_t* total_cand;     // nr: all clusters (optional)
+  uint32_t h_lo, h_hi;      // process reads with h_lo < H <= h_hi
+  int* err;                 // device error word
+};
+size_t cluster_smem(uint32_t hmax, int threads);
+void launch_cluster(const ClusterArgs& a, uint32_t hmax, int threads, cudaStream_t st);
+
+// ---- K3 alignment ----
+// One alignment problem: query = read (forward) or its reverse complement,
+// against ref window [ref_start, ref_end) of contig, banded around
+// j = i + hint (smith_waterman.rs:190-194).
+struct AlnJob {
+  unsigned long long ref_start, ref_end;
+  long long hint;
+  uint32_t read;            // index into the offsets array
+  uint32_t slot;            // output slot
+  uint32_t contig;
+  uint32_t band;            // band half-width (max_indel_len, or the window length)
+  uint8_t rev;              // query is the reverse complement
+  uint8_t valid;
+  uint8_t mate;             // 0: reads in bases/quals/offs, 1: in bases2/quals2/offs2
+  uint8_t pad;
+  uint32_t pad2;
+  int32_t gap_open, gap_extend;
+};
+struct AlnOut {
+  double log_lk;
+  unsigned long long pos;   // true_start, 0-based (single.rs:135)
+  int32_t score;
+  uint32_t span;            // cigar_reference_span
+  uint32_t n_ops;
+  uint32_t cig_pool;        // offset into the CIGAR pool when n_ops > CIG_INLINE
+  uint32_t cig[CIG_INLINE];
+  // log_entropy inputs (bayesian.rs:306-357) and edit distance
+  int32_t n_hq, m_hq, readlen, ins_runs, del_runs, gc, total, nm;
+};
+struct AlignArgs {
+  DevGenome G;
+  const DevTables* tab;
+  const double* gc_lnb;     // gc tables, triangular by total
+  const double* gc_lnbm1;
+  const uint8_t* bases;     // reads (also used for explicit problems)
+  const uint8_t* quals;
+  const uint64_t* offs;
+  const uint8_t* bases2;    // second read set (mate 2) for paired jobs
+  const uint8_t* quals2;
+  const uint64_t* offs2;
+  const AlnJob* jobs;
+  const unsigned int* n_jobs;  // device count (work queue size)
+  unsigned int* next_job;      // work queue head
+  AlnOut* out;
+  uint32_t* cig_pool;
+  unsigned int* cig_pool_used;
+  uint32_t cig_pool_cap;
+  // explicit reference windows (pbw_align_batch): if non-null, job.ref_* index these bytes
+  const uint8_t* ref_bytes;
+  int lmax;                 // longest query
+  int nmax;                 // longest reference window
+  size_t tb_smem;           // bytes of shared traceback per warp
+  unsigned char* tb_global; // traceback scratch for windows too wide for shared memory
+  size_t tb_global_per_warp;
+  unsigned long long* counters;  // jobs, cells
+  int* err;
+};
+void launch_align(const AlignArgs& a, int grid, cudaStream_t st);
+void launch_align_wide(const AlignArgs& a, int grid, cudaStream_t st);
+size_t wide_slab_bytes(int lmax, int nmax);
+size_t align_smem_per_warp(int lmax, int nmax, size_t tb_smem);
+
+// ---- K4 finalize (single-end) ----
+struct FinalizeArgs {
+  DevGenome G;
+  const DevTables* tab;
+  const double* ln_n;
+  const uint8_t* quals;
+  const uint64_t* offs;
+  uint32_t r0, nr;
+  const AlnOut* aln;        // nr * MAX_CAND
+  const uint32_t* n_cand;
+  const Cand* cand;
+  const uint8_t* rep;
+  uint32_t wcap;
+  const double* gc_lnb;
+  const double* gc_lnbm1;
+  uint64_t seed_k;
+  // outputs (device, chunk-relative)
+  int32_t* contig;
+  unsigned long long* pos;
+  uint8_t* mapq;
+  uint16_t* flag;
+  double* log_lk;
+  double* posterior;
+  int32_t* as_score;
+  int32_t* nm;
+  uint32_t* n_ops;          // per read CIGAR op count
+  int32_t* best;            // per read winning slot (-1 unmapped)
+};
+void launch_finalize(const FinalizeArgs& a, int grid, cudaStream_t st);
+
+// ---- index build ----
+void launch_build_csr_counts(const uint32_t* tab, uint64_t n, uint64_t npos, unsigned int* counts, int* err,
+                             cudaStream_t st);
+uint32_t host_unmix32(uint32_t h);
+void launch_build_csr_fill(const uint32_t* tab, uint64_t n, const unsigned long long* pos_in, uint64_t npos,
+                           const unsigned int* csr, unsigned long long* ent, const unsigned long long* clen,
+                           uint32_t ncontig, int* err, cudaStream_t st);
+
+}  // namespace pbw

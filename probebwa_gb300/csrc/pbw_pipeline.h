@@ -1,0 +1,131 @@
+// pbw_pipeline.h -- the handle and its device buffers.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/probebwa_gpu.h"
+#include "pbw_common.cuh"
+#include "pbw_kernels.h"
+#include "paired.h"
+
+namespace pbw {
+
+// Owned device allocation that only grows.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  ~DevBuf() { release(); }
+};
+
+// Pinned host staging that only grows.
+struct HostBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf&) = delete;
+  HostBuf& operator=(const HostBuf&) = delete;
+  bool ensure(size_t n) {
+    if (n <= cap) return true;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMallocHost(&p, n) != cudaSuccess) return false;
+    cap = n;
+    return true;
+  }
+  ~HostBuf() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+}  // namespace pbw
+
+struct pbw_handle {
+  std::string err;
+  pbw_options opt;
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t st = nullptr;
+  std::string species, assembly;
+  std::vector<std::string> names;
+  std::vector<uint64_t> lens;
+  uint64_t total_length = 0;
+  uint64_t seed_k = 15;
+  uint64_t n_ent = 0;
+  // index
+  pbw::DevBuf<unsigned long long> d_bits;
+  pbw::DevBuf<unsigned int> d_nmask;
+  pbw::DevBuf<unsigned long long> d_cbase, d_clen;
+  pbw::DevBuf<int> d_name_class;
+  pbw::DevBuf<unsigned int> d_csr;
+  pbw::DevBuf<unsigned long long> d_ent;
+  pbw::DevGenome G{};
+  pbw::DevIndex I{};
+  // parameter tables
+  pbw::DevTables tab_host{};
+  pbw::DevBuf<pbw::DevTables> d_tab;
+  pbw::DevBuf<double> d_ln_n, d_gc_lnb, d_gc_lnbm1;
+  pbw::DevBuf<int> d_err;
+  // inputs of a call
+  pbw::DevBuf<uint8_t> d_bases, d_quals, d_bases2, d_quals2;
+  pbw::DevBuf<uint64_t> d_offs, d_offs2;
+  // per-chunk work
+  pbw::DevBuf<unsigned long long> d_hits;
+  pbw::DevBuf<uint32_t> d_hit_cnt;
+  pbw::DevBuf<uint16_t> d_hit_rpos;
+  pbw::DevBuf<uint8_t> d_overflow, d_rep;
+  pbw::DevBuf<pbw::Cand> d_cand;
+  pbw::DevBuf<uint32_t> d_n_cand, d_total_cand;
+  pbw::DevBuf<pbw::AlnJob> d_jobs;
+  pbw::DevBuf<pbw::AlnOut> d_aln;
+  pbw::DevBuf<uint32_t> d_cig_pool;
+  pbw::DevBuf<unsigned int> d_cnt32;        // 0 n_jobs, 1 next_job, 2 cig_pool_used, 3 n_overflow, 4 cig_total
+  pbw::DevBuf<unsigned long long> d_cnt64;  // 0 probes, 1 entries, 2 hits, 3 dp jobs, 4 dp cells
+  pbw::DevBuf<unsigned int> d_scan_sums;
+  pbw::DevBuf<unsigned char> d_tb_global;
+  // outputs of a call
+  pbw::DevBuf<int32_t> o_contig, o_mate_contig, o_as, o_nm, o_best;
+  pbw::DevBuf<unsigned long long> o_pos, o_mate_pos;
+  pbw::DevBuf<long long> o_tlen;
+  pbw::DevBuf<uint8_t> o_mapq;
+  pbw::DevBuf<uint16_t> o_flag;
+  pbw::DevBuf<double> o_log_lk, o_post;
+  pbw::DevBuf<uint32_t> o_nops, o_cig_off, o_cigar;
+  // paired-end buffers
+  pbw::DevBuf<uint32_t> o_cig_off2, o_cigar2, o_len;
+  pbw::DevBuf<const pbw::AlnOut*> o_cigsrc;
+  pbw::DevBuf<pbw::Cand> d_cand2;
+  pbw::DevBuf<uint32_t> d_n_cand2;
+  pbw::DevBuf<pbw::AlnOut> d_aln2, d_xout;
+  pbw::DevBuf<uint8_t> d_rep2;
+  pbw::DevBuf<pbw::ReadSum> d_sum;
+  pbw::DevBuf<pbw::PairWork> d_work;
+  pbw::DevBuf<pbw::XMeta> d_xmeta;
+  pbw::DevBuf<pbw::PairModel> d_model;
+  pbw::DevBuf<double> d_obs;
+  pbw::DevBuf<pbw::AlnJob> d_xjobs;
+  pbw::HostBuf h_stage;
+  std::vector<cudaEvent_t> events;
+  pbw_stats stats{};
+  ~pbw_handle() {
+    for (auto e : events) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+namespace pbw {
+int pipeline_init(pbw_handle* h);
+}

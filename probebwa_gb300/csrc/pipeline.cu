@@ -1,0 +1,1083 @@
+// pipeline.cu -- the device pipeline behind pbw_map_single and the stage
+// entry points (include/probebwa_gpu.h).
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/probebwa_gpu.h"
+#include "pbw_common.cuh"
+#include "pbw_host.h"
+#include "pbw_kernels.h"
+#include "pbw_pipeline.h"
+#include "paired.h"
+
+namespace pbw {
+
+#define CK(call)                                                   \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) {                                       \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_); \
+      return PBW_ERR_CUDA;                                         \
+    }                                                              \
+  } while (0)
+#define TRY(x)                     \
+  do {                             \
+    int rc_ = (x);                 \
+    if (rc_ != PBW_OK) return rc_; \
+  } while (0)
+
+template <class T>
+static int grow(pbw_handle* h, DevBuf<T>& b, size_t n) {
+  if (n <= b.cap) return PBW_OK;
+  b.release();
+  size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void**)&b.p, bytes);
+  if (e != cudaSuccess) {
+    h->err = "cudaMalloc(" + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+    b.p = nullptr;
+    return PBW_ERR_NOMEM;
+  }
+  b.cap = n;
+  return PBW_OK;
+}
+
+int pipeline_init(pbw_handle* h) {
+  TRY(grow(h, h->d_cnt32, 16));
+  TRY(grow(h, h->d_cnt64, 16));
+  for (int i = 0; i < 32; i++) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    h->events.push_back(e);
+  }
+  return PBW_OK;
+}
+
+// Scratch sizing for one chunk.
+struct ChunkCfg {
+  uint32_t ch;      // reads per chunk
+  int lmax;
+  uint32_t hcap;
+  uint32_t wcap;
+  int nmax;         // longest reference window
+  size_t tb_smem;   // shared traceback bytes per warp
+  size_t tb_glob;   // global traceback bytes per warp (0 = none)
+};
+
+static ChunkCfg chunk_cfg(pbw_handle* h, uint64_t n, int lmax) {
+  ChunkCfg c;
+  c.ch = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(n, 1), h->opt.chunk_reads);
+  c.lmax = std::max(lmax, 1);
+  c.hcap = 4096;
+  c.wcap = (uint32_t)std::max(c.lmax - KMER + 1, 1);
+  const uint64_t rp = std::max<uint64_t>(h->opt.max_indel_len, 10);
+  c.nmax = (int)(c.lmax + 10 + rp);
+  const uint64_t band = h->opt.max_indel_len;
+  const size_t width = band <= 31 ? 2 * band + 1 : (size_t)c.nmax + 1;
+  const size_t need = (size_t)c.lmax * ((width + 7) / 8) * 4;
+  if (need <= 48 * 1024) {
+    c.tb_smem = need;
+    c.tb_glob = 0;
+  } else {
+    c.tb_smem = 0;
+    c.tb_glob = need;
+  }
+  return c;
+}
+
+static int ensure_chunk(pbw_handle* h, const ChunkCfg& c, int align_grid_warps) {
+  TRY(grow(h, h->d_hits, (size_t)c.ch * c.hcap));
+  TRY(grow(h, h->d_hit_cnt, c.ch));
+  TRY(grow(h, h->d_overflow, c.ch));
+  TRY(grow(h, h->d_rep, (size_t)c.ch * c.wcap));
+  TRY(grow(h, h->d_cand, (size_t)c.ch * MAX_CAND));
+  TRY(grow(h, h->d_n_cand, c.ch));
+  TRY(grow(h, h->d_total_cand, c.ch));
+  TRY(grow(h, h->d_jobs, (size_t)c.ch * MAX_CAND));
+  TRY(grow(h, h->d_aln, (size_t)c.ch * MAX_CAND));
+  TRY(grow(h, h->d_cig_pool, (size_t)c.ch * MAX_CAND * 24 + 4096));
+  TRY(grow(h, h->d_scan_sums, scan_blocks(c.ch) + 4));
+  if (c.tb_glob) TRY(grow(h, h->d_tb_global, c.tb_glob * (size_t)align_grid_warps));
+  if (h->opt.max_indel_len > 31)
+    TRY(grow(h, h->d_tb_global, wide_slab_bytes(c.lmax, c.nmax) * (size_t)h->num_sms * 16));
+  return PBW_OK;
+}
+
+static int ensure_outputs(pbw_handle* h, uint64_t n, uint64_t cig_cap) {
+  TRY(grow(h, h->o_contig, n));
+  TRY(grow(h, h->o_mate_contig, n));
+  TRY(grow(h, h->o_as, n));
+  TRY(grow(h, h->o_nm, n));
+  TRY(grow(h, h->o_best, n));
+  TRY(grow(h, h->o_pos, n));
+  TRY(grow(h, h->o_mate_pos, n));
+  TRY(grow(h, h->o_tlen, n));
+  TRY(grow(h, h->o_mapq, n));
+  TRY(grow(h, h->o_flag, n));
+  TRY(grow(h, h->o_log_lk, n));
+  TRY(grow(h, h->o_post, n));
+  TRY(grow(h, h->o_nops, n));
+  TRY(grow(h, h->o_cig_off, n + 1));
+  TRY(grow(h, h->o_cigar, cig_cap));
+  return PBW_OK;
+}
+
+static int align_grid(pbw_handle* h, int lmax, int nmax, size_t tb_smem) {
+  size_t per_block = align_smem_per_warp(lmax, nmax, tb_smem) * 4;
+  int bps = (int)std::max<size_t>(1, std::min<size_t>(8, (h->smem_optin ? 228 * 1024 : 100 * 1024) / per_block));
+  return h->num_sms * bps;
+}
+
+struct Timer {
+  pbw_handle* h;
+  int next = 0;
+  cudaEvent_t mark() {
+    cudaEvent_t e = h->events[next++ % h->events.size()];
+    cudaEventRecord(e, h->st);
+    return e;
+  }
+};
+
+static double ms_between(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+// Buffers receiving one read set's candidates and seeded alignments.
+struct MateBufs {
+  Cand* cand;
+  uint32_t* n_cand;
+  AlnOut* aln;
+  uint8_t* rep;
+  uint8_t mate;
+};
+
+// K1 -> K2 -> jobs -> K3 for reads [r0, r0+nr) of one read set. Events
+// ev[0..3] mark seed / cluster / align boundaries. reset_pool clears the
+// CIGAR pool (the first read set of a chunk).
+static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
+                          const uint64_t* offs, uint32_t r0, uint32_t nr, int grid_align, const MateBufs& mb,
+                          cudaEvent_t* ev, bool reset_pool) {
+  cudaStream_t st = h->st;
+  unsigned int* c32 = h->d_cnt32.p;
+  CK(cudaMemsetAsync(c32, 0, (reset_pool ? 3 : 2) * sizeof(unsigned int), st));  // n_jobs, next_job[, cig_pool_used]
+  CK(cudaMemsetAsync(mb.n_cand, 0, nr * sizeof(uint32_t), st));
+  CK(cudaEventRecord(ev[0], st));
+  SeedArgs sa{};
+  sa.G = h->G;
+  sa.idx = h->I;
+  sa.bases = bases;
+  sa.offs = offs;
+  sa.r0 = r0;
+  sa.nr = nr;
+  sa.lmax = cfg.lmax;
+  sa.hits = h->d_hits.p;
+  sa.hcap = cfg.hcap;
+  sa.hit_cnt = h->d_hit_cnt.p;
+  sa.overflow = h->d_overflow.p;
+  sa.n_overflow = c32 + 3;
+  sa.rep = mb.rep;
+  sa.wcap = cfg.wcap;
+  sa.hit_rpos = nullptr;
+  sa.counters = h->d_cnt64.p;
+  {
+    size_t sm = seed_smem_per_warp(cfg.lmax) * 8;
+    int bps = (int)std::max<size_t>(1, std::min<size_t>(8, (228 * 1024) / std::max<size_t>(sm, 1)));
+    launch_seed(sa, h->num_sms * bps, st);
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ev[1], st));
+  ClusterArgs ca{};
+  ca.hits = h->d_hits.p;
+  ca.hit_cnt = h->d_hit_cnt.p;
+  ca.overflow = h->d_overflow.p;
+  ca.hcap = cfg.hcap;
+  ca.offs = offs;
+  ca.r0 = r0;
+  ca.nr = nr;
+  ca.group_width = h->opt.group_width;
+  ca.max_out = MAX_CAND;
+  ca.cand = mb.cand;
+  ca.n_cand = mb.n_cand;
+  ca.total_cand = h->d_total_cand.p;
+  ca.err = h->d_err.p;
+  ca.h_lo = 0;
+  ca.h_hi = 512;
+  launch_cluster(ca, 512, 64, st);
+  ca.h_lo = 512;
+  ca.h_hi = cfg.hcap;
+  launch_cluster(ca, cfg.hcap, 256, st);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ev[2], st));
+  MakeJobsArgs ma{};
+  ma.G = h->G;
+  ma.offs = offs;
+  ma.r0 = r0;
+  ma.nr = nr;
+  ma.cand = mb.cand;
+  ma.n_cand = mb.n_cand;
+  ma.right_pad = std::max<uint64_t>(h->opt.max_indel_len, 10);
+  ma.band = (uint32_t)h->opt.max_indel_len;
+  ma.gap_open = h->tab_host.gap_open;
+  ma.gap_extend = h->tab_host.gap_extend;
+  ma.jobs = h->d_jobs.p;
+  ma.n_jobs = c32 + 0;
+  ma.out = mb.aln;
+  ma.mate = 0;
+  launch_make_jobs_single(ma, st);
+  AlignArgs aa{};
+  aa.G = h->G;
+  aa.tab = h->d_tab.p;
+  aa.gc_lnb = h->d_gc_lnb.p;
+  aa.gc_lnbm1 = h->d_gc_lnbm1.p;
+  aa.bases = bases;
+  aa.quals = quals;
+  aa.offs = offs;
+  aa.bases2 = bases;
+  aa.quals2 = quals;
+  aa.offs2 = offs;
+  aa.jobs = h->d_jobs.p;
+  aa.n_jobs = c32 + 0;
+  aa.next_job = c32 + 1;
+  aa.out = mb.aln;
+  aa.cig_pool = h->d_cig_pool.p;
+  aa.cig_pool_used = c32 + 2;
+  aa.cig_pool_cap = (uint32_t)h->d_cig_pool.cap;
+  aa.ref_bytes = nullptr;
+  aa.lmax = cfg.lmax;
+  aa.nmax = cfg.nmax;
+  aa.tb_smem = cfg.tb_smem;
+  aa.tb_global = h->d_tb_global.p;
+  aa.tb_global_per_warp = cfg.tb_glob;
+  aa.counters = h->d_cnt64.p + 3;
+  aa.err = h->d_err.p;
+  if (h->opt.max_indel_len <= 31) {
+    launch_align(aa, grid_align, st);
+  } else {
+    aa.tb_smem = 0;
+    aa.tb_global = h->d_tb_global.p;
+    aa.tb_global_per_warp = wide_slab_bytes(cfg.lmax, cfg.nmax);
+    launch_align_wide(aa, h->num_sms * 4, st);
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ev[3], st));
+  h->stats.kernel_launches += 6;
+  return PBW_OK;
+}
+
+// One chunk of single-end reads: seeding through finalize and CIGAR gather.
+// Per-phase event pairs are recorded into ev (5 phases).
+static int run_chunk_single(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
+                            const uint64_t* offs, uint32_t r0, uint32_t nr, int grid_align, cudaEvent_t* ev) {
+  cudaStream_t st = h->st;
+  unsigned int* c32 = h->d_cnt32.p;
+  MateBufs mb{h->d_cand.p, h->d_n_cand.p, h->d_aln.p, h->d_rep.p, 0};
+  TRY(run_seed_align(h, cfg, bases, quals, offs, r0, nr, grid_align, mb, ev, true));
+  FinalizeArgs fa{};
+  fa.G = h->G;
+  fa.tab = h->d_tab.p;
+  fa.ln_n = h->d_ln_n.p;
+  fa.quals = quals;
+  fa.offs = offs;
+  fa.r0 = r0;
+  fa.nr = nr;
+  fa.aln = h->d_aln.p;
+  fa.n_cand = h->d_n_cand.p;
+  fa.cand = h->d_cand.p;
+  fa.rep = h->d_rep.p;
+  fa.wcap = cfg.wcap;
+  fa.gc_lnb = h->d_gc_lnb.p;
+  fa.gc_lnbm1 = h->d_gc_lnbm1.p;
+  fa.seed_k = h->seed_k;
+  fa.contig = h->o_contig.p + r0;
+  fa.pos = h->o_pos.p + r0;
+  fa.mapq = h->o_mapq.p + r0;
+  fa.flag = h->o_flag.p + r0;
+  fa.log_lk = h->o_log_lk.p + r0;
+  fa.posterior = h->o_post.p + r0;
+  fa.as_score = h->o_as.p + r0;
+  fa.nm = h->o_nm.p + r0;
+  fa.n_ops = h->o_nops.p + r0;
+  fa.best = h->o_best.p + r0;
+  launch_finalize(fa, 0, st);
+  launch_scan_excl(h->o_nops.p + r0, nr, h->o_cig_off.p + r0, h->d_scan_sums.p, c32 + 4, c32 + 4, st);
+  CigarGatherArgs ga{};
+  ga.offs = offs;
+  ga.r0 = r0;
+  ga.nr = nr;
+  ga.best = h->o_best.p + r0;
+  ga.aln = h->d_aln.p;
+  ga.cig_pool = h->d_cig_pool.p;
+  ga.cig_off = h->o_cig_off.p + r0;
+  ga.cigar = h->o_cigar.p;
+  launch_cigar_gather(ga, st);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ev[4], st));
+  h->stats.kernel_launches += 4;
+  return PBW_OK;
+}
+
+static int check_device_errors(pbw_handle* h) {
+  int err = 0;
+  unsigned int c32[8];
+  CK(cudaMemcpy(&err, h->d_err.p, 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(c32, h->d_cnt32.p, sizeof(c32), cudaMemcpyDeviceToHost));
+  if (c32[3]) {
+    h->err = std::to_string(c32[3]) + " read(s) produced more seed hits than the per-read capacity";
+    CK(cudaMemset(h->d_cnt32.p + 3, 0, 4));
+    return PBW_ERR_LIMIT;
+  }
+  if (err) {
+    h->err = "device kernel reported internal error " + std::to_string(err);
+    CK(cudaMemset(h->d_err.p, 0, 4));
+    return PBW_ERR_DEVICE;
+  }
+  return PBW_OK;
+}
+
+static int copy_records_out(pbw_handle* h, uint64_t n, pbw_records* out, bool paired_fields) {
+  unsigned int total = 0;
+  CK(cudaMemcpy(&total, h->d_cnt32.p + 4, 4, cudaMemcpyDeviceToHost));
+  if (out->cigar_cap < total) {
+    h->err = "cigar_cap " + std::to_string(out->cigar_cap) + " < " + std::to_string(total);
+    return PBW_ERR_CAPACITY;
+  }
+  cudaStream_t st = h->st;
+  CK(cudaMemcpyAsync(h->o_cig_off.p + n, h->d_cnt32.p + 4, 4, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(out->contig, h->o_contig.p, n * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->pos, h->o_pos.p, n * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->mapq, h->o_mapq.p, n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->flag, h->o_flag.p, n * 2, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->log_lk, h->o_log_lk.p, n * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->posterior, h->o_post.p, n * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->as_score, h->o_as.p, n * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->nm, h->o_nm.p, n * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->cigar_off, h->o_cig_off.p, (n + 1) * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(out->cigar, h->o_cigar.p, (size_t)total * 4, cudaMemcpyDeviceToHost, st));
+  if (paired_fields) {
+    CK(cudaMemcpyAsync(out->mate_contig, h->o_mate_contig.p, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(out->mate_pos, h->o_mate_pos.p, n * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(out->tlen, h->o_tlen.p, n * 8, cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  if (!paired_fields) {
+    for (uint64_t i = 0; i < n; i++) {
+      out->mate_contig[i] = -1;
+      out->mate_pos[i] = 0;
+      out->tlen[i] = 0;
+    }
+  }
+  return PBW_OK;
+}
+
+static int validate_reads(pbw_handle* h, const pbw_reads* r, uint64_t& total, int& lmax) {
+  if (!r || (r->n && (!r->offsets))) { h->err = "null reads"; return PBW_ERR_ARG; }
+  lmax = 0;
+  total = r->n ? r->offsets[r->n] - r->offsets[0] : 0;
+  if (r->n && r->offsets[0] != 0) { h->err = "offsets[0] must be 0"; return PBW_ERR_ARG; }
+  for (uint64_t i = 0; i < r->n; i++) {
+    if (r->offsets[i + 1] < r->offsets[i]) { h->err = "offsets must be non-decreasing"; return PBW_ERR_ARG; }
+    uint64_t L = r->offsets[i + 1] - r->offsets[i];
+    if (L > PBW_MAX_READ_LEN) {
+      h->err = "read " + std::to_string(i) + " longer than PBW_MAX_READ_LEN";
+      return PBW_ERR_LIMIT;
+    }
+    lmax = std::max(lmax, (int)L);
+  }
+  if (r->n >= (1ull << 31)) { h->err = "too many reads in one call"; return PBW_ERR_LIMIT; }
+  return PBW_OK;
+}
+
+// Map reads whose bases/quals/offsets are already on the device.
+static int map_single_dev(pbw_handle* h, const uint8_t* d_bases, const uint8_t* d_quals, const uint64_t* d_offs,
+                          uint64_t n, uint64_t total_bases, int lmax, pbw_records* out) {
+  ChunkCfg cfg = chunk_cfg(h, n, lmax);
+  int grid = align_grid(h, cfg.lmax, cfg.nmax, cfg.tb_smem);
+  TRY(ensure_chunk(h, cfg, grid * 4));
+  TRY(ensure_outputs(h, std::max<uint64_t>(n, 1), 2 * total_bases + 2 * n + 16));
+  CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * sizeof(unsigned int), h->st));
+  CK(cudaMemsetAsync(h->d_cnt64.p, 0, 16 * sizeof(unsigned long long), h->st));
+  std::vector<std::vector<cudaEvent_t>> evs;
+  double t_seed = 0, t_cl = 0, t_al = 0, t_fin = 0;
+  cudaEvent_t e0 = h->events[0], e1 = h->events[1];
+  CK(cudaEventRecord(e0, h->st));
+  int ev_next = 2;
+  for (uint64_t r0 = 0; r0 < n; r0 += cfg.ch) {
+    uint32_t nr = (uint32_t)std::min<uint64_t>(cfg.ch, n - r0);
+    cudaEvent_t* ev = &h->events[ev_next];
+    TRY(run_chunk_single(h, cfg, d_bases, d_quals, d_offs, (uint32_t)r0, nr, grid, ev));
+    // accumulate phase times once the chunk's events complete (next sync)
+    CK(cudaEventSynchronize(ev[4]));
+    t_seed += ms_between(ev[0], ev[1]);
+    t_cl += ms_between(ev[1], ev[2]);
+    t_al += ms_between(ev[2], ev[3]);
+    t_fin += ms_between(ev[3], ev[4]);
+  }
+  CK(cudaEventRecord(e1, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  TRY(check_device_errors(h));
+  h->stats.ms_seed = t_seed;
+  h->stats.ms_cluster = t_cl;
+  h->stats.ms_align = t_al;
+  h->stats.ms_finalize = t_fin;
+  unsigned long long c64[8];
+  CK(cudaMemcpy(c64, h->d_cnt64.p, sizeof(c64), cudaMemcpyDeviceToHost));
+  h->stats.seed_probes = c64[0];
+  h->stats.seed_entries = c64[1];
+  h->stats.seed_hits = c64[2];
+  h->stats.dp_jobs = c64[3];
+  h->stats.dp_cells = c64[4];
+  cudaEvent_t e2 = h->events[ev_next + 5];
+  TRY(copy_records_out(h, n, out, false));
+  CK(cudaEventRecord(e2, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->stats.ms_d2h = ms_between(e1, e2);
+  return PBW_OK;
+}
+
+static int upload_reads(pbw_handle* h, const pbw_reads* r, uint64_t total, DevBuf<uint8_t>& db, DevBuf<uint8_t>& dq,
+                        DevBuf<uint64_t>& doff) {
+  TRY(grow(h, db, total + 16));
+  TRY(grow(h, dq, total + 16));
+  TRY(grow(h, doff, r->n + 1));
+  if (total) {
+    CK(cudaMemcpyAsync(db.p, r->bases, total, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(dq.p, r->quals, total, cudaMemcpyHostToDevice, h->st));
+  }
+  CK(cudaMemcpyAsync(doff.p, r->offsets, (r->n + 1) * 8, cudaMemcpyHostToDevice, h->st));
+  return PBW_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// paired end
+// ---------------------------------------------------------------------------
+// The schedule of map_paired (src/lib.rs:145-185): pairs 0..499 one at a
+// time with the model updated after each, then batches of 2000 against a
+// frozen snapshot, observations folded in pair order after each batch.
+static std::vector<std::pair<uint64_t, uint64_t>> pair_batches(uint64_t n) {
+  std::vector<std::pair<uint64_t, uint64_t>> b;
+  const uint64_t warm = std::min<uint64_t>(n, 500);
+  for (uint64_t i = 0; i < warm; i++) b.push_back({i, 1});
+  for (uint64_t s = warm; s < n; s += 2000) b.push_back({s, std::min<uint64_t>(2000, n - s)});
+  return b;
+}
+
+static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t* b1, const uint8_t* q1,
+                          const uint64_t* of1, const uint8_t* b2, const uint8_t* q2, const uint64_t* of2, uint64_t n,
+                          uint64_t tot1, uint64_t tot2, int lmax, pbw_records* o1, pbw_records* o2) {
+  cudaStream_t st = h->st;
+  const auto batches = pair_batches(n);
+  // super-chunks: whole batches, at most chunk_reads pairs
+  const uint64_t S = std::max<uint64_t>(h->opt.chunk_reads, 2000);
+  ChunkCfg cfg = chunk_cfg(h, std::min<uint64_t>(n, S), lmax);
+  cfg.ch = (uint32_t)std::min<uint64_t>(n, S);
+  const int grid_s = align_grid(h, cfg.lmax, cfg.nmax, cfg.tb_smem);
+  TRY(ensure_chunk(h, cfg, grid_s * 4));
+  const uint32_t ch = cfg.ch;
+  TRY(grow(h, h->d_cand2, (size_t)ch * MAX_CAND));
+  TRY(grow(h, h->d_n_cand2, ch));
+  TRY(grow(h, h->d_aln2, (size_t)ch * MAX_CAND));
+  TRY(grow(h, h->d_rep2, (size_t)ch * cfg.wcap));
+  TRY(grow(h, h->d_sum, 2 * (size_t)ch));
+  TRY(grow(h, h->d_work, ch));
+  TRY(grow(h, h->d_xout, (size_t)ch * MAX_CROSS));
+  TRY(grow(h, h->d_xmeta, (size_t)ch * MAX_CROSS));
+  TRY(grow(h, h->d_xjobs, (size_t)2000 * MAX_CROSS));
+  TRY(grow(h, h->d_obs, ch));
+  TRY(grow(h, h->d_model, 1));
+  TRY(grow(h, h->d_cig_pool, (size_t)ch * (2 * MAX_CAND + MAX_CROSS) * 16 + 4096));
+  const uint64_t n2 = 2 * n;
+  TRY(ensure_outputs(h, std::max<uint64_t>(n2, 1), 2 * tot1 + 2 * n + 16));
+  TRY(grow(h, h->o_cig_off2, n + 1));
+  TRY(grow(h, h->o_cigar2, 2 * tot2 + 2 * n + 16));
+  TRY(grow(h, h->o_cigsrc, std::max<uint64_t>(n2, 1)));
+  TRY(grow(h, h->o_len, std::max<uint64_t>(n2, 1)));
+  // wide DP: window = L + 2 * (ceil(5 sd) + L); slabs sized for 8192 columns
+  const int wide_n = 8192;
+  const int grid_w = h->num_sms * 4;
+  const size_t slab = wide_slab_bytes(cfg.lmax, wide_n);
+  TRY(grow(h, h->d_tb_global, slab * (size_t)grid_w * 4));
+  PairModel pm;
+  pm.mean = model->mean;
+  pm.sd = model->sd;
+  pm.n = model->n_observed;
+  pm.ln_2pi_sd2 = std::log(2.0 * 3.141592653589793 * pm.sd * pm.sd);
+  CK(cudaMemcpyAsync(h->d_model.p, &pm, sizeof(pm), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * sizeof(unsigned int), st));
+  CK(cudaMemsetAsync(h->d_cnt64.p, 0, 16 * sizeof(unsigned long long), st));
+  cudaEvent_t* ev = &h->events[2];
+  double t_seed = 0, t_cl = 0, t_al = 0, t_pair = 0, t_fin = 0;
+  size_t bi = 0;
+  while (bi < batches.size()) {
+    const uint64_t a = batches[bi].first;
+    size_t be = bi;
+    uint64_t b = a;
+    while (be < batches.size() && batches[be].first + batches[be].second - a <= S) {
+      b = batches[be].first + batches[be].second;
+      be++;
+    }
+    const uint32_t nr = (uint32_t)(b - a);
+    // phase A: both mates through K1-K3 and the per-read summaries
+    MateBufs m1{h->d_cand.p, h->d_n_cand.p, h->d_aln.p, h->d_rep.p, 0};
+    MateBufs m2{h->d_cand2.p, h->d_n_cand2.p, h->d_aln2.p, h->d_rep2.p, 0};
+    TRY(run_seed_align(h, cfg, b1, q1, of1, (uint32_t)a, nr, grid_s, m1, ev, true));
+    CK(cudaEventSynchronize(ev[3]));
+    t_seed += ms_between(ev[0], ev[1]);
+    t_cl += ms_between(ev[1], ev[2]);
+    t_al += ms_between(ev[2], ev[3]);
+    TRY(run_seed_align(h, cfg, b2, q2, of2, (uint32_t)a, nr, grid_s, m2, ev, false));
+    CK(cudaEventSynchronize(ev[3]));
+    t_seed += ms_between(ev[0], ev[1]);
+    t_cl += ms_between(ev[1], ev[2]);
+    t_al += ms_between(ev[2], ev[3]);
+    CK(cudaEventRecord(ev[0], st));
+    for (int mate = 0; mate < 2; mate++) {
+      ReadSummaryArgs ra{};
+      ra.tab = h->d_tab.p;
+      ra.ln_n = h->d_ln_n.p;
+      ra.gc_lnb = h->d_gc_lnb.p;
+      ra.gc_lnbm1 = h->d_gc_lnbm1.p;
+      ra.quals = mate ? q2 : q1;
+      ra.offs = mate ? of2 : of1;
+      ra.r0 = (uint32_t)a;
+      ra.nr = nr;
+      ra.aln = mate ? h->d_aln2.p : h->d_aln.p;
+      ra.n_cand = mate ? h->d_n_cand2.p : h->d_n_cand.p;
+      ra.rep = mate ? h->d_rep2.p : h->d_rep.p;
+      ra.wcap = cfg.wcap;
+      ra.sum = h->d_sum.p + (size_t)mate * ch;
+      launch_read_summary(ra, st);
+    }
+    // phase B: batches
+    PairArgs pa{};
+    pa.G = h->G;
+    pa.tab = h->d_tab.p;
+    pa.ln_n = h->d_ln_n.p;
+    pa.gc_lnb = h->d_gc_lnb.p;
+    pa.gc_lnbm1 = h->d_gc_lnbm1.p;
+    pa.offs1 = of1;
+    pa.offs2 = of2;
+    pa.read0 = (uint32_t)a;
+    pa.sum[0] = h->d_sum.p;
+    pa.sum[1] = h->d_sum.p + ch;
+    pa.aln[0] = h->d_aln.p;
+    pa.aln[1] = h->d_aln2.p;
+    pa.cand[0] = h->d_cand.p;
+    pa.cand[1] = h->d_cand2.p;
+    pa.work = h->d_work.p;
+    pa.model = h->d_model.p;
+    pa.sv_prior_log_prob = h->tab_host.sv_prior_log_prob;
+    pa.gap_open = h->tab_host.gap_open;
+    pa.gap_extend = h->tab_host.gap_extend;
+    pa.jobs = h->d_xjobs.p;
+    pa.n_jobs = h->d_cnt32.p + 8;
+    pa.xout = h->d_xout.p;
+    pa.xmeta = h->d_xmeta.p;
+    pa.obs = h->d_obs.p;
+    pa.out_base = a;
+    pa.n_total = n;
+    pa.o_contig = h->o_contig.p;
+    pa.o_pos = h->o_pos.p;
+    pa.o_mapq = h->o_mapq.p;
+    pa.o_flag = h->o_flag.p;
+    pa.o_mate_contig = h->o_mate_contig.p;
+    pa.o_mate_pos = h->o_mate_pos.p;
+    pa.o_tlen = h->o_tlen.p;
+    pa.o_log_lk = h->o_log_lk.p;
+    pa.o_post = h->o_post.p;
+    pa.o_as = h->o_as.p;
+    pa.o_nm = h->o_nm.p;
+    pa.o_nops = h->o_nops.p;
+    pa.o_cigsrc = h->o_cigsrc.p;
+    pa.o_len = h->o_len.p;
+    AlignArgs aa{};
+    aa.G = h->G;
+    aa.tab = h->d_tab.p;
+    aa.gc_lnb = h->d_gc_lnb.p;
+    aa.gc_lnbm1 = h->d_gc_lnbm1.p;
+    aa.bases = b1;
+    aa.quals = q1;
+    aa.offs = of1;
+    aa.bases2 = b2;
+    aa.quals2 = q2;
+    aa.offs2 = of2;
+    aa.jobs = h->d_xjobs.p;
+    aa.n_jobs = h->d_cnt32.p + 8;
+    aa.next_job = h->d_cnt32.p + 9;
+    aa.out = h->d_xout.p;
+    aa.cig_pool = h->d_cig_pool.p;
+    aa.cig_pool_used = h->d_cnt32.p + 2;
+    aa.cig_pool_cap = (uint32_t)h->d_cig_pool.cap;
+    aa.ref_bytes = nullptr;
+    aa.lmax = cfg.lmax;
+    aa.nmax = wide_n;
+    aa.tb_smem = 0;
+    aa.tb_global = h->d_tb_global.p;
+    aa.tb_global_per_warp = slab;
+    aa.counters = h->d_cnt64.p + 3;
+    aa.err = h->d_err.p;
+    for (size_t k = bi; k < be; k++) {
+      pa.p0 = (uint32_t)(batches[k].first - a);
+      pa.np = (uint32_t)batches[k].second;
+      CK(cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st));
+      launch_pair_decide(pa, st);
+      const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, ((uint64_t)pa.np * MAX_CROSS + 3) / 4);
+      launch_align_wide(aa, std::max(gw, 1), st);
+      launch_pair_resolve(pa, st);
+      launch_fold_model(h->d_model.p, h->d_obs.p, pa.p0, pa.np, st);
+      h->stats.kernel_launches += 4;
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ev[1], st));
+    // packed CIGARs of this super-chunk's records, mate 1 then mate 2
+    launch_scan_excl(h->o_nops.p + a, nr, h->o_cig_off.p + a, h->d_scan_sums.p, h->d_cnt32.p + 4, h->d_cnt32.p + 4,
+                     st);
+    launch_pair_cigar_gather(pa, h->o_cig_off.p, h->d_cig_pool.p, h->o_cigar.p, a, nr, st);
+    // mate 2 records live at n + pair; their offsets go to o_cig_off2
+    {
+      PairArgs pb = pa;
+      pb.o_cigsrc = h->o_cigsrc.p + n;
+      pb.o_len = h->o_len.p + n;
+      launch_scan_excl(h->o_nops.p + n + a, nr, h->o_cig_off2.p + a, h->d_scan_sums.p, h->d_cnt32.p + 5,
+                       h->d_cnt32.p + 5, st);
+      launch_pair_cigar_gather(pb, h->o_cig_off2.p, h->d_cig_pool.p, h->o_cigar2.p, a, nr, st);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ev[2], st));
+    CK(cudaEventSynchronize(ev[2]));
+    t_pair += ms_between(ev[0], ev[1]);
+    t_fin += ms_between(ev[1], ev[2]);
+    bi = be;
+  }
+  CK(cudaStreamSynchronize(st));
+  TRY(check_device_errors(h));
+  h->stats.ms_seed = t_seed;
+  h->stats.ms_cluster = t_cl;
+  h->stats.ms_align = t_al;
+  h->stats.ms_pair = t_pair;
+  h->stats.ms_finalize = t_fin;
+  unsigned long long c64[8];
+  CK(cudaMemcpy(c64, h->d_cnt64.p, sizeof(c64), cudaMemcpyDeviceToHost));
+  h->stats.seed_probes = c64[0];
+  h->stats.seed_entries = c64[1];
+  h->stats.seed_hits = c64[2];
+  h->stats.dp_jobs = c64[3];
+  h->stats.dp_cells = c64[4];
+  // outputs
+  unsigned int tot[2];
+  CK(cudaMemcpy(tot, h->d_cnt32.p + 4, 8, cudaMemcpyDeviceToHost));
+  if (o1->cigar_cap < tot[0] || o2->cigar_cap < tot[1]) {
+    h->err = "cigar_cap too small";
+    return PBW_ERR_CAPACITY;
+  }
+  cudaEvent_t e1 = h->events[20], e2 = h->events[21];
+  CK(cudaEventRecord(e1, st));
+  CK(cudaMemcpyAsync(h->o_cig_off.p + n, h->d_cnt32.p + 4, 4, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(h->o_cig_off2.p + n, h->d_cnt32.p + 5, 4, cudaMemcpyDeviceToDevice, st));
+  pbw_records* outs[2] = {o1, o2};
+  for (int k = 0; k < 2; k++) {
+    pbw_records* o = outs[k];
+    const uint64_t g = (uint64_t)k * n;
+    CK(cudaMemcpyAsync(o->contig, h->o_contig.p + g, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->pos, h->o_pos.p + g, n * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->mapq, h->o_mapq.p + g, n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->flag, h->o_flag.p + g, n * 2, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->mate_contig, h->o_mate_contig.p + g, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->mate_pos, h->o_mate_pos.p + g, n * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->tlen, h->o_tlen.p + g, n * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->log_lk, h->o_log_lk.p + g, n * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->posterior, h->o_post.p + g, n * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->as_score, h->o_as.p + g, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->nm, h->o_nm.p + g, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(o->cigar_off, (k ? h->o_cig_off2.p : h->o_cig_off.p), (n + 1) * 4, cudaMemcpyDeviceToHost,
+                       st));
+    CK(cudaMemcpyAsync(o->cigar, (k ? h->o_cigar2.p : h->o_cigar.p), (size_t)tot[k] * 4, cudaMemcpyDeviceToHost,
+                       st));
+  }
+  CK(cudaMemcpyAsync(&pm, h->d_model.p, sizeof(pm), cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(e2, st));
+  CK(cudaStreamSynchronize(st));
+  h->stats.ms_d2h = ms_between(e1, e2);
+  model->mean = pm.mean;
+  model->sd = pm.sd;
+  model->n_observed = pm.n;
+  return PBW_OK;
+}
+}  // namespace pbw
+
+using namespace pbw;
+
+extern "C" {
+
+int pbw_map_single(pbw_handle* h, const pbw_reads* reads, pbw_records* out) {
+  if (!h || !reads || !out) return PBW_ERR_ARG;
+  if (out->n < reads->n) { h->err = "records array smaller than reads"; return PBW_ERR_CAPACITY; }
+  cudaSetDevice(h->device);
+  h->stats = pbw_stats{};
+  uint64_t total;
+  int lmax;
+  TRY(validate_reads(h, reads, total, lmax));
+  if (reads->n == 0) {
+    if (out->cigar_off) out->cigar_off[0] = 0;
+    return PBW_OK;
+  }
+  cudaEvent_t a = h->events[30], b = h->events[31];
+  CK(cudaEventRecord(a, h->st));
+  TRY(upload_reads(h, reads, total, h->d_bases, h->d_quals, h->d_offs));
+  CK(cudaEventRecord(b, h->st));
+  TRY(map_single_dev(h, h->d_bases.p, h->d_quals.p, h->d_offs.p, reads->n, total, lmax, out));
+  h->stats.ms_h2d = ms_between(a, b);
+  h->stats.ms_total = h->stats.ms_h2d + h->stats.ms_seed + h->stats.ms_cluster + h->stats.ms_align +
+                      h->stats.ms_finalize + h->stats.ms_d2h;
+  return PBW_OK;
+}
+
+
+int pbw_map_paired(pbw_handle* h, pbw_insert_model* model, const pbw_reads* r1, const pbw_reads* r2,
+                   pbw_records* o1, pbw_records* o2) {
+  if (!h || !model || !r1 || !r2 || !o1 || !o2) return PBW_ERR_ARG;
+  cudaSetDevice(h->device);
+  h->stats = pbw_stats{};
+  if (r1->n != r2->n) {
+    h->err = "paired-end inputs have different read counts (" + std::to_string(r1->n) + " vs " +
+             std::to_string(r2->n) + ")";
+    return PBW_ERR_ARG;
+  }
+  if (o1->n < r1->n || o2->n < r2->n) { h->err = "records array smaller than reads"; return PBW_ERR_CAPACITY; }
+  uint64_t t1, t2;
+  int l1, l2;
+  TRY(validate_reads(h, r1, t1, l1));
+  TRY(validate_reads(h, r2, t2, l2));
+  const uint64_t n = r1->n;
+  if (n == 0) {
+    if (o1->cigar_off) o1->cigar_off[0] = 0;
+    if (o2->cigar_off) o2->cigar_off[0] = 0;
+    return PBW_OK;
+  }
+  cudaEvent_t a = h->events[30], b = h->events[31];
+  CK(cudaEventRecord(a, h->st));
+  TRY(upload_reads(h, r1, t1, h->d_bases, h->d_quals, h->d_offs));
+  TRY(upload_reads(h, r2, t2, h->d_bases2, h->d_quals2, h->d_offs2));
+  CK(cudaEventRecord(b, h->st));
+  TRY(map_paired_dev(h, model, h->d_bases.p, h->d_quals.p, h->d_offs.p, h->d_bases2.p, h->d_quals2.p,
+                     h->d_offs2.p, n, t1, t2, std::max(l1, l2), o1, o2));
+  h->stats.ms_h2d = ms_between(a, b);
+  h->stats.ms_total = h->stats.ms_h2d + h->stats.ms_seed + h->stats.ms_cluster + h->stats.ms_align +
+                      h->stats.ms_pair + h->stats.ms_finalize + h->stats.ms_d2h;
+  return PBW_OK;
+}
+
+int pbw_map_single_device(pbw_handle* h, const pbw_reads* dev_reads, pbw_records* out) {
+  if (!h || !dev_reads || !out) return PBW_ERR_ARG;
+  cudaSetDevice(h->device);
+  h->stats = pbw_stats{};
+  const uint64_t n = dev_reads->n;
+  if (out->n < n) { h->err = "records array smaller than reads"; return PBW_ERR_CAPACITY; }
+  if (n == 0) return PBW_OK;
+  // read lengths are needed for sizing: one small copy of the offsets
+  std::vector<uint64_t> offs(n + 1);
+  CK(cudaMemcpy(offs.data(), dev_reads->offsets, (n + 1) * 8, cudaMemcpyDeviceToHost));
+  pbw_reads hr{n, nullptr, nullptr, offs.data()};
+  uint64_t total;
+  int lmax;
+  TRY(validate_reads(h, &hr, total, lmax));
+  TRY(map_single_dev(h, dev_reads->bases, dev_reads->quals, dev_reads->offsets, n, total, lmax, out));
+  h->stats.ms_total = h->stats.ms_seed + h->stats.ms_cluster + h->stats.ms_align + h->stats.ms_finalize +
+                      h->stats.ms_d2h;
+  return PBW_OK;
+}
+
+int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8_t* quals, const uint64_t* read_off,
+                    const uint8_t* refs, const uint64_t* ref_off, const int64_t* hint, const uint64_t* band,
+                    int32_t* score, uint64_t* offset, uint32_t* cigar_off, uint32_t* cigar, uint64_t cigar_cap) {
+  if (!h) return PBW_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (n == 0) {
+    if (cigar_off) cigar_off[0] = 0;
+    return PBW_OK;
+  }
+  const uint64_t qtot = read_off[n], rtot = ref_off[n];
+  int lmax = 0, nmax = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    lmax = std::max<int>(lmax, (int)(read_off[i + 1] - read_off[i]));
+    nmax = std::max<int>(nmax, (int)(ref_off[i + 1] - ref_off[i]));
+  }
+  if (lmax > PBW_MAX_READ_LEN || nmax > 16384) { h->err = "problem larger than the device limits"; return PBW_ERR_LIMIT; }
+  TRY(grow(h, h->d_bases, qtot + 16));
+  TRY(grow(h, h->d_quals, qtot + 16));
+  TRY(grow(h, h->d_offs, n + 1));
+  TRY(grow(h, h->d_bases2, rtot + 16));
+  TRY(grow(h, h->d_jobs, n));
+  TRY(grow(h, h->d_aln, n));
+  TRY(grow(h, h->d_cig_pool, (size_t)(qtot + rtot) * 2 + 64));
+  CK(cudaMemcpy(h->d_bases.p, reads, qtot, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_quals.p, quals, qtot, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_offs.p, read_off, (n + 1) * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_bases2.p, refs, rtot, cudaMemcpyHostToDevice));
+  // band <= 31: row-strip kernel with shared traceback; wider: column tiles
+  std::vector<AlnJob> js, jw;
+  int lmax_s = 1, nmax_s = 1, lmax_w = 1, nmax_w = 1;
+  for (uint64_t i = 0; i < n; i++) {
+    AlnJob J;
+    memset(&J, 0, sizeof(J));
+    J.ref_start = ref_off[i];
+    J.ref_end = ref_off[i + 1];
+    J.hint = hint[i];
+    J.read = (uint32_t)i;
+    J.slot = (uint32_t)i;
+    J.band = (uint32_t)std::min<uint64_t>(band[i], 1ull << 30);
+    J.valid = 1;
+    J.gap_open = h->tab_host.gap_open;
+    J.gap_extend = h->tab_host.gap_extend;
+    const int m = (int)(read_off[i + 1] - read_off[i]);
+    const int nn = (int)(ref_off[i + 1] - ref_off[i]);
+    if (band[i] <= 31) {
+      js.push_back(J);
+      lmax_s = std::max(lmax_s, m);
+      nmax_s = std::max(nmax_s, nn);
+    } else {
+      jw.push_back(J);
+      lmax_w = std::max(lmax_w, m);
+      nmax_w = std::max(nmax_w, nn);
+    }
+  }
+  CK(cudaMemset(h->d_err.p, 0, 4));
+  AlignArgs aa{};
+  aa.G = h->G;
+  aa.tab = h->d_tab.p;
+  aa.gc_lnb = h->d_gc_lnb.p;
+  aa.gc_lnbm1 = h->d_gc_lnbm1.p;
+  aa.bases = h->d_bases.p;
+  aa.quals = h->d_quals.p;
+  aa.offs = h->d_offs.p;
+  aa.bases2 = h->d_bases.p;
+  aa.quals2 = h->d_quals.p;
+  aa.offs2 = h->d_offs.p;
+  aa.out = h->d_aln.p;
+  aa.cig_pool = h->d_cig_pool.p;
+  aa.cig_pool_used = h->d_cnt32.p + 2;
+  aa.cig_pool_cap = (uint32_t)h->d_cig_pool.cap;
+  aa.ref_bytes = h->d_bases2.p;
+  aa.counters = h->d_cnt64.p + 3;
+  aa.err = h->d_err.p;
+  CK(cudaMemset(h->d_cnt32.p, 0, 16 * 4));
+  if (!js.empty()) {
+    CK(cudaMemcpy(h->d_jobs.p, js.data(), js.size() * sizeof(AlnJob), cudaMemcpyHostToDevice));
+    unsigned int cnt = (unsigned int)js.size();
+    CK(cudaMemcpy(h->d_cnt32.p + 0, &cnt, 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(h->d_cnt32.p + 1, 0, 4));
+    const size_t tb_smem = (size_t)lmax_s * 8 * 4;
+    aa.jobs = h->d_jobs.p;
+    aa.n_jobs = h->d_cnt32.p + 0;
+    aa.next_job = h->d_cnt32.p + 1;
+    aa.lmax = lmax_s;
+    aa.nmax = nmax_s;
+    aa.tb_smem = tb_smem;
+    aa.tb_global = nullptr;
+    aa.tb_global_per_warp = 0;
+    launch_align(aa, align_grid(h, lmax_s, nmax_s, tb_smem), h->st);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+  }
+  if (!jw.empty()) {
+    CK(cudaMemcpy(h->d_jobs.p, jw.data(), jw.size() * sizeof(AlnJob), cudaMemcpyHostToDevice));
+    unsigned int cnt = (unsigned int)jw.size();
+    CK(cudaMemcpy(h->d_cnt32.p + 0, &cnt, 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(h->d_cnt32.p + 1, 0, 4));
+    const int grid = h->num_sms * 4;
+    const size_t slab = wide_slab_bytes(lmax_w, nmax_w);
+    TRY(grow(h, h->d_tb_global, slab * (size_t)grid * 4));
+    aa.jobs = h->d_jobs.p;
+    aa.n_jobs = h->d_cnt32.p + 0;
+    aa.next_job = h->d_cnt32.p + 1;
+    aa.lmax = lmax_w;
+    aa.nmax = nmax_w;
+    aa.tb_smem = 0;
+    aa.tb_global = h->d_tb_global.p;
+    aa.tb_global_per_warp = slab;
+    launch_align_wide(aa, grid, h->st);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+  }
+  int err = 0;
+  CK(cudaMemcpy(&err, h->d_err.p, 4, cudaMemcpyDeviceToHost));
+  if (err) { h->err = "align kernel error " + std::to_string(err); return PBW_ERR_DEVICE; }
+  std::vector<AlnOut> outs(n);
+  CK(cudaMemcpy(outs.data(), h->d_aln.p, n * sizeof(AlnOut), cudaMemcpyDeviceToHost));
+  unsigned int pool_used = 0;
+  CK(cudaMemcpy(&pool_used, h->d_cnt32.p + 2, 4, cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> pool(pool_used);
+  if (pool_used) CK(cudaMemcpy(pool.data(), h->d_cig_pool.p, pool_used * 4, cudaMemcpyDeviceToHost));
+  uint64_t co = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    score[i] = outs[i].score;
+    offset[i] = outs[i].pos - ref_off[i];
+    cigar_off[i] = (uint32_t)co;
+    const uint32_t* src = outs[i].n_ops > CIG_INLINE ? pool.data() + outs[i].cig_pool : outs[i].cig;
+    for (uint32_t k = 0; k < outs[i].n_ops; k++) {
+      if (co >= cigar_cap) { h->err = "cigar capacity"; return PBW_ERR_CAPACITY; }
+      cigar[co++] = src[k];
+    }
+  }
+  cigar_off[n] = (uint32_t)co;
+  return PBW_OK;
+}
+
+int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uint64_t* hits, uint32_t* hit_read_pos,
+                   uint64_t hit_cap, uint64_t* win_off, double* repeat_prob, uint64_t win_cap) {
+  if (!h || !reads) return PBW_ERR_ARG;
+  cudaSetDevice(h->device);
+  uint64_t total;
+  int lmax;
+  TRY(validate_reads(h, reads, total, lmax));
+  const uint64_t n = reads->n;
+  if (n == 0) { hit_off[0] = 0; win_off[0] = 0; return PBW_OK; }
+  TRY(upload_reads(h, reads, total, h->d_bases, h->d_quals, h->d_offs));
+  ChunkCfg cfg = chunk_cfg(h, n, lmax);
+  cfg.ch = (uint32_t)n;
+  TRY(grow(h, h->d_hits, (size_t)n * cfg.hcap));
+  TRY(grow(h, h->d_hit_rpos, (size_t)n * cfg.hcap));
+  TRY(grow(h, h->d_hit_cnt, n));
+  TRY(grow(h, h->d_overflow, n));
+  TRY(grow(h, h->d_rep, (size_t)n * cfg.wcap));
+  CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * 4, h->st));
+  SeedArgs sa{};
+  sa.G = h->G;
+  sa.idx = h->I;
+  sa.bases = h->d_bases.p;
+  sa.offs = h->d_offs.p;
+  sa.r0 = 0;
+  sa.nr = (uint32_t)n;
+  sa.lmax = cfg.lmax;
+  sa.hits = h->d_hits.p;
+  sa.hcap = cfg.hcap;
+  sa.hit_cnt = h->d_hit_cnt.p;
+  sa.overflow = h->d_overflow.p;
+  sa.n_overflow = h->d_cnt32.p + 3;
+  sa.rep = h->d_rep.p;
+  sa.wcap = cfg.wcap;
+  sa.hit_rpos = h->d_hit_rpos.p;
+  sa.counters = nullptr;
+  launch_seed(sa, h->num_sms * 4, h->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->st));
+  TRY(check_device_errors(h));
+  std::vector<uint32_t> cnt(n);
+  std::vector<unsigned long long> hw((size_t)n * cfg.hcap);
+  std::vector<uint16_t> rp((size_t)n * cfg.hcap);
+  std::vector<uint8_t> rep((size_t)n * cfg.wcap);
+  CK(cudaMemcpy(cnt.data(), h->d_hit_cnt.p, n * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hw.data(), h->d_hits.p, hw.size() * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(rp.data(), h->d_hit_rpos.p, rp.size() * 2, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(rep.data(), h->d_rep.p, rep.size(), cudaMemcpyDeviceToHost));
+  uint64_t ho = 0, wo = 0;
+  for (uint64_t r = 0; r < n; r++) {
+    hit_off[r] = ho;
+    win_off[r] = wo;
+    const uint64_t L = reads->offsets[r + 1] - reads->offsets[r];
+    for (uint32_t k = 0; k < cnt[r]; k++) {
+      if (ho >= hit_cap) { h->err = "hit capacity"; return PBW_ERR_CAPACITY; }
+      unsigned long long w = hw[(size_t)r * cfg.hcap + k];
+      uint32_t gk = (uint32_t)(w >> 40);
+      long long diag = (long long)(w & ((1ull << 40) - 1)) - (long long)DIAG_BIAS;
+      uint32_t rpos = rp[(size_t)r * cfg.hcap + k];
+      bool rev = gk & 1u;
+      unsigned long long pos = rev ? (unsigned long long)(diag - rpos) : (unsigned long long)(diag + rpos);
+      hits[ho] = ((unsigned long long)(rev ? 1 : 0) << 63) | ((unsigned long long)(gk >> 1) << 40) | pos;
+      hit_read_pos[ho] = rpos;
+      ho++;
+    }
+    const uint64_t nw = L >= 15 ? L - 14 : 0;
+    for (uint64_t w = 0; w < nw; w++) {
+      if (wo >= win_cap) { h->err = "window capacity"; return PBW_ERR_CAPACITY; }
+      uint8_t c = rep[(size_t)r * cfg.wcap + w];
+      const uint8_t q = reads->quals[reads->offsets[r] + w];
+      repeat_prob[wo++] = c == 2 ? 1.0 : (c == 1 ? h->tab_host.nrp[q] : 0.0);
+    }
+  }
+  hit_off[n] = ho;
+  win_off[n] = wo;
+  return PBW_OK;
+}
+
+int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_read, uint32_t* n_cand,
+                      uint32_t* total_cand, uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,
+                      double* cand_score) {
+  if (!h || !reads) return PBW_ERR_ARG;
+  cudaSetDevice(h->device);
+  uint64_t total;
+  int lmax;
+  TRY(validate_reads(h, reads, total, lmax));
+  const uint64_t n = reads->n;
+  if (n == 0) return PBW_OK;
+  TRY(upload_reads(h, reads, total, h->d_bases, h->d_quals, h->d_offs));
+  ChunkCfg cfg = chunk_cfg(h, n, lmax);
+  cfg.ch = (uint32_t)n;
+  TRY(grow(h, h->d_hits, (size_t)n * cfg.hcap));
+  TRY(grow(h, h->d_hit_cnt, n));
+  TRY(grow(h, h->d_overflow, n));
+  TRY(grow(h, h->d_rep, (size_t)n * cfg.wcap));
+  DevBuf<Cand> dc;
+  DevBuf<uint32_t> dn, dt;
+  TRY(grow(h, dc, (size_t)n * max_per_read));
+  TRY(grow(h, dn, n));
+  TRY(grow(h, dt, n));
+  CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * 4, h->st));
+  CK(cudaMemsetAsync(dn.p, 0, n * 4, h->st));
+  CK(cudaMemsetAsync(dt.p, 0, n * 4, h->st));
+  SeedArgs sa{};
+  sa.G = h->G;
+  sa.idx = h->I;
+  sa.bases = h->d_bases.p;
+  sa.offs = h->d_offs.p;
+  sa.r0 = 0;
+  sa.nr = (uint32_t)n;
+  sa.lmax = cfg.lmax;
+  sa.hits = h->d_hits.p;
+  sa.hcap = cfg.hcap;
+  sa.hit_cnt = h->d_hit_cnt.p;
+  sa.overflow = h->d_overflow.p;
+  sa.n_overflow = h->d_cnt32.p + 3;
+  sa.rep = h->d_rep.p;
+  sa.wcap = cfg.wcap;
+  launch_seed(sa, h->num_sms * 4, h->st);
+  ClusterArgs ca{};
+  ca.hits = h->d_hits.p;
+  ca.hit_cnt = h->d_hit_cnt.p;
+  ca.overflow = h->d_overflow.p;
+  ca.hcap = cfg.hcap;
+  ca.offs = h->d_offs.p;
+  ca.r0 = 0;
+  ca.nr = (uint32_t)n;
+  ca.group_width = h->opt.group_width;
+  ca.max_out = max_per_read;
+  ca.cand = dc.p;
+  ca.n_cand = dn.p;
+  ca.total_cand = dt.p;
+  ca.err = h->d_err.p;
+  ca.h_lo = 0;
+  ca.h_hi = 512;
+  launch_cluster(ca, 512, 64, h->st);
+  ca.h_lo = 512;
+  ca.h_hi = cfg.hcap;
+  launch_cluster(ca, cfg.hcap, 256, h->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->st));
+  TRY(check_device_errors(h));
+  std::vector<Cand> c((size_t)n * max_per_read);
+  CK(cudaMemcpy(c.data(), dc.p, c.size() * sizeof(Cand), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(n_cand, dn.p, n * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(total_cand, dt.p, n * 4, cudaMemcpyDeviceToHost));
+  for (uint64_t i = 0; i < (uint64_t)n * max_per_read; i++) {
+    cand_contig[i] = c[i].contig;
+    cand_pos[i] = c[i].pos;
+    cand_strand[i] = c[i].strand;
+    cand_score[i] = (double)c[i].score;
+  }
+  return PBW_OK;
+}
+
+}  // extern "C"
