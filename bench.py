@@ -138,13 +138,26 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+_PINNED = []  # pinned host tensors backing the numpy views below
+
+
 def pinned(a: np.ndarray) -> np.ndarray:
     import torch
-    t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
-    v = t.numpy().view(a.dtype).reshape(a.shape)
+    t = torch.empty(max(a.nbytes, 1), dtype=torch.uint8, pin_memory=True)
+    _PINNED.append(t)
+    v = t.numpy()[:a.nbytes].view(a.dtype).reshape(a.shape)
     v[...] = a
-    v._keep = t  # noqa: keep the pinned tensor alive
     return v
+
+
+def max_over_ranks(values, world: int, device: str = "cpu"):
+    """Step times of the slowest rank (replicas run the same workload)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
 
 
 def run_gpu(args, prefix, d, meta, rank, world):
@@ -198,21 +211,17 @@ def run_gpu(args, prefix, d, meta, rank, world):
     dev_ms = [s["ms_seed"] + s["ms_cluster"] + s["ms_align"] + s["ms_pair"] + s["ms_finalize"] + s["ms_d2h"]
               for s in stats]
     e2e_ms = [s["ms_total"] for s in stats]
-    mean_dev = statistics.mean(dev_ms) / 1e3
-    mean_e2e = statistics.mean(e2e_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([mean_dev, mean_e2e], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        mean_dev, mean_e2e = float(t[0]), float(t[1])
+    mean_dev, mean_e2e = max_over_ranks([statistics.mean(dev_ms) / 1e3, statistics.mean(e2e_ms) / 1e3], world,
+                                        "cuda")
     s0 = stats[-1]
     value = n_reads * world / mean_dev
     e2e = n_reads * world / mean_e2e
     h2d = int(R1.bases.nbytes + R1.quals.nbytes + R1.offsets.nbytes)
     if paired:
         h2d += int(R2.bases.nbytes + R2.quals.nbytes + R2.offsets.nbytes)
-    rec_bytes = sum(int(v.nbytes) for k, v in O1.items() if k != "cigar") + int(O1["cigar_off"][-1]) * 4
+    rec_bytes = sum(int(v.nbytes) for k, v in O1.items() if not k.startswith(("cigar", "_"))) + 4 * (len(O1["cigar_off"]) + int(O1["cigar_off"][-1]))
     if paired:
-        rec_bytes += sum(int(v.nbytes) for k, v in O2.items() if k != "cigar") + int(O2["cigar_off"][-1]) * 4
+        rec_bytes += sum(int(v.nbytes) for k, v in O2.items() if not k.startswith(("cigar", "_"))) + 4 * (len(O2["cigar_off"]) + int(O2["cigar_off"][-1]))
     # roofline of the dominant kernel
     phases = {"seed": s0["ms_seed"], "cluster": s0["ms_cluster"], "align_seeded": s0["ms_align"],
               "pair": s0["ms_pair"], "finalize": s0["ms_finalize"]}
@@ -280,7 +289,7 @@ def cpu_baseline(prefix, d, meta):
 
 def run_reference(args, prefix, d, meta):
     threads = os.cpu_count() or 1
-    n = 20_000 if meta["paired"] else 10_000
+    n = 50_000 if meta["paired"] else 10_000
     for _ in range(args.warmup):
         cpu_time(prefix, d, meta, min(n, 2000), threads)
     times, reads = [], 0

@@ -129,15 +129,18 @@ size_t cluster_smem(uint32_t hmax, int threads) {
   uint32_t np = 1;
   while (np < hmax) np <<= 1;
   // keys 8, vals 4, a 4, b 4, pre 8, gmin 4, gfirst 4, ggk 4, rank 4, clstart 4, clgrp 4 per element
-  size_t s = (size_t)np * 52 + 64 + 32 * 8 + 64;
+  size_t s = (size_t)np * 52 + 64;
   (void)threads;
   return (s + 15) & ~(size_t)15;
 }
 
-__global__ void k_cluster(ClusterArgs p, uint32_t np_max) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const uint32_t NP = np_max;
-  unsigned long long* keys = (unsigned long long*)smem_raw;
+// Clusters one read's H hits. Work arrays are carved from base (shared
+// memory, or a global scratch slab for reads with very many hits) for
+// NP = next_pow2(H) or more elements.
+__device__ void cluster_read(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
+                             unsigned char* base, uint32_t NP, uint32_t* wtmp32, unsigned long long* wtmp64,
+                             uint32_t& sh_G, uint32_t& sh_C) {
+  unsigned long long* keys = (unsigned long long*)base;
   unsigned long long* pre = keys + NP;           // NP + 1
   uint32_t* vals = (uint32_t*)(pre + NP + 1);
   uint32_t* a = vals + NP;                       // a and b contiguous: reused as 2*NP slots
@@ -148,10 +151,166 @@ __global__ void k_cluster(ClusterArgs p, uint32_t np_max) {
   uint32_t* rank = ggk + NP;
   uint32_t* clstart = rank + NP;                 // NP + 1
   uint32_t* clgrp = clstart + NP + 1;
-  unsigned long long* wtmp64 = (unsigned long long*)(((uintptr_t)(clgrp + NP) + 15) & ~(uintptr_t)15);
-  uint32_t* wtmp32 = (uint32_t*)(wtmp64 + 32);
-  __shared__ uint32_t sh_G, sh_C;
+  const uint64_t rg = (uint64_t)p.r0 + r;
+  const long long L = (long long)(p.offs[rg + 1] - p.offs[rg]);
+  const uint32_t n = next_pow2(H);
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    keys[i] = i < H ? hits[i] : ~0ull;
+    vals[i] = i;
+  }
+  __syncthreads();
+  bitonic_kv(keys, vals, n);
+  // boundaries
+  for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+    unsigned long long k = keys[i];
+    uint32_t gk = (uint32_t)(k >> 40);
+    long long d = (long long)(k & ((1ull << 40) - 1));
+    bool gs = i == 0, cs = i == 0;
+    if (i > 0) {
+      unsigned long long kp = keys[i - 1];
+      gs = (uint32_t)(kp >> 40) != gk;
+      long long dp = (long long)(kp & ((1ull << 40) - 1));
+      cs = gs || (d - dp > 50);  // MERGE_DISTANCE (candidates.rs:27)
+    }
+    a[i] = cs ? 1u : 0u;
+    b[i] = gs ? 1u : 0u;
+    pre[i] = (unsigned long long)d;
+  }
+  __syncthreads();
+  block_scan_incl<uint32_t>(a, H, wtmp32);
+  block_scan_incl<uint32_t>(b, H, wtmp32);
+  block_scan_incl<unsigned long long>(pre, H, wtmp64);
+  if (threadIdx.x == 0) {
+    sh_C = a[H - 1];
+    sh_G = b[H - 1];
+  }
+  __syncthreads();
+  const uint32_t C = sh_C, G = sh_G;
+  for (uint32_t g = threadIdx.x; g < G; g += blockDim.x) gmin[g] = 0xFFFFFFFFu;
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+    uint32_t cl = a[i] - 1, g = b[i] - 1;
+    bool cs = i == 0 || a[i] != a[i - 1];
+    bool gs = i == 0 || b[i] != b[i - 1];
+    if (gs) {
+      ggk[g] = (uint32_t)(keys[i] >> 40);
+      gfirst[g] = cl;
+    }
+    if (cs) {
+      clstart[cl] = i;
+      clgrp[cl] = g;
+    }
+    atomicMin(&gmin[g], vals[i]);
+  }
+  if (threadIdx.x == 0) clstart[C] = H;
+  __syncthreads();
+  // group insertion order = ascending first emission index
+  const uint32_t ng = next_pow2(G);
+  for (uint32_t g = threadIdx.x; g < ng; g += blockDim.x) {
+    keys[g] = g < G ? (((unsigned long long)gmin[g] << 32) | g) : ~0ull;
+    vals[g] = g;
+  }
+  __syncthreads();
+  bitonic_kv(keys, vals, ng);
+  // replay SwissTable insertion (single thread); slots live in a|b
+  if (threadIdx.x == 0) {
+    uint32_t* slots = a;  // 2*NP entries
+    uint32_t nb = 0, items = 0;
+    int bad = 0;
+    for (uint32_t t = 0; t < G && !bad; t++) {
+      uint32_t g = (uint32_t)(keys[t] & 0xFFFFFFFFu);
+      uint32_t gk = ggk[g];
+      unsigned long long h = fx_hash_group(gk >> 1, gk & 1u);
+      if (items + 1 > swiss_cap(nb)) {
+        uint32_t need = max(items + 1, swiss_cap(nb) + 1);
+        uint32_t nnb = swiss_buckets(need);
+        if (nnb > 2 * NP) { bad = 1; break; }
+        // rehash: old entries in bucket order into a fresh table at the
+        // upper half, then move back (nnb <= 2*NP, old table nb <= NP)
+        uint32_t* fresh = slots + (2 * NP - nnb);
+        // old table occupies slots[0..nb); fresh region must not overlap it
+        if (nb > 2 * NP - nnb) {
+          // copy old table out of the way into rank[] scratch (G <= NP)
+          for (uint32_t s = 0; s < nb; s++) rank[s] = slots[s];
+          for (uint32_t s = 0; s < nnb; s++) fresh[s] = 0xFFFFFFFFu;
+          for (uint32_t s = 0; s < nb; s++)
+            if (rank[s] != 0xFFFFFFFFu) {
+              uint32_t og = rank[s];
+              uint32_t ogk = ggk[og];
+              uint32_t q = swiss_find(fresh, nnb, fx_hash_group(ogk >> 1, ogk & 1u), p.group_width);
+              fresh[q] = og;
+            }
+        } else {
+          for (uint32_t s = 0; s < nnb; s++) fresh[s] = 0xFFFFFFFFu;
+          for (uint32_t s = 0; s < nb; s++)
+            if (slots[s] != 0xFFFFFFFFu) {
+              uint32_t og = slots[s];
+              uint32_t ogk = ggk[og];
+              uint32_t q = swiss_find(fresh, nnb, fx_hash_group(ogk >> 1, ogk & 1u), p.group_width);
+              fresh[q] = og;
+            }
+        }
+        for (uint32_t s = 0; s < nnb; s++) slots[s] = fresh[s];
+        nb = nnb;
+      }
+      uint32_t q = swiss_find(slots, nb, h, p.group_width);
+      if (q == 0xFFFFFFFFu) { bad = 1; break; }
+      slots[q] = g;
+      items++;
+    }
+    if (bad) {
+      atomicExch(p.err, 1);
+    } else {
+      uint32_t rk = 0;
+      for (uint32_t s = 0; s < nb; s++)
+        if (slots[s] != 0xFFFFFFFFu) rank[slots[s]] = rk++;
+    }
+  }
+  __syncthreads();
+  // cluster order keys: count desc, group rank asc, diagonal order asc
+  const uint32_t nc = next_pow2(C);
+  for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
+    unsigned long long key = ~0ull;
+    if (c < C) {
+      uint32_t g = clgrp[c];
+      uint32_t cnt = clstart[c + 1] - clstart[c];
+      key = ((unsigned long long)(0xFFFFFu - cnt) << 44) | ((unsigned long long)rank[g] << 24) |
+            (unsigned long long)(c - gfirst[g]);
+    }
+    keys[c] = key;
+    vals[c] = c;
+  }
+  __syncthreads();
+  bitonic_kv(keys, vals, nc);
+  const uint32_t nout = min(C, p.max_out);
+  for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
+    uint32_t c = vals[i];
+    uint32_t s = clstart[c], e = clstart[c + 1];
+    uint32_t cnt = e - s;
+    unsigned long long sumb = pre[e - 1] - (s > 0 ? pre[s - 1] : 0ull);
+    long long sum = (long long)sumb - (long long)cnt * (long long)DIAG_BIAS;
+    long long avg = sum / (long long)cnt;  // truncation toward zero, as Rust's i64 '/'
+    uint32_t gk = ggk[clgrp[c]];
+    long long posi = (gk & 1u) ? avg - L + KMER : avg;
+    Cand cd;
+    cd.pos = posi > 0 ? (unsigned long long)posi : 0ull;
+    cd.contig = gk >> 1;
+    cd.strand = (uint8_t)(gk & 1u);
+    cd.score = cnt;
+    p.cand[(size_t)r * p.max_out + i] = cd;
+  }
+  if (threadIdx.x == 0) {
+    p.n_cand[r] = nout;
+    if (p.total_cand) p.total_cand[r] = C;
+  }
+  __syncthreads();
+}
 
+__global__ void k_cluster(ClusterArgs p, uint32_t np_max) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long wtmp64[32];
+  __shared__ uint32_t wtmp32[32];
+  __shared__ uint32_t sh_G, sh_C;
   for (uint32_t r = blockIdx.x; r < p.nr; r += gridDim.x) {
     const uint32_t H = p.hit_cnt[r];
     if (p.overflow[r]) continue;
@@ -163,160 +322,22 @@ __global__ void k_cluster(ClusterArgs p, uint32_t np_max) {
       }
       continue;
     }
-    const uint64_t rg = (uint64_t)p.r0 + r;
-    const long long L = (long long)(p.offs[rg + 1] - p.offs[rg]);
-    const unsigned long long* hits = p.hits + (size_t)r * p.hcap;
-    const uint32_t n = next_pow2(H);
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-      keys[i] = i < H ? hits[i] : ~0ull;
-      vals[i] = i;
-    }
-    __syncthreads();
-    bitonic_kv(keys, vals, n);
-    // boundaries
-    for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
-      unsigned long long k = keys[i];
-      uint32_t gk = (uint32_t)(k >> 40);
-      long long d = (long long)(k & ((1ull << 40) - 1));
-      bool gs = i == 0, cs = i == 0;
-      if (i > 0) {
-        unsigned long long kp = keys[i - 1];
-        gs = (uint32_t)(kp >> 40) != gk;
-        long long dp = (long long)(kp & ((1ull << 40) - 1));
-        cs = gs || (d - dp > 50);  // MERGE_DISTANCE (candidates.rs:27)
-      }
-      a[i] = cs ? 1u : 0u;
-      b[i] = gs ? 1u : 0u;
-      pre[i] = (unsigned long long)d;
-    }
-    __syncthreads();
-    block_scan_incl<uint32_t>(a, H, wtmp32);
-    block_scan_incl<uint32_t>(b, H, wtmp32);
-    block_scan_incl<unsigned long long>(pre, H, wtmp64);
-    if (threadIdx.x == 0) {
-      sh_C = a[H - 1];
-      sh_G = b[H - 1];
-    }
-    __syncthreads();
-    const uint32_t C = sh_C, G = sh_G;
-    for (uint32_t g = threadIdx.x; g < G; g += blockDim.x) gmin[g] = 0xFFFFFFFFu;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
-      uint32_t cl = a[i] - 1, g = b[i] - 1;
-      bool cs = i == 0 || a[i] != a[i - 1];
-      bool gs = i == 0 || b[i] != b[i - 1];
-      if (gs) {
-        ggk[g] = (uint32_t)(keys[i] >> 40);
-        gfirst[g] = cl;
-      }
-      if (cs) {
-        clstart[cl] = i;
-        clgrp[cl] = g;
-      }
-      atomicMin(&gmin[g], vals[i]);
-    }
-    if (threadIdx.x == 0) clstart[C] = H;
-    __syncthreads();
-    // group insertion order = ascending first emission index
-    const uint32_t ng = next_pow2(G);
-    for (uint32_t g = threadIdx.x; g < ng; g += blockDim.x) {
-      keys[g] = g < G ? (((unsigned long long)gmin[g] << 32) | g) : ~0ull;
-      vals[g] = g;
-    }
-    __syncthreads();
-    bitonic_kv(keys, vals, ng);
-    // replay SwissTable insertion (single thread); slots live in a|b
-    if (threadIdx.x == 0) {
-      uint32_t* slots = a;  // 2*NP entries
-      uint32_t nb = 0, items = 0;
-      int bad = 0;
-      for (uint32_t t = 0; t < G && !bad; t++) {
-        uint32_t g = (uint32_t)(keys[t] & 0xFFFFFFFFu);
-        uint32_t gk = ggk[g];
-        unsigned long long h = fx_hash_group(gk >> 1, gk & 1u);
-        if (items + 1 > swiss_cap(nb)) {
-          uint32_t need = max(items + 1, swiss_cap(nb) + 1);
-          uint32_t nnb = swiss_buckets(need);
-          if (nnb > 2 * NP) { bad = 1; break; }
-          // rehash: old entries in bucket order into a fresh table at the
-          // upper half, then move back (nnb <= 2*NP, old table nb <= NP)
-          uint32_t* fresh = slots + (2 * NP - nnb);
-          // old table occupies slots[0..nb); fresh region must not overlap it
-          if (nb > 2 * NP - nnb) {
-            // copy old table out of the way into rank[] scratch (G <= NP)
-            for (uint32_t s = 0; s < nb; s++) rank[s] = slots[s];
-            for (uint32_t s = 0; s < nnb; s++) fresh[s] = 0xFFFFFFFFu;
-            for (uint32_t s = 0; s < nb; s++)
-              if (rank[s] != 0xFFFFFFFFu) {
-                uint32_t og = rank[s];
-                uint32_t ogk = ggk[og];
-                uint32_t q = swiss_find(fresh, nnb, fx_hash_group(ogk >> 1, ogk & 1u), p.group_width);
-                fresh[q] = og;
-              }
-          } else {
-            for (uint32_t s = 0; s < nnb; s++) fresh[s] = 0xFFFFFFFFu;
-            for (uint32_t s = 0; s < nb; s++)
-              if (slots[s] != 0xFFFFFFFFu) {
-                uint32_t og = slots[s];
-                uint32_t ogk = ggk[og];
-                uint32_t q = swiss_find(fresh, nnb, fx_hash_group(ogk >> 1, ogk & 1u), p.group_width);
-                fresh[q] = og;
-              }
-          }
-          for (uint32_t s = 0; s < nnb; s++) slots[s] = fresh[s];
-          nb = nnb;
-        }
-        uint32_t q = swiss_find(slots, nb, h, p.group_width);
-        if (q == 0xFFFFFFFFu) { bad = 1; break; }
-        slots[q] = g;
-        items++;
-      }
-      if (bad) {
-        atomicExch(p.err, 1);
-      } else {
-        uint32_t rk = 0;
-        for (uint32_t s = 0; s < nb; s++)
-          if (slots[s] != 0xFFFFFFFFu) rank[slots[s]] = rk++;
-      }
-    }
-    __syncthreads();
-    // cluster order keys: count desc, group rank asc, diagonal order asc
-    const uint32_t nc = next_pow2(C);
-    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
-      unsigned long long key = ~0ull;
-      if (c < C) {
-        uint32_t g = clgrp[c];
-        uint32_t cnt = clstart[c + 1] - clstart[c];
-        key = ((unsigned long long)(0xFFFFFu - cnt) << 44) | ((unsigned long long)rank[g] << 24) |
-              (unsigned long long)(c - gfirst[g]);
-      }
-      keys[c] = key;
-      vals[c] = c;
-    }
-    __syncthreads();
-    bitonic_kv(keys, vals, nc);
-    const uint32_t nout = min(C, p.max_out);
-    for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
-      uint32_t c = vals[i];
-      uint32_t s = clstart[c], e = clstart[c + 1];
-      uint32_t cnt = e - s;
-      unsigned long long sumb = pre[e - 1] - (s > 0 ? pre[s - 1] : 0ull);
-      long long sum = (long long)sumb - (long long)cnt * (long long)DIAG_BIAS;
-      long long avg = sum / (long long)cnt;  // truncation toward zero, as Rust's i64 '/'
-      uint32_t gk = ggk[clgrp[c]];
-      long long posi = (gk & 1u) ? avg - L + KMER : avg;
-      Cand cd;
-      cd.pos = posi > 0 ? (unsigned long long)posi : 0ull;
-      cd.contig = gk >> 1;
-      cd.strand = (uint8_t)(gk & 1u);
-      cd.score = cnt;
-      p.cand[(size_t)r * p.max_out + i] = cd;
-    }
-    if (threadIdx.x == 0) {
-      p.n_cand[r] = nout;
-      if (p.total_cand) p.total_cand[r] = C;
-    }
-    __syncthreads();
+    cluster_read(p, r, H, p.hits + (size_t)r * p.hcap, smem_raw, np_max, wtmp32, wtmp64, sh_G, sh_C);
+  }
+}
+
+// Overflowed reads (list mode): hits in the pool, arrays in global scratch.
+__global__ void k_cluster_list(ClusterArgs p) {
+  __shared__ unsigned long long wtmp64[32];
+  __shared__ uint32_t wtmp32[32];
+  __shared__ uint32_t sh_G, sh_C;
+  const unsigned int n = *p.list_n;
+  for (uint32_t w = blockIdx.x; w < n; w += gridDim.x) {
+    const uint32_t r = p.list[w];
+    const uint32_t H = p.need[r];
+    const unsigned long long off = p.list_hoff[w];
+    uint32_t NP = next_pow2(H);
+    cluster_read(p, r, H, p.hits_pool + off, p.scratch + 2 * off * 56, NP, wtmp32, wtmp64, sh_G, sh_C);
   }
 }
 
@@ -328,6 +349,10 @@ void launch_cluster(const ClusterArgs& a, uint32_t hmax, int threads, cudaStream
   if (grid < 1) grid = 1;
   cudaFuncSetAttribute(k_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_cluster<<<grid, threads, sm, st>>>(a, np);
+}
+
+void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st) {
+  k_cluster_list<<<grid, 256, 0, st>>>(a);
 }
 
 }  // namespace pbw

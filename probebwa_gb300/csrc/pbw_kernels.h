@@ -25,6 +25,15 @@ struct SeedArgs {
   uint32_t wcap;
   uint16_t* hit_rpos;       // optional nr * hcap read positions (parity tests)
   unsigned long long* counters;  // probes, entries, hits
+  // overflow handling: reads with more than hcap hits are queued with their
+  // exact hit count and seeded again in list mode into a pool
+  uint32_t* need;           // nr: exact hit count of an overflowed read
+  uint32_t* ovf_list;       // overflowed chunk-relative read indices
+  unsigned int* n_ovf;      // queue length
+  const uint32_t* list;     // list mode: work item w is read list[w]
+  const unsigned int* list_n;
+  const unsigned long long* list_hoff;  // hits pool offset of item w
+  unsigned long long* hits_pool;
 };
 __host__ __device__ inline size_t seed_smem_per_warp(int lmax) {
   int W = lmax - KMER + 1 > 0 ? lmax - KMER + 1 : 1;
@@ -55,9 +64,21 @@ struct ClusterArgs {
   uint32_t* total_cand;     // nr: all clusters (optional)
   uint32_t h_lo, h_hi;      // process reads with h_lo < H <= h_hi
   int* err;                 // device error word
+  // list mode (overflowed reads): hits in the pool, sort arrays in global scratch
+  const uint32_t* list;
+  const unsigned int* list_n;
+  const unsigned long long* list_hoff;
+  const unsigned long long* hits_pool;
+  const uint32_t* need;
+  unsigned char* scratch;   // 2 * 56 bytes per pooled hit
 };
 size_t cluster_smem(uint32_t hmax, int threads);
 void launch_cluster(const ClusterArgs& a, uint32_t hmax, int threads, cudaStream_t st);
+void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st);
+void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st);
+void launch_ovf_offsets(const uint32_t* list, const unsigned int* list_n, const uint32_t* need,
+                        unsigned long long* hoff, unsigned long long pool_cap, int* err, unsigned int* list_n_out,
+                        cudaStream_t st);
 
 // ---- K3 alignment ----
 // One alignment problem: query = read (forward) or its reverse complement,
@@ -118,6 +139,8 @@ struct AlignArgs {
 };
 void launch_align(const AlignArgs& a, int grid, cudaStream_t st);
 void launch_align_wide(const AlignArgs& a, int grid, cudaStream_t st);
+void launch_align_band(const AlignArgs& a, int grid, cudaStream_t st);
+size_t band_smem_per_warp(int lmax, int nmax);
 size_t wide_slab_bytes(int lmax, int nmax);
 size_t align_smem_per_warp(int lmax, int nmax, size_t tb_smem);
 

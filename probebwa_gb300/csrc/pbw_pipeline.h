@@ -96,6 +96,10 @@ struct pbw_handle {
   pbw::DevBuf<unsigned long long> d_cnt64;  // 0 probes, 1 entries, 2 hits, 3 dp jobs, 4 dp cells
   pbw::DevBuf<unsigned int> d_scan_sums;
   pbw::DevBuf<unsigned char> d_tb_global;
+  // reads with more seed hits than the per-read capacity
+  pbw::DevBuf<uint32_t> d_need, d_ovf_list;
+  pbw::DevBuf<unsigned long long> d_list_hoff, d_hits_pool;
+  pbw::DevBuf<unsigned char> d_cl_scratch;
   // outputs of a call
   pbw::DevBuf<int32_t> o_contig, o_mate_contig, o_as, o_nm, o_best;
   pbw::DevBuf<unsigned long long> o_pos, o_mate_pos;

@@ -1,6 +1,7 @@
 // pipeline.cu -- the device pipeline behind pbw_map_single and the stage
 // entry points (include/probebwa_gpu.h).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -54,6 +55,10 @@ int pipeline_init(pbw_handle* h) {
   return PBW_OK;
 }
 
+// Seed hits pooled for reads that overflow the per-read capacity (per
+// chunk); their clustering scratch takes 112 bytes per pooled hit.
+constexpr size_t OVF_POOL_HITS = 16ull << 20;
+
 // Scratch sizing for one chunk.
 struct ChunkCfg {
   uint32_t ch;      // reads per chunk
@@ -98,6 +103,11 @@ static int ensure_chunk(pbw_handle* h, const ChunkCfg& c, int align_grid_warps) 
   TRY(grow(h, h->d_aln, (size_t)c.ch * MAX_CAND));
   TRY(grow(h, h->d_cig_pool, (size_t)c.ch * MAX_CAND * 24 + 4096));
   TRY(grow(h, h->d_scan_sums, scan_blocks(c.ch) + 4));
+  TRY(grow(h, h->d_need, c.ch));
+  TRY(grow(h, h->d_ovf_list, c.ch));
+  TRY(grow(h, h->d_list_hoff, c.ch));
+  TRY(grow(h, h->d_hits_pool, OVF_POOL_HITS));
+  TRY(grow(h, h->d_cl_scratch, OVF_POOL_HITS * 112));
   if (c.tb_glob) TRY(grow(h, h->d_tb_global, c.tb_glob * (size_t)align_grid_warps));
   if (h->opt.max_indel_len > 31)
     TRY(grow(h, h->d_tb_global, wide_slab_bytes(c.lmax, c.nmax) * (size_t)h->num_sms * 16));
@@ -126,6 +136,13 @@ static int ensure_outputs(pbw_handle* h, uint64_t n, uint64_t cig_cap) {
 static int align_grid(pbw_handle* h, int lmax, int nmax, size_t tb_smem) {
   size_t per_block = align_smem_per_warp(lmax, nmax, tb_smem) * 4;
   int bps = (int)std::max<size_t>(1, std::min<size_t>(8, (h->smem_optin ? 228 * 1024 : 100 * 1024) / per_block));
+  return h->num_sms * bps;
+}
+
+// Resident blocks of the anti-diagonal band kernel (4 warps per block).
+static int band_grid(pbw_handle* h, int lmax, int nmax) {
+  const size_t per_block = band_smem_per_warp(lmax, nmax) * 4;
+  const int bps = (int)std::max<size_t>(1, std::min<size_t>(12, (220 * 1024) / per_block));
   return h->num_sms * bps;
 }
 
@@ -182,11 +199,28 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   sa.wcap = cfg.wcap;
   sa.hit_rpos = nullptr;
   sa.counters = h->d_cnt64.p;
+  sa.need = h->d_need.p;
+  sa.ovf_list = h->d_ovf_list.p;
+  sa.n_ovf = c32 + 6;
+  CK(cudaMemsetAsync(c32 + 6, 0, 2 * sizeof(unsigned int), st));
   {
     size_t sm = seed_smem_per_warp(cfg.lmax) * 8;
     int bps = (int)std::max<size_t>(1, std::min<size_t>(8, (228 * 1024) / std::max<size_t>(sm, 1)));
     launch_seed(sa, h->num_sms * bps, st);
   }
+  // reads over capacity: exact-size pool slots, seeded again in list mode
+  launch_ovf_offsets(h->d_ovf_list.p, c32 + 6, h->d_need.p, h->d_list_hoff.p, OVF_POOL_HITS, h->d_err.p, c32 + 7, st);
+  {
+    SeedArgs sl = sa;
+    sl.list = h->d_ovf_list.p;
+    sl.list_n = c32 + 7;
+    sl.list_hoff = h->d_list_hoff.p;
+    sl.hits_pool = h->d_hits_pool.p;
+    sl.ovf_list = nullptr;
+    sl.counters = nullptr;
+    launch_seed_list(sl, h->num_sms * 2, st);
+  }
+  h->stats.kernel_launches += 2;
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[1], st));
   ClusterArgs ca{};
@@ -209,6 +243,14 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   ca.h_lo = 512;
   ca.h_hi = cfg.hcap;
   launch_cluster(ca, cfg.hcap, 256, st);
+  ca.list = h->d_ovf_list.p;
+  ca.list_n = c32 + 7;
+  ca.list_hoff = h->d_list_hoff.p;
+  ca.hits_pool = h->d_hits_pool.p;
+  ca.need = h->d_need.p;
+  ca.scratch = h->d_cl_scratch.p;
+  launch_cluster_list(ca, h->num_sms, st);
+  h->stats.kernel_launches += 1;
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[2], st));
   MakeJobsArgs ma{};
@@ -254,7 +296,8 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   aa.counters = h->d_cnt64.p + 3;
   aa.err = h->d_err.p;
   if (h->opt.max_indel_len <= 31) {
-    launch_align(aa, grid_align, st);
+    (void)grid_align;
+    launch_align_band(aa, band_grid(h, cfg.lmax, cfg.nmax), st);
   } else {
     aa.tb_smem = 0;
     aa.tb_global = h->d_tb_global.p;
@@ -327,6 +370,11 @@ static int check_device_errors(pbw_handle* h) {
   if (c32[3]) {
     h->err = std::to_string(c32[3]) + " read(s) produced more seed hits than the per-read capacity";
     CK(cudaMemset(h->d_cnt32.p + 3, 0, 4));
+    return PBW_ERR_LIMIT;
+  }
+  if (err == 5) {
+    h->err = "seed hits of over-capacity reads exceed the overflow pool";
+    CK(cudaMemset(h->d_err.p, 0, 4));
     return PBW_ERR_LIMIT;
   }
   if (err) {
@@ -878,7 +926,7 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
     aa.tb_smem = tb_smem;
     aa.tb_global = nullptr;
     aa.tb_global_per_warp = 0;
-    launch_align(aa, align_grid(h, lmax_s, nmax_s, tb_smem), h->st);
+    launch_align_band(aa, band_grid(h, lmax_s, nmax_s), h->st);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->st));
   }

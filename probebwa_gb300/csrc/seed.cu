@@ -118,14 +118,18 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
   unsigned long long n_probe = 0, n_entry = 0, n_hit = 0;
   const int gw = blockIdx.x * wpb + wib;
   const int nwarps = gridDim.x * wpb;
-  for (uint32_t r = gw; r < p.nr; r += nwarps) {
+  const bool list_mode = p.list != nullptr;
+  const uint32_t nitems = list_mode ? *p.list_n : p.nr;
+  for (uint32_t item = gw; item < nitems; item += nwarps) {
+    const uint32_t r = list_mode ? p.list[item] : item;
     const uint64_t rg = (uint64_t)p.r0 + r;
     const uint64_t o0 = p.offs[rg];
     const int L = (int)(p.offs[rg + 1] - o0);
     uint8_t* rep = p.rep + (size_t)r * p.wcap;
-    unsigned long long* hits = p.hits + (size_t)r * p.hcap;
+    unsigned long long* hits = list_mode ? p.hits_pool + p.list_hoff[item] : p.hits + (size_t)r * p.hcap;
+    const uint32_t hcap = list_mode ? p.need[r] : p.hcap;
     if (L < KMER) {
-      if (lane == 0) { p.hit_cnt[r] = 0; p.overflow[r] = 0; }
+      if (lane == 0 && !list_mode) { p.hit_cnt[r] = 0; p.overflow[r] = 0; }
       continue;
     }
     const int nw = L - KMER + 1;
@@ -254,25 +258,33 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
         unsigned int rank = __popc(bal & ((1u << lane) - 1u));
         if (pass) {
           uint32_t slot = nh + rank;
-          if (slot < p.hcap) {
+          if (slot < hcap) {
             hits[slot] = word;
-            if (p.hit_rpos) p.hit_rpos[(size_t)r * p.hcap + slot] = (uint16_t)s_w;
+            if (p.hit_rpos && !list_mode) p.hit_rpos[(size_t)r * p.hcap + slot] = (uint16_t)s_w;
           }
           n_hit++;
         }
         nh += __popc(bal);
       }
     }
-    if (nh > p.hcap) over = true;
+    if (nh > hcap) over = true;
     __syncwarp();
-    if (lane == 0) {
+    if (lane == 0 && !list_mode) {
       p.hit_cnt[r] = over ? p.hcap : nh;
       p.overflow[r] = over ? 1 : 0;
-      if (over) atomicAdd(p.n_overflow, 1u);
+      if (over) {
+        if (p.ovf_list) {
+          p.need[r] = nh;
+          p.ovf_list[atomicAdd(p.n_ovf, 1u)] = r;
+        } else {
+          atomicAdd(p.n_overflow, 1u);
+        }
+      }
     }
     __syncwarp();
   }
-  // counters
+  // counters (the list-mode pass repeats work already counted)
+  if (list_mode) return;
   for (int d = 16; d >= 1; d >>= 1) {
     n_probe += __shfl_down_sync(0xffffffffu, n_probe, d);
     n_entry += __shfl_down_sync(0xffffffffu, n_entry, d);
@@ -283,6 +295,38 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
     atomicAdd(&p.counters[1], n_entry);
     atomicAdd(&p.counters[2], n_hit);
   }
+}
+
+// Exclusive offsets of the overflowed reads' exact hit counts in the pool.
+__global__ void k_ovf_offsets(const uint32_t* list, const unsigned int* list_n, const uint32_t* need,
+                              unsigned long long* hoff, unsigned long long pool_cap, int* err,
+                              unsigned int* list_n_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const unsigned int n = *list_n;
+  unsigned long long acc = 0;
+  for (unsigned int i = 0; i < n; i++) {
+    hoff[i] = acc;
+    acc += need[list[i]];
+  }
+  if (acc > pool_cap) {
+    atomicExch(err, 5);
+    *list_n_out = 0;
+  } else {
+    *list_n_out = n;
+  }
+}
+
+void launch_ovf_offsets(const uint32_t* list, const unsigned int* list_n, const uint32_t* need,
+                        unsigned long long* hoff, unsigned long long pool_cap, int* err, unsigned int* list_n_out,
+                        cudaStream_t st) {
+  k_ovf_offsets<<<1, 32, 0, st>>>(list, list_n, need, hoff, pool_cap, err, list_n_out);
+}
+
+void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st) {
+  const int threads = 256;
+  size_t sm = seed_smem_per_warp(a.lmax) * (threads / 32);
+  cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_seed<<<grid, threads, sm, st>>>(a);
 }
 
 void launch_seed(const SeedArgs& a, int grid, cudaStream_t st) {

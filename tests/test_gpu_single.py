@@ -182,3 +182,37 @@ def test_sam_text_matches_oracle(P, oracle, tmp_path):
     a = open(tmp_path / "gpu.sam", "rb").read()
     b = open(tmp_path / "cpu.sam", "rb").read()
     assert a == b
+
+
+def test_reads_over_seed_hit_capacity(P, oracle, tmp_path):
+    """Reads whose one-mismatch neighbours hit a high-copy repeat family
+    produce far more than 4096 seed hits; they go through the overflow pool
+    (list-mode seeding and global-scratch clustering) and must still match."""
+    from probebwa_gb300 import synth
+    rng = np.random.default_rng(77)
+    unit = synth.rand_codes(rng, 1000)
+    parts = []
+    for _ in range(1500):
+        parts.append(synth.mutate_subs(rng, unit, 0.003))
+        parts.append(synth.rand_codes(rng, int(rng.integers(3, 40))))
+    g = np.concatenate(parts)
+    prefix = str(tmp_path / "g")
+    synth.write_index(prefix, [("rep", g)])
+    seqs, quals = [], []
+    for i in range(40):
+        s = int(rng.integers(0, 1000 - 150))
+        frag = unit[s:s + 150].copy()
+        frag[::16] = (frag[::16] + 1) % 4  # one private change in every 15-mer window
+        if i % 2:
+            frag = (3 - frag[::-1])
+        seqs.append(synth.ASCII[frag].tobytes())
+        quals.append(bytes(rng.integers(20, 41, size=150).astype(np.uint8)))
+    seqs2, quals2, _ = synth.reads_single(78, [("rep", g)], n=200, L=150)
+    R = P.Reads.from_lists(seqs + seqs2, quals + quals2)
+    with P.Mapper(prefix) as m:
+        got = m.map_single(R)
+        st = m.stats()
+    om = oracle.Mapper(prefix)
+    exp = om.map_single(to_oracle_reads(oracle, R))
+    compare_records(P, oracle, got, exp, "over-capacity reads")
+    assert st["seed_hits"] > 4096 * 5
