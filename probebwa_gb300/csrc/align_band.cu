@@ -148,8 +148,11 @@ __global__ void __launch_bounds__(128) k_align_band(AlignArgs p) {
       const long long j = jof(R0 - 1, c);
       return (j >= 0 && j <= n) ? 0 : NEG;
     };
-    int32_t EM = ev_ok ? init_m(c_even) : NEG, EI = NEG, ED = NEG;  // last even-column output
-    int32_t OM = od_ok ? init_m(c_odd) : NEG, OI = NEG, OD = NEG;   // last odd-column output
+    // last even / odd column outputs; they start as the initial row, which
+    // has M = 0 at every j of the window -- also just beyond the band, where
+    // the first processed row's last column looks up
+    int32_t EM = init_m(c_even), EI = NEG, ED = NEG;
+    int32_t OM = init_m(c_odd), OI = NEG, OD = NEG;
     unsigned long long bestKey = 0;
     unsigned long long cells = 0;
     uint32_t tbyte = 0;
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__(128) k_align_band(AlignArgs p) {
           lM = EM; lD = ED;                          // (i, 2k)
         }
         int32_t oM = NEG, oI = NEG, oD = NEG;
-        if (!on && i == R0 - 1 && col_ok) oM = init_m(c);  // the initial row, as the lane passes it
+        if (!on && i == R0 - 1) oM = init_m(c);  // the initial row, as the lane passes it
         if (on) {
           const int jj = (int)j;
           const int32_t sc = qs[i - 1] == rs[jj - 1] ? 20 : qmm[i - 1];

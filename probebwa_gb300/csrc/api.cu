@@ -28,6 +28,12 @@ using namespace pbw;
 
 static std::string g_open_err;
 
+namespace pbw {
+// Errors of calls without a handle (a failed pbw_open, handle-free entry
+// points), read through pbw_last_error(NULL).
+void set_handleless_error(const std::string& s) { g_open_err = s; }
+}  // namespace pbw
+
 // ---------------------------------------------------------------------------
 // small helpers
 // ---------------------------------------------------------------------------
@@ -99,10 +105,10 @@ static const double H_DB = -0.1 * H_LN_10;
 
 // Host parameter tables: quality- and integer-indexed values computed once
 // with the host libm (the same one the CPU reference path uses).
-static int build_tables(pbw_handle* h) {
-  DevTables T;
+namespace pbw {
+void fill_tables(const pbw_options& opt, uint64_t total_length, DevTables& T) {
   memset(&T, 0, sizeof(T));
-  const double sub = h->opt.substitution_rate;
+  const double sub = opt.substitution_rate;
   T.subphred = h_py_int_round(std::log(std::max(sub, 1e-30)) / H_DB);  // bayesian.rs:104
   for (int q = 0; q < 256; q++) {
     double eq = h_logadd((double)q, T.subphred);
@@ -118,21 +124,31 @@ static int build_tables(pbw_handle* h) {
   }
   for (int p = 0; p < 100; p++) T.pow_neg_tenth[p] = std::pow(10.0, -(double)p / 10.0);
   T.ln_quarter = std::log(0.25);
-  T.ln_two_g = std::log(2.0 * (double)std::max<uint64_t>(h->total_length, 1));
+  T.ln_two_g = std::log(2.0 * (double)std::max<uint64_t>(total_length, 1));
   T.ln30 = std::log(30.0);
   T.floor_wrong = std::exp(99.0 * H_DB);
   T.ln_floor_wrong = std::log(T.floor_wrong);
   T.log10_099 = std::log10(0.99);
   T.log10_1e30 = std::log10(1e-30);
-  T.sv_prior_log_prob = -h->opt.sv_prior_phred / 10.0 * H_LN_10;
-  int32_t go = h_sat_i32(std::round(-90.0 * (double)h->opt.gap_open_phred / 40.0));
-  int32_t ge = h_sat_i32(std::round(-1.0 * (double)h->opt.gap_extend_phred / 3.0));
-  T.gap_open = std::min(go, -1);
-  T.gap_extend = std::min(ge, -1);
-  const int LNMAX = 4096;
-  T.ln_n_max = LNMAX;
-  const int TMAX = 1280;
-  T.gc_tmax = TMAX;
+  T.sv_prior_log_prob = -opt.sv_prior_phred / 10.0 * H_LN_10;
+  gap_costs(opt.gap_open_phred, opt.gap_extend_phred, T.gap_open, T.gap_extend);
+  T.ln_n_max = 4096;
+  T.gc_tmax = 1280;
+}
+
+// SmithWatermanAligner::new (smith_waterman.rs:113-130): gap costs scaled
+// from the -90 / -1 baseline at --gapopen 40 / --gapextend 3, at most -1.
+void gap_costs(uint32_t gop, uint32_t gep, int32_t& go, int32_t& ge) {
+  go = std::min(h_sat_i32(std::round(-90.0 * (double)gop / 40.0)), -1);
+  ge = std::min(h_sat_i32(std::round(-1.0 * (double)gep / 3.0)), -1);
+}
+}  // namespace pbw
+
+static int build_tables(pbw_handle* h) {
+  DevTables T;
+  fill_tables(h->opt, h->total_length, T);
+  const int LNMAX = T.ln_n_max;
+  const int TMAX = T.gc_tmax;
   h->tab_host = T;
   TRY(dev_alloc(h, h->d_tab, 1));
   CK(cudaMemcpy(h->d_tab.p, &T, sizeof(T), cudaMemcpyHostToDevice));

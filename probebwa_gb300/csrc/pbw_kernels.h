@@ -2,9 +2,11 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "pbw_common.cuh"
+#include "../../include/probebwa_gpu.h"
 
 namespace pbw {
 
@@ -173,6 +175,11 @@ struct FinalizeArgs {
   int32_t* best;            // per read winning slot (-1 unmapped)
 };
 void launch_finalize(const FinalizeArgs& a, int grid, cudaStream_t st);
+
+// ---- host parameter tables (api.cu) ----
+void fill_tables(const pbw_options& opt, uint64_t total_length, DevTables& T);
+void gap_costs(uint32_t gop, uint32_t gep, int32_t& go, int32_t& ge);
+void set_handleless_error(const std::string& s);
 
 // ---- index build ----
 void launch_build_csr_counts(const uint32_t* tab, uint64_t n, uint64_t npos, unsigned int* counts, int* err,
