@@ -189,6 +189,37 @@ int pbw_map_single_device(pbw_handle* h, const pbw_reads* dev_reads, pbw_records
 int pbw_write_sam(pbw_handle* h, const char* path, const char* command_line, const pbw_reads* reads,
                   const char* const* read_ids, const pbw_records* recs);
 
+/* Allocation-free window alignment. No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc -- code running while a stream is
+ * captured into a CUDA graph, applications whose allocator owns all device
+ * memory, fixed-budget real-time loops. It performs the same alignment as
+ * pbw_align_batch (SmithWatermanAligner::align) on the wide-band DP kernel and
+ * needs no handle.
+ *
+ * Every pointer is DEVICE memory owned by the caller: n problems with reads /
+ * quals concatenated at read_off (n+1), reference windows concatenated at
+ * ref_off (n+1), hint[n], band[n]; outputs score[n], offset[n] (start of the
+ * alignment in its window), n_ops[n] and cigar[n * cigar_stride] ((len << 4) |
+ * op, op 0=M 1=I 2=D 4=S), the i-th CIGAR at cigar + i * cigar_stride.
+ * stream is a cudaStream_t (NULL = legacy default stream); the call returns
+ * after the stream has finished its work.
+ *
+ * Limits: n <= 4096 problems per call, reads <= 256 bases, windows <= 2048
+ * bases; beyond them PBW_ERR_LIMIT, and a CIGAR longer than cigar_stride gives
+ * PBW_ERR_CAPACITY; pbw_last_error(NULL) describes the failure.
+ *
+ * Scratch: a file-scope device array of about 20 MB, held on every GPU that
+ * loads the library until the process exits. The first call on a device (with
+ * that device current) looks up the array's device address and writes its
+ * parameter table; make that first call before any stream capture. Every call
+ * reuses the same array and clears its counters first, so calls that overlap
+ * on the GPU (two streams, two host threads) race and must be serialised by
+ * the caller. */
+int pbw_align_noalloc(uint64_t n, const uint8_t* reads, const uint8_t* quals, const uint64_t* read_off,
+                      const uint8_t* refs, const uint64_t* ref_off, const int64_t* hint, const uint64_t* band,
+                      uint32_t gap_open_phred, uint32_t gap_extend_phred, int32_t* score, uint64_t* offset,
+                      uint32_t* n_ops, uint32_t* cigar, uint32_t cigar_stride, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -116,6 +116,8 @@ def lib():
         L.pbw_cluster_batch.argtypes = [vp, C.POINTER(ReadsC), u32, vp, vp, vp, vp, vp, vp]
         L.pbw_last_stats.argtypes = [vp, C.POINTER(StatsC)]
         L.pbw_write_sam.argtypes = [vp, cp, cp, C.POINTER(ReadsC), C.POINTER(cp), C.POINTER(RecordsC)]
+        if hasattr(L, "pbw_align_noalloc"):
+            L.pbw_align_noalloc.argtypes = [u64, vp, vp, vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, u32, vp]
         _lib = L
     return _lib
 
