@@ -208,7 +208,7 @@ int pbw_write_sam(pbw_handle* h, const char* path, const char* command_line, con
  * bases; beyond them PBW_ERR_LIMIT, and a CIGAR longer than cigar_stride gives
  * PBW_ERR_CAPACITY; pbw_last_error(NULL) describes the failure.
  *
- * Scratch: a file-scope device array of about 20 MB, held on every GPU that
+ * Scratch: a file-scope device array of about 6 MB, held on every GPU that
  * loads the library until the process exits. The first call on a device (with
  * that device current) looks up the array's device address and writes its
  * parameter table; make that first call before any stream capture. Every call

@@ -11,7 +11,7 @@
 // one step earlier): two shuffles per step, and every lane computes one cell
 // per step -- 2*m + 2*band + 2 steps per alignment. The traceback of a row is
 // one byte per lane (both columns' nibbles), 32 bytes per row in shared
-// memory. Integer semantics are those of the row-strip kernel (align.cu).
+// memory. Integer semantics are those of the window kernel (align_window.cu).
 #include "align_finish.cuh"
 #include "pbw_common.cuh"
 #include "pbw_kernels.h"

@@ -1,5 +1,6 @@
 // align_finish.cuh -- traceback and per-alignment bookkeeping shared by the
-// two DP kernels (row strips: align.cu, column tiles: align_wide.cu).
+// two DP kernels (anti-diagonal band: align_band.cu, column tiles:
+// align_window.cu).
 //
 // traceback (src/align/smith_waterman.rs:299-344): from (m, endJ, endS),
 // j == 0 emits an insertion; M follows tb_m to the parent state and moves

@@ -5,7 +5,7 @@
 //   K1 k_seed            seed hits + repeat codes            (seed.cu)
 //   K2 k_cluster x2      candidates (small / large hit sets)  (cluster.cu)
 //      k_make_jobs       candidate windows -> work queue       (mapq.cu)
-//   K3 k_align           banded DP + traceback + likelihood    (align.cu)
+//   K3 k_align_band      banded DP + traceback + likelihood    (align_band.cu)
 //   K4 k_finalize        select_best + MAPQ -> records         (mapq.cu)
 //      scan + gather     packed CIGARs                         (mapq.cu)
 #include <algorithm>

@@ -1,10 +1,9 @@
 // noalloc.cu -- window alignment for callers that cannot allocate device memory.
 //
-// pbw_align_noalloc runs the wide DP of align_wide.cu (the kernel whose
-// traceback lives in global scratch) with every piece of scratch -- jobs,
-// per-alignment outputs, queue counters, the CIGAR overflow pool, the
-// per-warp traceback slabs and the parameter table -- inside one file-scope
-// device array. Inputs and outputs are device memory owned by the caller.
+// pbw_align_noalloc runs the window DP of align_window.cu with every piece of
+// scratch -- jobs, per-alignment outputs, queue counters, the CIGAR overflow
+// pool, the per-block slabs for windows too large for shared memory and the
+// parameter table -- inside one file-scope device array. Inputs and outputs are device memory owned by the caller.
 // Callers that are not allowed to call cudaMalloc (code running while a
 // stream is being captured into a CUDA graph, allocators that own all device
 // memory, real-time loops with a fixed memory budget) can call it; it calls no
@@ -23,21 +22,18 @@ namespace pbw {
 constexpr uint64_t NA_MAX_PROBLEMS = 4096;
 constexpr int NA_MAX_READ = 256;
 constexpr int NA_MAX_REF = 2048;
-constexpr int NA_BLOCKS = 16;                 // 4 warps each
-constexpr int NA_WARPS = NA_BLOCKS * 4;
+constexpr int NA_BLOCKS = 16;                 // window kernel blocks (8 warps each)
 constexpr uint64_t NA_POOL_OPS = NA_MAX_PROBLEMS * 64;
 
 constexpr size_t na16(size_t x) { return (x + 255) & ~(size_t)255; }
-constexpr size_t NA_SLAB = ((4 * (size_t)NA_MAX_REF + 15) & ~(size_t)15) +
-                           ((4 * ((size_t)NA_MAX_REF + 1) * (((size_t)NA_MAX_READ + 8) / 8) + 15) & ~(size_t)15) +
-                           (((size_t)NA_MAX_READ + NA_MAX_REF + 2 + 15) & ~(size_t)15);
+constexpr size_t NA_SLAB = window_slab_bytes(NA_MAX_READ, NA_MAX_REF);
 constexpr size_t NA_OFF_TAB = 0;
 constexpr size_t NA_OFF_CNT = na16(NA_OFF_TAB + sizeof(DevTables));
 constexpr size_t NA_OFF_JOBS = na16(NA_OFF_CNT + 64);
 constexpr size_t NA_OFF_OUT = na16(NA_OFF_JOBS + NA_MAX_PROBLEMS * sizeof(AlnJob));
 constexpr size_t NA_OFF_POOL = na16(NA_OFF_OUT + NA_MAX_PROBLEMS * sizeof(AlnOut));
 constexpr size_t NA_OFF_SLAB = na16(NA_OFF_POOL + NA_POOL_OPS * 4);
-constexpr size_t NA_BYTES = na16(NA_OFF_SLAB + NA_SLAB * NA_WARPS);  // about 20 MB
+constexpr size_t NA_BYTES = na16(NA_OFF_SLAB + NA_SLAB * NA_BLOCKS);  // about 6 MB
 
 // The scratch. Every GPU that loads this library holds it until the process
 // exits. In host code the name is only a handle for cudaGetSymbolAddress.
@@ -185,7 +181,7 @@ extern "C" int pbw_align_noalloc(uint64_t n, const uint8_t* reads, const uint8_t
   aa.tb_global_per_warp = NA_SLAB;
   aa.counters = nullptr;
   aa.err = (int*)(cnt + 3);
-  launch_align_wide(aa, NA_BLOCKS, st);
+  launch_align_window(aa, NA_BLOCKS, st);
   k_noalloc_out<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, ref_off, base, score, offset, n_ops, cigar,
                                                               cigar_stride);
   cudaError_t e = cudaGetLastError();

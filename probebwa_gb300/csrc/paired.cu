@@ -466,25 +466,98 @@ __global__ void k_pair_resolve(PairArgs p) {
 
 // InsertSizeDistribution::update (insert_size.rs:32-44), folded serially in
 // pair order, then the next batch's ln(2*pi*sd^2) (insert_size.rs:29).
-__global__ void k_fold_model(PairModel* M, const double* obs, uint32_t p0, uint32_t np) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double mean = M->mean, sd = M->sd;
-  unsigned long long n = M->n;
-  for (uint32_t i = 0; i < np; i++) {
-    const double x = obs[p0 + i];
-    if (isnan(x)) continue;
-    n++;
-    const double nn = (double)n;
-    const double delta = x - mean;
-    mean += delta / nn;
-    const double delta2 = x - mean;
-    const double var = nn > 1.0 ? ((sd * sd) * (nn - 1.0) + delta * delta2) / nn : sd * sd;
-    sd = fmax(sqrt(var), 1.0);
+//
+// The recurrence is serial, so its latency per observation is what counts.
+// The block first stages a tile of observations in shared memory, drops the
+// NaNs (pairs that gave no observation), and gives every kept observation its
+// count nn and the correctly rounded reciprocal 1/nn, all in parallel. One
+// thread then runs the recurrence from shared memory, dividing by nn with
+// Markstein's correction (y = RN(1/nn), q0 = RN(a*y), r = a - q0*nn exactly
+// by FMA, q = RN(q0 + r*y)), which is the correctly rounded a/nn because y is
+// within half an ulp of 1/nn and q0 within one ulp of a/nn (P. Markstein,
+// IBM J. Res. Dev. 34(1), 1990). The results are those of IEEE division.
+constexpr int FOLD_THREADS = 256;
+constexpr int FOLD_TILE = 1024;
+
+__device__ __forceinline__ double div_by_count(double a, double nn, double y) {
+  const double q0 = a * y;
+  const double r = fma(-q0, nn, a);
+  return fma(r, y, q0);
+}
+
+__global__ void __launch_bounds__(FOLD_THREADS) k_fold_model(PairModel* M, const double* obs, uint32_t p0,
+                                                             uint32_t np) {
+  __shared__ double xs[FOLD_TILE];
+  __shared__ double nns[FOLD_TILE];
+  __shared__ double rcp[FOLD_TILE];
+  __shared__ uint32_t warp_cnt[FOLD_THREADS / 32];
+  __shared__ double s_mean, s_sd;
+  __shared__ unsigned long long s_n;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) {
+    s_mean = M->mean;
+    s_sd = M->sd;
+    s_n = M->n;
   }
-  M->mean = mean;
-  M->sd = sd;
-  M->n = n;
-  M->ln_2pi_sd2 = log(2.0 * 3.141592653589793115997963468544185161590576171875 * sd * sd);
+  constexpr int PER = FOLD_TILE / FOLD_THREADS;  // consecutive observations per thread
+  for (uint32_t base = 0; base < np; base += FOLD_TILE) {
+    __syncthreads();
+    const uint32_t cnt_tile = min((uint32_t)FOLD_TILE, np - base);
+    double v[PER];
+    uint32_t mine = 0;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      const uint32_t i = (uint32_t)t * PER + k;
+      v[k] = i < cnt_tile ? obs[p0 + base + i] : __longlong_as_double(0x7ff8000000000000ll);
+      mine += isnan(v[k]) ? 0u : 1u;
+    }
+    // exclusive prefix of kept observations over the block, in pair order
+    uint32_t incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += o;
+    }
+    if (lane == 31) warp_cnt[w] = incl;
+    __syncthreads();
+    uint32_t before = incl - mine, total = 0;
+    for (int k = 0; k < FOLD_THREADS / 32; k++) {
+      if (k < w) before += warp_cnt[k];
+      total += warp_cnt[k];
+    }
+    const unsigned long long n0 = s_n;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      if (isnan(v[k])) continue;
+      const double nn = (double)(n0 + before + 1);
+      xs[before] = v[k];
+      nns[before] = nn;
+      rcp[before] = 1.0 / nn;
+      before++;
+    }
+    __syncthreads();
+    if (t == 0) {
+      double mean = s_mean, sd = s_sd;
+      for (uint32_t j = 0; j < total; j++) {
+        const double x = xs[j], nn = nns[j], y = rcp[j];
+        const double delta = x - mean;
+        mean = mean + div_by_count(delta, nn, y);
+        const double delta2 = x - mean;
+        const double var = nn > 1.0 ? div_by_count((sd * sd) * (nn - 1.0) + delta * delta2, nn, y) : sd * sd;
+        sd = fmax(sqrt(var), 1.0);
+      }
+      s_mean = mean;
+      s_sd = sd;
+      s_n = n0 + total;
+    }
+  }
+  if (t == 0) {
+    const double sd = s_sd;
+    M->mean = s_mean;
+    M->sd = sd;
+    M->n = s_n;
+    M->ln_2pi_sd2 = log(2.0 * 3.141592653589793115997963468544185161590576171875 * sd * sd);
+  }
 }
 
 __global__ void k_pair_cigar_gather(const PairArgs p, const uint32_t* cig_off, const uint32_t* cig_pool, uint32_t* cigar,
@@ -515,7 +588,7 @@ void launch_pair_resolve(const PairArgs& a, cudaStream_t st) {
   k_pair_resolve<<<(a.np + 127) / 128, 128, 0, st>>>(a);
 }
 void launch_fold_model(PairModel* M, const double* obs, uint32_t p0, uint32_t np, cudaStream_t st) {
-  k_fold_model<<<1, 32, 0, st>>>(M, obs, p0, np);
+  k_fold_model<<<1, FOLD_THREADS, 0, st>>>(M, obs, p0, np);
 }
 void launch_pair_cigar_gather(const PairArgs& a, const uint32_t* cig_off, const uint32_t* cig_pool, uint32_t* cigar,
                               uint64_t g0, uint32_t n, cudaStream_t st) {

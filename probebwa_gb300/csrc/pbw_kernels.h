@@ -133,18 +133,26 @@ struct AlignArgs {
   const uint8_t* ref_bytes;
   int lmax;                 // longest query
   int nmax;                 // longest reference window
-  size_t tb_smem;           // bytes of shared traceback per warp
-  unsigned char* tb_global; // traceback scratch for windows too wide for shared memory
-  size_t tb_global_per_warp;
+  size_t tb_smem;           // unused (0)
+  unsigned char* tb_global; // K3w: per-block slabs for windows too wide for shared memory
+  size_t tb_global_per_warp;  // K3w: bytes of one block's slab
   unsigned long long* counters;  // jobs, cells
   int* err;
 };
-void launch_align(const AlignArgs& a, int grid, cudaStream_t st);
-void launch_align_wide(const AlignArgs& a, int grid, cudaStream_t st);
 void launch_align_band(const AlignArgs& a, int grid, cudaStream_t st);
 size_t band_smem_per_warp(int lmax, int nmax);
-size_t wide_slab_bytes(int lmax, int nmax);
-size_t align_smem_per_warp(int lmax, int nmax, size_t tb_smem);
+// K3w, one job per block of 8 warps; tb_global_per_warp is the global slab of
+// one block (window_slab_bytes), used by windows that do not fit the block's
+// shared memory.
+void launch_align_window(const AlignArgs& a, int grid, cudaStream_t st);
+size_t window_smem_bytes(int lmax, int nmax);
+// per job: window symbols, gap opens, traceback ops, (lmax + 7) / 8 traceback
+// words per column; 16-byte aligned pieces
+constexpr size_t window_slab_bytes(int lmax, int nmax) {
+  return (((size_t)nmax + 15) & ~(size_t)15) + ((4 * (size_t)nmax + 15) & ~(size_t)15) +
+         (((size_t)lmax + nmax + 2 + 15) & ~(size_t)15) +
+         ((4 * ((size_t)nmax + 1) * (((size_t)lmax + 7) / 8) + 15) & ~(size_t)15);
+}
 
 // ---- K4 finalize (single-end) ----
 struct FinalizeArgs {

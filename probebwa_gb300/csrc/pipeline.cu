@@ -66,8 +66,6 @@ struct ChunkCfg {
   uint32_t hcap;
   uint32_t wcap;
   int nmax;         // longest reference window
-  size_t tb_smem;   // shared traceback bytes per warp
-  size_t tb_glob;   // global traceback bytes per warp (0 = none)
 };
 
 static ChunkCfg chunk_cfg(pbw_handle* h, uint64_t n, int lmax) {
@@ -78,20 +76,17 @@ static ChunkCfg chunk_cfg(pbw_handle* h, uint64_t n, int lmax) {
   c.wcap = (uint32_t)std::max(c.lmax - KMER + 1, 1);
   const uint64_t rp = std::max<uint64_t>(h->opt.max_indel_len, 10);
   c.nmax = (int)(c.lmax + 10 + rp);
-  const uint64_t band = h->opt.max_indel_len;
-  const size_t width = band <= 31 ? 2 * band + 1 : (size_t)c.nmax + 1;
-  const size_t need = (size_t)c.lmax * ((width + 7) / 8) * 4;
-  if (need <= 48 * 1024) {
-    c.tb_smem = need;
-    c.tb_glob = 0;
-  } else {
-    c.tb_smem = 0;
-    c.tb_glob = need;
-  }
   return c;
 }
 
-static int ensure_chunk(pbw_handle* h, const ChunkCfg& c, int align_grid_warps) {
+// Blocks of the window kernel (K3w) and its global slab for windows that do
+// not fit a block's shared memory.
+static int window_grid(pbw_handle* h) { return h->num_sms * 2; }
+static int ensure_window_slab(pbw_handle* h, int lmax, int nmax, int grid) {
+  return grow(h, h->d_tb_global, window_slab_bytes(lmax, nmax) * (size_t)grid);
+}
+
+static int ensure_chunk(pbw_handle* h, const ChunkCfg& c) {
   TRY(grow(h, h->d_hits, (size_t)c.ch * c.hcap));
   TRY(grow(h, h->d_hit_cnt, c.ch));
   TRY(grow(h, h->d_overflow, c.ch));
@@ -108,9 +103,7 @@ static int ensure_chunk(pbw_handle* h, const ChunkCfg& c, int align_grid_warps) 
   TRY(grow(h, h->d_list_hoff, c.ch));
   TRY(grow(h, h->d_hits_pool, OVF_POOL_HITS));
   TRY(grow(h, h->d_cl_scratch, OVF_POOL_HITS * 112));
-  if (c.tb_glob) TRY(grow(h, h->d_tb_global, c.tb_glob * (size_t)align_grid_warps));
-  if (h->opt.max_indel_len > 31)
-    TRY(grow(h, h->d_tb_global, wide_slab_bytes(c.lmax, c.nmax) * (size_t)h->num_sms * 16));
+  if (h->opt.max_indel_len > 31) TRY(ensure_window_slab(h, c.lmax, c.nmax, window_grid(h)));
   return PBW_OK;
 }
 
@@ -131,12 +124,6 @@ static int ensure_outputs(pbw_handle* h, uint64_t n, uint64_t cig_cap) {
   TRY(grow(h, h->o_cig_off, n + 1));
   TRY(grow(h, h->o_cigar, cig_cap));
   return PBW_OK;
-}
-
-static int align_grid(pbw_handle* h, int lmax, int nmax, size_t tb_smem) {
-  size_t per_block = align_smem_per_warp(lmax, nmax, tb_smem) * 4;
-  int bps = (int)std::max<size_t>(1, std::min<size_t>(8, (h->smem_optin ? 228 * 1024 : 100 * 1024) / per_block));
-  return h->num_sms * bps;
 }
 
 // Resident blocks of the anti-diagonal band kernel (4 warps per block).
@@ -175,7 +162,7 @@ struct MateBufs {
 // ev[0..3] mark seed / cluster / align boundaries. reset_pool clears the
 // CIGAR pool (the first read set of a chunk).
 static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
-                          const uint64_t* offs, uint32_t r0, uint32_t nr, int grid_align, const MateBufs& mb,
+                          const uint64_t* offs, uint32_t r0, uint32_t nr, const MateBufs& mb,
                           cudaEvent_t* ev, bool reset_pool) {
   cudaStream_t st = h->st;
   unsigned int* c32 = h->d_cnt32.p;
@@ -290,19 +277,17 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   aa.ref_bytes = nullptr;
   aa.lmax = cfg.lmax;
   aa.nmax = cfg.nmax;
-  aa.tb_smem = cfg.tb_smem;
-  aa.tb_global = h->d_tb_global.p;
-  aa.tb_global_per_warp = cfg.tb_glob;
+  aa.tb_smem = 0;
+  aa.tb_global = nullptr;
+  aa.tb_global_per_warp = 0;
   aa.counters = h->d_cnt64.p + 3;
   aa.err = h->d_err.p;
   if (h->opt.max_indel_len <= 31) {
-    (void)grid_align;
     launch_align_band(aa, band_grid(h, cfg.lmax, cfg.nmax), st);
   } else {
-    aa.tb_smem = 0;
     aa.tb_global = h->d_tb_global.p;
-    aa.tb_global_per_warp = wide_slab_bytes(cfg.lmax, cfg.nmax);
-    launch_align_wide(aa, h->num_sms * 4, st);
+    aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, cfg.nmax);
+    launch_align_window(aa, window_grid(h), st);
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[3], st));
@@ -313,11 +298,11 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
 // One chunk of single-end reads: seeding through finalize and CIGAR gather.
 // Per-phase event pairs are recorded into ev (5 phases).
 static int run_chunk_single(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
-                            const uint64_t* offs, uint32_t r0, uint32_t nr, int grid_align, cudaEvent_t* ev) {
+                            const uint64_t* offs, uint32_t r0, uint32_t nr, cudaEvent_t* ev) {
   cudaStream_t st = h->st;
   unsigned int* c32 = h->d_cnt32.p;
   MateBufs mb{h->d_cand.p, h->d_n_cand.p, h->d_aln.p, h->d_rep.p, 0};
-  TRY(run_seed_align(h, cfg, bases, quals, offs, r0, nr, grid_align, mb, ev, true));
+  TRY(run_seed_align(h, cfg, bases, quals, offs, r0, nr, mb, ev, true));
   FinalizeArgs fa{};
   fa.G = h->G;
   fa.tab = h->d_tab.p;
@@ -442,8 +427,7 @@ static int validate_reads(pbw_handle* h, const pbw_reads* r, uint64_t& total, in
 static int map_single_dev(pbw_handle* h, const uint8_t* d_bases, const uint8_t* d_quals, const uint64_t* d_offs,
                           uint64_t n, uint64_t total_bases, int lmax, pbw_records* out) {
   ChunkCfg cfg = chunk_cfg(h, n, lmax);
-  int grid = align_grid(h, cfg.lmax, cfg.nmax, cfg.tb_smem);
-  TRY(ensure_chunk(h, cfg, grid * 4));
+  TRY(ensure_chunk(h, cfg));
   TRY(ensure_outputs(h, std::max<uint64_t>(n, 1), 2 * total_bases + 2 * n + 16));
   CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * sizeof(unsigned int), h->st));
   CK(cudaMemsetAsync(h->d_cnt64.p, 0, 16 * sizeof(unsigned long long), h->st));
@@ -455,7 +439,7 @@ static int map_single_dev(pbw_handle* h, const uint8_t* d_bases, const uint8_t* 
   for (uint64_t r0 = 0; r0 < n; r0 += cfg.ch) {
     uint32_t nr = (uint32_t)std::min<uint64_t>(cfg.ch, n - r0);
     cudaEvent_t* ev = &h->events[ev_next];
-    TRY(run_chunk_single(h, cfg, d_bases, d_quals, d_offs, (uint32_t)r0, nr, grid, ev));
+    TRY(run_chunk_single(h, cfg, d_bases, d_quals, d_offs, (uint32_t)r0, nr, ev));
     // accumulate phase times once the chunk's events complete (next sync)
     CK(cudaEventSynchronize(ev[4]));
     t_seed += ms_between(ev[0], ev[1]);
@@ -522,8 +506,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   const uint64_t S = std::max<uint64_t>(h->opt.chunk_reads, 2000);
   ChunkCfg cfg = chunk_cfg(h, std::min<uint64_t>(n, S), lmax);
   cfg.ch = (uint32_t)std::min<uint64_t>(n, S);
-  const int grid_s = align_grid(h, cfg.lmax, cfg.nmax, cfg.tb_smem);
-  TRY(ensure_chunk(h, cfg, grid_s * 4));
+  TRY(ensure_chunk(h, cfg));
   const uint32_t ch = cfg.ch;
   TRY(grow(h, h->d_cand2, (size_t)ch * MAX_CAND));
   TRY(grow(h, h->d_n_cand2, ch));
@@ -545,9 +528,8 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   TRY(grow(h, h->o_len, std::max<uint64_t>(n2, 1)));
   // wide DP: window = L + 2 * (ceil(5 sd) + L); slabs sized for 8192 columns
   const int wide_n = 8192;
-  const int grid_w = h->num_sms * 4;
-  const size_t slab = wide_slab_bytes(cfg.lmax, wide_n);
-  TRY(grow(h, h->d_tb_global, slab * (size_t)grid_w * 4));
+  const int grid_w = window_grid(h);
+  TRY(ensure_window_slab(h, cfg.lmax, wide_n, grid_w));
   PairModel pm;
   pm.mean = model->mean;
   pm.sd = model->sd;
@@ -571,12 +553,12 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     // phase A: both mates through K1-K3 and the per-read summaries
     MateBufs m1{h->d_cand.p, h->d_n_cand.p, h->d_aln.p, h->d_rep.p, 0};
     MateBufs m2{h->d_cand2.p, h->d_n_cand2.p, h->d_aln2.p, h->d_rep2.p, 0};
-    TRY(run_seed_align(h, cfg, b1, q1, of1, (uint32_t)a, nr, grid_s, m1, ev, true));
+    TRY(run_seed_align(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, true));
     CK(cudaEventSynchronize(ev[3]));
     t_seed += ms_between(ev[0], ev[1]);
     t_cl += ms_between(ev[1], ev[2]);
     t_al += ms_between(ev[2], ev[3]);
-    TRY(run_seed_align(h, cfg, b2, q2, of2, (uint32_t)a, nr, grid_s, m2, ev, false));
+    TRY(run_seed_align(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev, false));
     CK(cudaEventSynchronize(ev[3]));
     t_seed += ms_between(ev[0], ev[1]);
     t_cl += ms_between(ev[1], ev[2]);
@@ -664,7 +646,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     aa.nmax = wide_n;
     aa.tb_smem = 0;
     aa.tb_global = h->d_tb_global.p;
-    aa.tb_global_per_warp = slab;
+    aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, wide_n);
     aa.counters = h->d_cnt64.p + 3;
     aa.err = h->d_err.p;
     for (size_t k = bi; k < be; k++) {
@@ -672,8 +654,8 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       pa.np = (uint32_t)batches[k].second;
       CK(cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st));
       launch_pair_decide(pa, st);
-      const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, ((uint64_t)pa.np * MAX_CROSS + 3) / 4);
-      launch_align_wide(aa, std::max(gw, 1), st);
+      const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, (uint64_t)pa.np * MAX_CROSS);
+      launch_align_window(aa, std::max(gw, 1), st);
       launch_pair_resolve(pa, st);
       launch_fold_model(h->d_model.p, h->d_obs.p, pa.p0, pa.np, st);
       h->stats.kernel_launches += 4;
@@ -865,7 +847,7 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
   CK(cudaMemcpy(h->d_quals.p, quals, qtot, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_offs.p, read_off, (n + 1) * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_bases2.p, refs, rtot, cudaMemcpyHostToDevice));
-  // band <= 31: row-strip kernel with shared traceback; wider: column tiles
+  // band <= 31: anti-diagonal band kernel; wider: window kernel (column tiles)
   std::vector<AlnJob> js, jw;
   int lmax_s = 1, nmax_s = 1, lmax_w = 1, nmax_w = 1;
   for (uint64_t i = 0; i < n; i++) {
@@ -935,9 +917,8 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
     unsigned int cnt = (unsigned int)jw.size();
     CK(cudaMemcpy(h->d_cnt32.p + 0, &cnt, 4, cudaMemcpyHostToDevice));
     CK(cudaMemset(h->d_cnt32.p + 1, 0, 4));
-    const int grid = h->num_sms * 4;
-    const size_t slab = wide_slab_bytes(lmax_w, nmax_w);
-    TRY(grow(h, h->d_tb_global, slab * (size_t)grid * 4));
+    const int grid = window_grid(h);
+    TRY(ensure_window_slab(h, lmax_w, nmax_w, grid));
     aa.jobs = h->d_jobs.p;
     aa.n_jobs = h->d_cnt32.p + 0;
     aa.next_job = h->d_cnt32.p + 1;
@@ -945,8 +926,8 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
     aa.nmax = nmax_w;
     aa.tb_smem = 0;
     aa.tb_global = h->d_tb_global.p;
-    aa.tb_global_per_warp = slab;
-    launch_align_wide(aa, grid, h->st);
+    aa.tb_global_per_warp = window_slab_bytes(lmax_w, nmax_w);
+    launch_align_window(aa, grid, h->st);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->st));
   }
