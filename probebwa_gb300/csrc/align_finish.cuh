@@ -18,8 +18,9 @@ namespace pbw {
 
 // tbr(i, j) -> traceback nibble (tb_m | tb_i << 2 | tb_d << 3), 0 outside.
 // rsym(j)   -> reference symbol (ASCII) at window index j (0-based).
-template <class TbRead, class RefSym>
-__device__ void finish_alignment(int m, int endV, int endJ, int endS, const uint8_t* qs, const uint8_t* qq,
+// qs(i), qq(i) -> query symbol and Phred quality at read index i (0-based).
+template <class TbRead, class RefSym, class QSym, class QQual>
+__device__ void finish_alignment(int m, int endV, int endJ, int endS, QSym qs, QQual qq,
                                  uint8_t* ops, TbRead tbr, RefSym rsym, unsigned long long ref_start,
                                  const DevTables* T, AlnOut* O, uint32_t* cig_pool, unsigned int* cig_pool_used,
                                  uint32_t cig_pool_cap, int* err) {
@@ -91,8 +92,8 @@ __device__ void finish_alignment(int m, int endV, int endJ, int endS, const uint
       if (cur != 0) indel_runs++;
       cur = 0;
       if (qi < m && ri < span) {
-        const uint8_t a = qs[qi], r = rsym(off + ri);
-        const uint8_t q = qq[qi];
+        const uint8_t a = qs(qi), r = rsym(off + ri);
+        const uint8_t q = qq(qi);
         lk += a == r ? T->llk_match[q] : T->llk_mismatch[q];
         const bool hq = q >= 10;
         if (hq) n_hq++;

@@ -353,7 +353,9 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
         return (tb[(size_t)j * TBS + (rr >> 3)] >> ((rr & 7) * 4)) & 15u;
       };
       auto rsym = [&](int j) -> uint8_t { return rs[j]; };
-      finish_alignment(m, endV, endJ, endS, qs, qq, ops, tbr, rsym, J.ref_start, p.tab, O, p.cig_pool,
+      auto qsym = [&](int i) -> uint8_t { return qs[i]; };
+      auto qqual = [&](int i) -> uint8_t { return qq[i]; };
+      finish_alignment(m, endV, endJ, endS, qsym, qqual, ops, tbr, rsym, J.ref_start, p.tab, O, p.cig_pool,
                        p.cig_pool_used, p.cig_pool_cap, p.err);
     }
     __syncthreads();

@@ -139,8 +139,9 @@ struct AlignArgs {
   unsigned long long* counters;  // jobs, cells
   int* err;
 };
-void launch_align_band(const AlignArgs& a, int grid, cudaStream_t st);
-size_t band_smem_per_warp(int lmax, int nmax);
+// K3b, band <= band_max <= 31; grid sized from the shared memory per warp.
+void launch_align_band(const AlignArgs& a, int num_sms, int band_max, cudaStream_t st);
+size_t band_smem_bytes(int lmax, int nmax);  // per warp at 8 columns per lane
 // K3w, one job per block of 8 warps; tb_global_per_warp is the global slab of
 // one block (window_slab_bytes), used by windows that do not fit the block's
 // shared memory.

@@ -127,12 +127,6 @@ static int ensure_outputs(pbw_handle* h, uint64_t n, uint64_t cig_cap) {
 }
 
 // Resident blocks of the anti-diagonal band kernel (4 warps per block).
-static int band_grid(pbw_handle* h, int lmax, int nmax) {
-  const size_t per_block = band_smem_per_warp(lmax, nmax) * 4;
-  const int bps = (int)std::max<size_t>(1, std::min<size_t>(12, (220 * 1024) / per_block));
-  return h->num_sms * bps;
-}
-
 struct Timer {
   pbw_handle* h;
   int next = 0;
@@ -283,7 +277,7 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   aa.counters = h->d_cnt64.p + 3;
   aa.err = h->d_err.p;
   if (h->opt.max_indel_len <= 31) {
-    launch_align_band(aa, band_grid(h, cfg.lmax, cfg.nmax), st);
+    launch_align_band(aa, h->num_sms, (int)h->opt.max_indel_len, st);
   } else {
     aa.tb_global = h->d_tb_global.p;
     aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, cfg.nmax);
@@ -849,7 +843,7 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
   CK(cudaMemcpy(h->d_bases2.p, refs, rtot, cudaMemcpyHostToDevice));
   // band <= 31: anti-diagonal band kernel; wider: window kernel (column tiles)
   std::vector<AlnJob> js, jw;
-  int lmax_s = 1, nmax_s = 1, lmax_w = 1, nmax_w = 1;
+  int lmax_s = 1, nmax_s = 1, lmax_w = 1, nmax_w = 1, bmax_s = 0;
   for (uint64_t i = 0; i < n; i++) {
     AlnJob J;
     memset(&J, 0, sizeof(J));
@@ -864,10 +858,13 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
     J.gap_extend = h->tab_host.gap_extend;
     const int m = (int)(read_off[i + 1] - read_off[i]);
     const int nn = (int)(ref_off[i + 1] - ref_off[i]);
-    if (band[i] <= 31) {
+    // K3b holds the read and window of four alignments per warp in shared
+    // memory: bands <= 31 over windows of at most 1280 columns
+    if (band[i] <= 31 && nn <= 1280) {
       js.push_back(J);
       lmax_s = std::max(lmax_s, m);
       nmax_s = std::max(nmax_s, nn);
+      bmax_s = std::max(bmax_s, (int)band[i]);
     } else {
       jw.push_back(J);
       lmax_w = std::max(lmax_w, m);
@@ -899,16 +896,15 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
     unsigned int cnt = (unsigned int)js.size();
     CK(cudaMemcpy(h->d_cnt32.p + 0, &cnt, 4, cudaMemcpyHostToDevice));
     CK(cudaMemset(h->d_cnt32.p + 1, 0, 4));
-    const size_t tb_smem = (size_t)lmax_s * 8 * 4;
     aa.jobs = h->d_jobs.p;
     aa.n_jobs = h->d_cnt32.p + 0;
     aa.next_job = h->d_cnt32.p + 1;
     aa.lmax = lmax_s;
     aa.nmax = nmax_s;
-    aa.tb_smem = tb_smem;
+    aa.tb_smem = 0;
     aa.tb_global = nullptr;
     aa.tb_global_per_warp = 0;
-    launch_align_band(aa, band_grid(h, lmax_s, nmax_s), h->st);
+    launch_align_band(aa, h->num_sms, bmax_s, h->st);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->st));
   }
