@@ -24,38 +24,30 @@ __device__ void finish_alignment(int m, int endV, int endJ, int endS, QSym qs, Q
                                  uint8_t* ops, TbRead tbr, RefSym rsym, unsigned long long ref_start,
                                  const DevTables* T, AlnOut* O, uint32_t* cig_pool, unsigned int* cig_pool_used,
                                  uint32_t cig_pool_cap, int* err) {
+  // The loops below are written without data-dependent branches so that the
+  // lanes of one warp that finish different alignments stay converged.
+  // traceback, ops in reverse order: 0 = M, 1 = I, 2 = D
   int i = m, j = endJ, st = endS, nops = 0;
   while (i > 0) {
-    if (j == 0) {
-      ops[nops++] = 1;
-      i--;
-      continue;
-    }
-    const uint32_t nib = tbr(i, j);
-    if (st == 0) {
-      ops[nops++] = 0;
-      i--;
-      j--;
-      st = (int)(nib & 3u);
-    } else if (st == 1) {
-      ops[nops++] = 1;
-      i--;
-      st = (nib & 4u) ? 1 : 0;
-    } else {
-      ops[nops++] = 2;
-      j--;
-      st = (nib & 8u) ? 2 : 0;
-    }
+    const bool j0 = j == 0;
+    const uint32_t nib = j0 ? 0u : tbr(i, j);
+    const int op = j0 ? 1 : st;
+    const int from_m = (int)(nib & 3u), from_i = (int)((nib >> 2) & 1u), from_d = (int)((nib >> 2) & 2u);
+    const int nst = j0 ? st : (st == 0 ? from_m : (st == 1 ? from_i : from_d));
+    ops[nops++] = (uint8_t)op;
+    i -= op != 2 ? 1 : 0;
+    j -= op != 1 ? 1 : 0;
+    st = nst;
   }
   const int off = j;
+  // runs (collapse_cigar) and cigar_reference_span
   uint32_t ncig = 0;
-  int lastop = -1;
+  int span = 0, lastop = -1;
   for (int k = nops - 1; k >= 0; k--) {
     const int op = ops[k];
-    if (op != lastop) {
-      ncig++;
-      lastop = op;
-    }
+    ncig += op != lastop ? 1u : 0u;
+    lastop = op;
+    span += op != 1 ? 1 : 0;
   }
   uint32_t pool_base = 0xFFFFFFFFu;
   if (ncig > CIG_INLINE) {
@@ -66,70 +58,45 @@ __device__ void finish_alignment(int m, int endV, int endJ, int endS, QSym qs, Q
     }
   }
   uint32_t* cdst = ncig > CIG_INLINE ? (pool_base != 0xFFFFFFFFu ? cig_pool + pool_base : nullptr) : O->cig;
+  // forward walk: CIGAR runs, likelihood (sequential FP64 sum in op order),
+  // log_entropy counts, edit distance, GC of the reference span
   uint32_t ci = 0, run = 0;
-  int span = 0;
   lastop = -1;
-  for (int k = nops - 1; k >= 0; k--) {
-    const int op = ops[k];
-    if (op != lastop) {
-      if (lastop >= 0) {
-        if (cdst) cdst[ci] = (run << 4) | (uint32_t)lastop;
-        ci++;
-      }
-      lastop = op;
-      run = 0;
-    }
-    run++;
-    if (op != 1) span++;
-  }
-  if (lastop >= 0 && cdst) cdst[ci] = (run << 4) | (uint32_t)lastop;
   double lk = 0.0;
   int qi = 0, ri = 0;
-  int n_hq = 0, m_hq = 0, readlen = 0, indel_runs = 0, del_runs = 0, cur = 0, nm = 0;
+  int n_hq = 0, m_hq = 0, readlen = 0, indel_runs = 0, del_runs = 0, cur = 0, nm = 0, gc = 0, tot = 0;
   for (int k = nops - 1; k >= 0; k--) {
     const int op = ops[k];
-    if (op == 0) {
-      if (cur != 0) indel_runs++;
-      cur = 0;
-      if (qi < m && ri < span) {
-        const uint8_t a = qs(qi), r = rsym(off + ri);
-        const uint8_t q = qq(qi);
-        lk += a == r ? T->llk_match[q] : T->llk_mismatch[q];
-        const bool hq = q >= 10;
-        if (hq) n_hq++;
-        if (a != r && a != 'N' && r != 'N' && hq) m_hq++;
-        if (a != r) nm++;
-        readlen++;
-      }
-      qi++;
-      ri++;
-    } else if (op == 1) {
-      if (cur != 1) indel_runs++;
-      cur = 1;
-      readlen++;
-      if (qi < m) lk += T->ln_quarter;
-      qi++;
-      nm++;
-    } else {
-      if (cur != 2) {
-        del_runs++;
-        indel_runs++;
-      }
-      cur = 2;
-      ri++;
-      nm++;
-    }
+    if (op != lastop && lastop >= 0 && cdst) cdst[ci] = (run << 4) | (uint32_t)lastop;
+    ci += (op != lastop && lastop >= 0) ? 1u : 0u;
+    run = op != lastop ? 1u : run + 1u;
+    lastop = op;
+    const bool isM = op == 0, isI = op == 1, isD = op == 2;
+    indel_runs += cur != op ? 1 : 0;
+    del_runs += (isD && cur != 2) ? 1 : 0;
+    cur = op;
+    const bool qv = qi < m;
+    const uint8_t a = qv ? qs(qi) : (uint8_t)0;
+    const uint8_t q = qv ? qq(qi) : (uint8_t)0;
+    const uint8_t r = isI ? (uint8_t)0 : rsym(off + ri);
+    const bool mcond = isM && qv && ri < span;
+    const bool mism = a != r;
+    const double tm = mism ? T->llk_mismatch[q] : T->llk_match[q];
+    // adding +0.0 leaves lk unchanged: lk starts at +0.0 and every term is
+    // negative or +0.0, so lk is never -0.0
+    lk += mcond ? tm : ((isI && qv) ? T->ln_quarter : 0.0);
+    const bool hq = q >= 10;
+    n_hq += (mcond && hq) ? 1 : 0;
+    m_hq += (mcond && mism && a != 'N' && r != 'N' && hq) ? 1 : 0;
+    nm += ((mcond && mism) || !isM) ? 1 : 0;
+    readlen += (mcond || isI) ? 1 : 0;
+    const bool g_or_c = !isI && (r == 'G' || r == 'C');
+    gc += g_or_c ? 1 : 0;
+    tot += (g_or_c || (!isI && (r == 'A' || r == 'T'))) ? 1 : 0;
+    qi += isD ? 0 : 1;
+    ri += isI ? 0 : 1;
   }
-  int gc = 0, tot = 0;
-  for (int r = 0; r < span; r++) {
-    const uint8_t b = rsym(off + r);
-    if (b == 'G' || b == 'C') {
-      gc++;
-      tot++;
-    } else if (b == 'A' || b == 'T') {
-      tot++;
-    }
-  }
+  if (lastop >= 0 && cdst) cdst[ci] = (run << 4) | (uint32_t)lastop;
   O->log_lk = lk;
   O->pos = ref_start + (unsigned long long)off;
   O->score = endV;

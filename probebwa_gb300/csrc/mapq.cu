@@ -49,9 +49,9 @@ __global__ void k_make_jobs_single(MakeJobsArgs p) {
   }
 }
 
+// One thread per read (serial FP64 per read; see k_read_summary).
 __global__ void k_finalize_single(FinalizeArgs p) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= p.nr) return;
   const uint64_t rg = (uint64_t)p.r0 + r;
   const uint64_t qo = p.offs[rg];
@@ -66,19 +66,17 @@ __global__ void k_finalize_single(FinalizeArgs p) {
     double v = A[i].log_lk;
     if (best < 0 || v >= mx) { mx = v; best = (int)i; }
   }
-  if (best < 0) {
-    if (lane == 0) {  // unmapped_record (single.rs:362-383)
-      p.contig[r] = -1;
-      p.pos[r] = 0;
-      p.mapq[r] = 0;
-      p.flag[r] = 0x4;
-      p.log_lk[r] = 0.0;
-      p.posterior[r] = 0.0;
-      p.as_score[r] = 0;
-      p.nm[r] = 0;
-      p.n_ops[r] = 1;
-      p.best[r] = -1;
-    }
+  if (best < 0) {  // unmapped_record (single.rs:362-383)
+    p.contig[r] = -1;
+    p.pos[r] = 0;
+    p.mapq[r] = 0;
+    p.flag[r] = 0x4;
+    p.log_lk[r] = 0.0;
+    p.posterior[r] = 0.0;
+    p.as_score[r] = 0;
+    p.nm[r] = 0;
+    p.n_ops[r] = 1;
+    p.best[r] = -1;
     return;
   }
   double se = -0.0;
@@ -90,25 +88,23 @@ __global__ void k_finalize_single(FinalizeArgs p) {
   const uint8_t* q = p.quals + qo;
   const uint8_t* rep = p.rep + (size_t)r * p.wcap;
   const int nwin = L >= KMER ? L - KMER + 1 : 0;
-  const double pmiss = missing_locus_warp(q, L, rep, nwin, p.tab);
-  if (lane == 0) {
-    EntropyIn e{W.n_hq, W.m_hq, W.readlen, W.ins_runs, W.del_runs, W.gc, W.total};
-    const double ent = log_entropy(e, p.tab, p.gc_lnb, p.gc_lnbm1, p.ln_n);
-    uint8_t mq;
-    double post;
-    finalize_mapq(se, ent, pmiss, p.tab, mq, post);
-    const Cand c = p.cand[(size_t)r * MAX_CAND + best];
-    p.contig[r] = (int32_t)c.contig;
-    p.pos[r] = W.pos + 1;
-    p.mapq[r] = mq;
-    p.flag[r] = c.strand ? 0x10 : 0;
-    p.log_lk[r] = W.log_lk;
-    p.posterior[r] = post;
-    p.as_score[r] = W.score;
-    p.nm[r] = W.nm;
-    p.n_ops[r] = W.n_ops;
-    p.best[r] = (int32_t)(r * MAX_CAND + best);
-  }
+  const double pmiss = missing_locus_thread(q, L, rep, nwin, p.tab);
+  EntropyIn e{W.n_hq, W.m_hq, W.readlen, W.ins_runs, W.del_runs, W.gc, W.total};
+  const double ent = log_entropy(e, p.tab, p.gc_lnb, p.gc_lnbm1, p.ln_n);
+  uint8_t mq;
+  double post;
+  finalize_mapq(se, ent, pmiss, p.tab, mq, post);
+  const Cand c = p.cand[(size_t)r * MAX_CAND + best];
+  p.contig[r] = (int32_t)c.contig;
+  p.pos[r] = W.pos + 1;
+  p.mapq[r] = mq;
+  p.flag[r] = c.strand ? 0x10 : 0;
+  p.log_lk[r] = W.log_lk;
+  p.posterior[r] = post;
+  p.as_score[r] = W.score;
+  p.nm[r] = W.nm;
+  p.n_ops[r] = W.n_ops;
+  p.best[r] = (int32_t)(r * MAX_CAND + best);
 }
 
 __global__ void k_cigar_gather(CigarGatherArgs p) {
@@ -239,8 +235,7 @@ void launch_make_jobs_single(const MakeJobsArgs& a, cudaStream_t st) {
 void launch_finalize(const FinalizeArgs& a, int, cudaStream_t st) {
   if (a.nr == 0) return;
   const int threads = 128;
-  uint64_t warps = a.nr;
-  k_finalize_single<<<(unsigned)((warps * 32 + threads - 1) / threads), threads, 0, st>>>(a);
+  k_finalize_single<<<(unsigned)(((uint64_t)a.nr + threads - 1) / threads), threads, 0, st>>>(a);
 }
 void launch_cigar_gather(const CigarGatherArgs& a, cudaStream_t st) {
   if (a.nr == 0) return;

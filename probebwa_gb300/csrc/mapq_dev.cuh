@@ -100,17 +100,13 @@ __device__ inline double missing_phase(int phase, const uint8_t* q, int len, con
   return exp(logp);
 }
 
-// Whole missing-locus probability, computed by lanes 0..4 of a warp, result
-// valid in every lane.
-__device__ inline double missing_locus_warp(const uint8_t* q, int len, const uint8_t* rep, int nwin,
-                                            const DevTables* T) {
-  const int lane = threadIdx.x & 31;
+// Whole missing-locus probability by one thread: offset_means starts at 0.0
+// and adds phases 0..4 in order.
+__device__ inline double missing_locus_thread(const uint8_t* q, int len, const uint8_t* rep, int nwin,
+                                              const DevTables* T) {
   if (len < KMER) return 0.5;
-  double ph = 0.0;
-  if (lane < 5) ph = missing_phase(lane, q, len, rep, nwin, T);
   double s = 0.0;
-  for (int k = 0; k < 5; k++) s += __shfl_sync(0xffffffffu, ph, k);
-  // offset_means starts at 0.0 and adds phases 0..4 in order
+  for (int k = 0; k < 5; k++) s += missing_phase(k, q, len, rep, nwin, T);
   return fmin(s / 5.0, 0.99);
 }
 

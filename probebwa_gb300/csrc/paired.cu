@@ -14,8 +14,9 @@
 //                    paired.rs:486-496), select_best, mapq_for_winning_pair
 //                    (paired.rs:398-435), flags / TLEN / proper pair and the
 //                    insert-size observation (map_pair_readonly, paired.rs:154-234)
-//   k_fold_model     the serial InsertSizeDistribution::update over the
-//                    batch's observations in pair order (paired.rs:139-143)
+//   fold_insert_model (host) the serial InsertSizeDistribution::update over
+//                    the batch's observations in pair order (paired.rs:139-143)
+#include <algorithm>
 #include <cmath>
 
 #include "mapq_dev.cuh"
@@ -32,9 +33,11 @@ constexpr double SHORTLIST_MASS = 0.999;     // paired.rs:71
 constexpr int SHORTLIST_MIN = 3;             // paired.rs:72
 constexpr int SHORTLIST_MAX = 20;            // paired.rs:73
 
+// One thread per read: the work is serial FP64 per read (GB300 runs FP64 at a
+// low rate, so every lane of a warp must carry a read for the pipe to be
+// used at all).
 __global__ void k_read_summary(ReadSummaryArgs p) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= p.nr) return;
   const uint64_t rg = (uint64_t)p.r0 + r;
   const uint64_t qo = p.offs[rg];
@@ -46,8 +49,7 @@ __global__ void k_read_summary(ReadSummaryArgs p) {
   for (uint32_t i = 0; i < nc; i++)
     if (A[i].n_ops != 0) S.vslot[S.n_aln++] = (uint8_t)i;
   const int nwin = L >= KMER ? L - KMER + 1 : 0;
-  const double pmiss = missing_locus_warp(p.quals + qo, L, p.rep + (size_t)r * p.wcap, nwin, p.tab);
-  if (lane != 0) return;
+  const double pmiss = missing_locus_thread(p.quals + qo, L, p.rep + (size_t)r * p.wcap, nwin, p.tab);
   S.missing = pmiss;
   S.best = -1;
   S.sum_exp = 0.0;
@@ -309,7 +311,7 @@ __device__ __forceinline__ void fin(const PairArgs& p, double se, const CandView
 }
 
 // InsertSizeDistribution::log_likelihood (insert_size.rs:23-30) with the
-// batch's ln(2*pi*sd^2) precomputed by the fold kernel.
+// batch's ln(2*pi*sd^2) precomputed on the host (fold_insert_model).
 __device__ __forceinline__ double insert_ll(const PairModel* M, double x) {
   if (M->sd <= 0.0) return -1e300;
   const double diff = x - M->mean;
@@ -464,100 +466,35 @@ __global__ void k_pair_resolve(PairArgs p) {
   p.obs[pl] = obs;
 }
 
-// InsertSizeDistribution::update (insert_size.rs:32-44), folded serially in
-// pair order, then the next batch's ln(2*pi*sd^2) (insert_size.rs:29).
+// InsertSizeDistribution::update (insert_size.rs:32-44) over one batch's
+// observations in pair order (paired.rs:139-143; NaN = the pair gave none),
+// then the next batch's ln(2*pi*sd^2) (insert_size.rs:29).
 //
-// The recurrence is serial, so its latency per observation is what counts.
-// The block first stages a tile of observations in shared memory, drops the
-// NaNs (pairs that gave no observation), and gives every kept observation its
-// count nn and the correctly rounded reciprocal 1/nn, all in parallel. One
-// thread then runs the recurrence from shared memory, dividing by nn with
-// Markstein's correction (y = RN(1/nn), q0 = RN(a*y), r = a - q0*nn exactly
-// by FMA, q = RN(q0 + r*y)), which is the correctly rounded a/nn because y is
-// within half an ulp of 1/nn and q0 within one ulp of a/nn (P. Markstein,
-// IBM J. Res. Dev. 34(1), 1990). The results are those of IEEE division.
-constexpr int FOLD_THREADS = 256;
-constexpr int FOLD_TILE = 1024;
-
-__device__ __forceinline__ double div_by_count(double a, double nn, double y) {
-  const double q0 = a * y;
-  const double r = fma(-q0, nn, a);
-  return fma(r, y, q0);
-}
-
-__global__ void __launch_bounds__(FOLD_THREADS) k_fold_model(PairModel* M, const double* obs, uint32_t p0,
-                                                             uint32_t np) {
-  __shared__ double xs[FOLD_TILE];
-  __shared__ double nns[FOLD_TILE];
-  __shared__ double rcp[FOLD_TILE];
-  __shared__ uint32_t warp_cnt[FOLD_THREADS / 32];
-  __shared__ double s_mean, s_sd;
-  __shared__ unsigned long long s_n;
-  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  if (t == 0) {
-    s_mean = M->mean;
-    s_sd = M->sd;
-    s_n = M->n;
+// This runs in the host runtime between batches. The recurrence is one
+// dependent chain of about twenty FP64 operations per observation (two
+// divisions and a square root among them); on GB300 a dependent FP64 chain
+// costs ~40 cycles per operation, ~0.4 us per observation, while the host
+// cores take ~20 ns. Host code is compiled without FMA contraction, so every
+// operation rounds exactly as the reference's f64 arithmetic, and the
+// logarithm is the host libm's, as in the reference.
+void fold_insert_model(PairModel& M, const double* obs, uint32_t np) {
+  double mean = M.mean, sd = M.sd;
+  unsigned long long n = M.n;
+  for (uint32_t i = 0; i < np; i++) {
+    const double x = obs[i];
+    if (std::isnan(x)) continue;
+    n++;
+    const double nn = (double)n;
+    const double delta = x - mean;
+    mean += delta / nn;
+    const double delta2 = x - mean;
+    const double var = nn > 1.0 ? ((sd * sd) * (nn - 1.0) + delta * delta2) / nn : sd * sd;
+    sd = std::max(std::sqrt(var), 1.0);
   }
-  constexpr int PER = FOLD_TILE / FOLD_THREADS;  // consecutive observations per thread
-  for (uint32_t base = 0; base < np; base += FOLD_TILE) {
-    __syncthreads();
-    const uint32_t cnt_tile = min((uint32_t)FOLD_TILE, np - base);
-    double v[PER];
-    uint32_t mine = 0;
-#pragma unroll
-    for (int k = 0; k < PER; k++) {
-      const uint32_t i = (uint32_t)t * PER + k;
-      v[k] = i < cnt_tile ? obs[p0 + base + i] : __longlong_as_double(0x7ff8000000000000ll);
-      mine += isnan(v[k]) ? 0u : 1u;
-    }
-    // exclusive prefix of kept observations over the block, in pair order
-    uint32_t incl = mine;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
-      if (lane >= d) incl += o;
-    }
-    if (lane == 31) warp_cnt[w] = incl;
-    __syncthreads();
-    uint32_t before = incl - mine, total = 0;
-    for (int k = 0; k < FOLD_THREADS / 32; k++) {
-      if (k < w) before += warp_cnt[k];
-      total += warp_cnt[k];
-    }
-    const unsigned long long n0 = s_n;
-#pragma unroll
-    for (int k = 0; k < PER; k++) {
-      if (isnan(v[k])) continue;
-      const double nn = (double)(n0 + before + 1);
-      xs[before] = v[k];
-      nns[before] = nn;
-      rcp[before] = 1.0 / nn;
-      before++;
-    }
-    __syncthreads();
-    if (t == 0) {
-      double mean = s_mean, sd = s_sd;
-      for (uint32_t j = 0; j < total; j++) {
-        const double x = xs[j], nn = nns[j], y = rcp[j];
-        const double delta = x - mean;
-        mean = mean + div_by_count(delta, nn, y);
-        const double delta2 = x - mean;
-        const double var = nn > 1.0 ? div_by_count((sd * sd) * (nn - 1.0) + delta * delta2, nn, y) : sd * sd;
-        sd = fmax(sqrt(var), 1.0);
-      }
-      s_mean = mean;
-      s_sd = sd;
-      s_n = n0 + total;
-    }
-  }
-  if (t == 0) {
-    const double sd = s_sd;
-    M->mean = s_mean;
-    M->sd = sd;
-    M->n = s_n;
-    M->ln_2pi_sd2 = log(2.0 * 3.141592653589793115997963468544185161590576171875 * sd * sd);
-  }
+  M.mean = mean;
+  M.sd = sd;
+  M.n = n;
+  M.ln_2pi_sd2 = std::log(2.0 * 3.141592653589793115997963468544185161590576171875 * sd * sd);
 }
 
 __global__ void k_pair_cigar_gather(const PairArgs p, const uint32_t* cig_off, const uint32_t* cig_pool, uint32_t* cigar,
@@ -577,7 +514,7 @@ __global__ void k_pair_cigar_gather(const PairArgs p, const uint32_t* cig_off, c
 
 void launch_read_summary(const ReadSummaryArgs& a, cudaStream_t st) {
   if (a.nr == 0) return;
-  k_read_summary<<<(unsigned)(((uint64_t)a.nr * 32 + 127) / 128), 128, 0, st>>>(a);
+  k_read_summary<<<(unsigned)(((uint64_t)a.nr + 127) / 128), 128, 0, st>>>(a);
 }
 void launch_pair_decide(const PairArgs& a, cudaStream_t st) {
   if (a.np == 0) return;
@@ -586,9 +523,6 @@ void launch_pair_decide(const PairArgs& a, cudaStream_t st) {
 void launch_pair_resolve(const PairArgs& a, cudaStream_t st) {
   if (a.np == 0) return;
   k_pair_resolve<<<(a.np + 127) / 128, 128, 0, st>>>(a);
-}
-void launch_fold_model(PairModel* M, const double* obs, uint32_t p0, uint32_t np, cudaStream_t st) {
-  k_fold_model<<<1, FOLD_THREADS, 0, st>>>(M, obs, p0, np);
 }
 void launch_pair_cigar_gather(const PairArgs& a, const uint32_t* cig_off, const uint32_t* cig_pool, uint32_t* cigar,
                               uint64_t g0, uint32_t n, cudaStream_t st) {

@@ -110,7 +110,7 @@ struct PairArgs {
 void launch_read_summary(const ReadSummaryArgs& a, cudaStream_t st);
 void launch_pair_decide(const PairArgs& a, cudaStream_t st);
 void launch_pair_resolve(const PairArgs& a, cudaStream_t st);
-void launch_fold_model(PairModel* M, const double* obs, uint32_t p0, uint32_t np, cudaStream_t st);
+void fold_insert_model(PairModel& M, const double* obs, uint32_t np);
 void launch_pair_cigar_gather(const PairArgs& a, const uint32_t* cig_off, const uint32_t* cig_pool, uint32_t* cigar,
                               uint64_t g0, uint32_t n, cudaStream_t st);
 

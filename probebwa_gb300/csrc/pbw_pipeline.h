@@ -122,6 +122,7 @@ struct pbw_handle {
   pbw::DevBuf<double> d_obs;
   pbw::DevBuf<pbw::AlnJob> d_xjobs;
   pbw::HostBuf h_stage;
+  pbw::HostBuf h_fold;  // one batch's insert-size observations + the model
   std::vector<cudaEvent_t> events;
   pbw_stats stats{};
   ~pbw_handle() {

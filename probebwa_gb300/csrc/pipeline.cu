@@ -529,7 +529,14 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   pm.sd = model->sd;
   pm.n = model->n_observed;
   pm.ln_2pi_sd2 = std::log(2.0 * 3.141592653589793 * pm.sd * pm.sd);
-  CK(cudaMemcpyAsync(h->d_model.p, &pm, sizeof(pm), cudaMemcpyHostToDevice, st));
+  if (!h->h_fold.ensure(sizeof(PairModel) + 2000 * sizeof(double))) {
+    h->err = "cudaMallocHost failed";
+    return PBW_ERR_NOMEM;
+  }
+  PairModel* h_pm = (PairModel*)h->h_fold.p;
+  double* h_obs = (double*)((char*)h->h_fold.p + sizeof(PairModel));
+  *h_pm = pm;
+  CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(pm), cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * sizeof(unsigned int), st));
   CK(cudaMemsetAsync(h->d_cnt64.p, 0, 16 * sizeof(unsigned long long), st));
   cudaEvent_t* ev = &h->events[2];
@@ -651,8 +658,13 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, (uint64_t)pa.np * MAX_CROSS);
       launch_align_window(aa, std::max(gw, 1), st);
       launch_pair_resolve(pa, st);
-      launch_fold_model(h->d_model.p, h->d_obs.p, pa.p0, pa.np, st);
-      h->stats.kernel_launches += 4;
+      // the next batch sees the model updated by this batch's observations
+      CK(cudaMemcpyAsync(h_obs, h->d_obs.p + pa.p0, (size_t)pa.np * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      fold_insert_model(pm, h_obs, pa.np);
+      *h_pm = pm;
+      CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st));
+      h->stats.kernel_launches += 3;
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev[1], st));
@@ -721,7 +733,6 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     CK(cudaMemcpyAsync(o->cigar, (k ? h->o_cigar2.p : h->o_cigar.p), (size_t)tot[k] * 4, cudaMemcpyDeviceToHost,
                        st));
   }
-  CK(cudaMemcpyAsync(&pm, h->d_model.p, sizeof(pm), cudaMemcpyDeviceToHost, st));
   CK(cudaEventRecord(e2, st));
   CK(cudaStreamSynchronize(st));
   h->stats.ms_d2h = ms_between(e1, e2);
