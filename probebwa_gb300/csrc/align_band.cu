@@ -1,23 +1,24 @@
 // align_band.cu -- K3b: the seeded DP (band <= 31, i.e. the max_indel_len
 // band of SingleEndMapper, src/mapper/single.rs:59) of
-// SmithWatermanAligner::align (src/align/smith_waterman.rs:113-255), four
+// SmithWatermanAligner::align (src/align/smith_waterman.rs:113-255), several
 // alignments per warp.
 //
 // Band coordinates: cell (i, c) is window column j = i + hint - band + c,
 // 0 <= c <= 2*band. It depends on (i-1, c) [diagonal], (i-1, c+1) [up] and
-// (i, c-1) [left]. An alignment gets 8 lanes; lane k owns the C consecutive
-// band columns c = k*C .. k*C + C - 1 (8*C > 2*band + 1) and lags lane k-1 by
+// (i, c-1) [left]. An alignment gets G lanes (8 or 16; 32/G alignments per
+// warp); lane k owns the C consecutive band columns c = k*C .. k*C + C - 1
+// (G*C > 2*band + 1) and lags lane k-1 by
 // one row: at step s it computes its C cells of row i = R0 + s - k from left
 // to right. The left input of its first column is lane k-1's last column of
 // the same row (computed one step earlier, __shfl_up_sync); the up input of
 // its last column is lane k+1's first column one row up (computed earlier in
 // the same step, __shfl_down_sync). Everything else stays in registers: the
 // lane's previous row gives its diagonal and up inputs. An alignment takes
-// m + 7 steps of C cells per lane.
+// m + G - 1 steps of C cells per lane.
 //
 // Shared memory per alignment: the read as packed words (symbol, quality,
 // mismatch penalty), the window as (gap open, symbol) pairs, the traceback
-// (4 bits per cell, C/2 bytes per lane per row) and the traceback ops. The
+// (4 bits per cell, G*C/2 bytes per row) and the traceback ops. The
 // alignment's first lane then runs the traceback and bookkeeping
 // (align_finish.cuh).
 //
@@ -25,6 +26,7 @@
 // NEG_INF exactly as in the reference; rows before R0 hold the initial row
 // (M = 0 at every window column, smith_waterman.rs:174-176).
 #include <algorithm>
+#include <cstdlib>
 
 #include "align_finish.cuh"
 #include "pbw_common.cuh"
@@ -32,23 +34,22 @@
 
 namespace pbw {
 
-constexpr int BG = 8;        // lanes per alignment
-constexpr int BJ = 4;        // alignments per warp
 constexpr int B_PADC = 16;   // window padding (columns) on each side, >= C
-constexpr int B_PADR = 8;    // read padding (rows) on each side, >= BG
+constexpr int B_PADR = 16;   // read padding (rows) on each side, >= lanes per alignment
 
 static __host__ __device__ inline size_t b16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 struct BandLayout {
   size_t o_col, o_tb, o_ops, bytes;
 };
-// Offsets inside one alignment's area; the areas of one warp start 32 bytes
-// apart modulo 128 so that the four alignments use different banks.
-__host__ __device__ inline BandLayout band_layout(int lmax, int nmax, int C) {
+// Offsets inside one alignment's area (traceback rows of row_bytes); the
+// areas of one warp start 32 bytes apart modulo 128 so that the alignments of
+// a warp use different banks.
+__host__ __device__ inline BandLayout band_layout(int lmax, int nmax, int row_bytes) {
   BandLayout L;
   L.o_col = b16(4 * ((size_t)lmax + 2 * B_PADR));
   L.o_tb = L.o_col + b16(8 * ((size_t)nmax + 2 * B_PADC));
-  L.o_ops = L.o_tb + b16((size_t)(lmax + 1) * 4 * C);
+  L.o_ops = L.o_tb + b16((size_t)(lmax + 1) * row_bytes);
   const size_t s = L.o_ops + b16((size_t)lmax + nmax + 2);
   L.bytes = ((s + 127) & ~(size_t)127) + 32;
   return L;
@@ -72,12 +73,14 @@ __device__ __forceinline__ void store_tb(unsigned char* row, int k, uint32_t wor
   else row[k] = (uint8_t)word;
 }
 
-template <int C>
+template <int C, int G>
 __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr int BJ = 32 / G;         // alignments per warp
+  constexpr int ROWB = G * C / 2;    // traceback bytes per row
   const int lane = threadIdx.x & 31;
-  const int g = lane >> 3, k = lane & (BG - 1);
+  const int g = lane / G, k = lane % G;
   unsigned char* my = smem_raw + (size_t)g * LY.bytes;
   int32_t* rowi = (int32_t*)my + B_PADR;         // rowi[i - 1] describes read row i
   int2* coli = (int2*)(my + LY.o_col) + B_PADC;  // coli[j - 1] = (gap open, symbol) of window column j
@@ -106,7 +109,7 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
       n = (int)(J.ref_end - J.ref_start);
       if (k == 0) jobs_acc++;
       // stage the read and the window
-      for (int i = k; i < m; i += BG) {
+      for (int i = k; i < m; i += G) {
         uint8_t s, q;
         if (p.ref_bytes) {
           s = qbases[qo + i];
@@ -123,47 +126,47 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
       rowi[-1 - k] = 0;
       rowi[m + k] = 0;
       if (p.ref_bytes) {
-        for (int j = k; j < n; j += BG) coli[j] = make_int2(0, p.ref_bytes[J.ref_start + j]);
+        for (int j = k; j < n; j += G) coli[j] = make_int2(0, p.ref_bytes[J.ref_start + j]);
       } else {
         const uint64_t gb = __ldg(&p.G.cbase[J.contig]) + J.ref_start;
-        for (int j = k; j < n; j += BG) coli[j] = make_int2(0, (int)(uint8_t)"ACGTN"[gcode(p.G, gb + j)]);
+        for (int j = k; j < n; j += G) coli[j] = make_int2(0, (int)(uint8_t)"ACGTN"[gcode(p.G, gb + j)]);
       }
-      for (int j = k; j < B_PADC; j += BG) {
+      for (int j = k; j < B_PADC; j += G) {
         coli[-1 - j] = make_int2(0, 0);
         coli[n + j] = make_int2(0, 0);
       }
     }
     __syncwarp();
     // gap open per window column from its homopolymer run (smith_waterman.rs:288-291, 348-363):
-    // run start by a forward max-scan, run end by a backward min-scan, 8 lanes per alignment
+    // run start by a forward max-scan, run end by a backward min-scan, G lanes per alignment
     int nmx = act ? n : 0;
     for (int d = 16; d >= 1; d >>= 1) nmx = max(nmx, __shfl_xor_sync(FULL, nmx, d));
     {
       int carry = 0;
-      for (int c0 = 0; c0 < nmx; c0 += BG) {
+      for (int c0 = 0; c0 < nmx; c0 += G) {
         const int j = c0 + k;
         const bool in = act && j < n;
         int v = (in && (j == 0 || coli[j].y != coli[j - 1].y)) ? j : -1;
 #pragma unroll
-        for (int d = 1; d < BG; d <<= 1) {
-          const int y = __shfl_up_sync(FULL, v, d, BG);
+        for (int d = 1; d < G; d <<= 1) {
+          const int y = __shfl_up_sync(FULL, v, d, G);
           if (k >= d) v = max(v, y);
         }
         v = max(v, carry);
         if (in) coli[j].x = v;
-        carry = __shfl_sync(FULL, v, BG - 1, BG);
+        carry = __shfl_sync(FULL, v, G - 1, G);
       }
       __syncwarp();
       int carry_e = act ? n - 1 : 0;
-      const int top = nmx > 0 ? ((nmx - 1) / BG) * BG : -BG;
-      for (int c0 = top; c0 >= 0; c0 -= BG) {
+      const int top = nmx > 0 ? ((nmx - 1) / G) * G : -G;
+      for (int c0 = top; c0 >= 0; c0 -= G) {
         const int j = c0 + k;
         const bool in = act && j < n;
         int v = (in && (j == n - 1 || coli[j + 1].y != coli[j].y)) ? j : INT32_MAX;
 #pragma unroll
-        for (int d = 1; d < BG; d <<= 1) {
-          const int y = __shfl_down_sync(FULL, v, d, BG);
-          if (k + d < BG) v = min(v, y);
+        for (int d = 1; d < G; d <<= 1) {
+          const int y = __shfl_down_sync(FULL, v, d, G);
+          if (k + d < G) v = min(v, y);
         }
         v = min(v, carry_e);
         if (in) {
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
           const long long gg = (long long)J.gap_open + (run - 1);
           coli[j].x = gg > -1 ? -1 : (int32_t)gg;
         }
-        carry_e = __shfl_sync(FULL, v, 0, BG);
+        carry_e = __shfl_sync(FULL, v, 0, G);
       }
       __syncwarp();
     }
@@ -211,13 +214,13 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
       PI[t] = NEG;
       PD[t] = NEG;
     }
-    int T = nrows > 0 ? nrows + BG - 1 : 0;
+    int T = nrows > 0 ? nrows + G - 1 : 0;
     for (int d = 16; d >= 1; d >>= 1) T = max(T, __shfl_xor_sync(FULL, T, d));
     unsigned long long bestKey = 0;  // (value + 2^31) << 32 | j << 1 | state; 0 = none
     for (int s = 0; s < T; s++) {
       const int i = R0 + s - k;
-      const int32_t sLM = __shfl_up_sync(FULL, PM[C - 1], 1, BG);
-      const int32_t sLD = __shfl_up_sync(FULL, PD[C - 1], 1, BG);
+      const int32_t sLM = __shfl_up_sync(FULL, PM[C - 1], 1, G);
+      const int32_t sLD = __shfl_up_sync(FULL, PD[C - 1], 1, G);
       int32_t lM = k ? sLM : NEG, lD = k ? sLD : NEG;
       const int ri = min(max(i - 1, -B_PADR), m - 1 + B_PADR);
       const int32_t rw = rowi[ri];
@@ -253,14 +256,14 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
         lM = nM;
         lD = nD;
         if (t == 0) {
-          const int32_t a = __shfl_down_sync(FULL, nM, 1, BG);
-          const int32_t b = __shfl_down_sync(FULL, nI, 1, BG);
-          upM = k < BG - 1 ? a : NEG;
-          upI = k < BG - 1 ? b : NEG;
+          const int32_t a = __shfl_down_sync(FULL, nM, 1, G);
+          const int32_t b = __shfl_down_sync(FULL, nI, 1, G);
+          upM = k < G - 1 ? a : NEG;
+          upI = k < G - 1 ? b : NEG;
         }
       }
       if (i >= R0 && i <= R1) {
-        store_tb<C>(tb + (size_t)(i - R0) * (4 * C), k, word);
+        store_tb<C>(tb + (size_t)(i - R0) * ROWB, k, word);
         if (i == R1) {
           // last row: in-band (M, I) endpoint candidates (smith_waterman.rs:248-251)
 #pragma unroll
@@ -276,7 +279,7 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
         }
       }
     }
-    for (int d = 4; d >= 1; d >>= 1) bestKey = max(bestKey, __shfl_xor_sync(FULL, bestKey, d, BG));
+    for (int d = G / 2; d >= 1; d >>= 1) bestKey = max(bestKey, __shfl_xor_sync(FULL, bestKey, d, G));
     __syncwarp();
     if (act && k == 0) {
       AlnOut* O = p.out + J.slot;
@@ -309,14 +312,11 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
           const long long c = (long long)jj - ((long long)i + basel);
           if (c < 0 || c > 2 * B) return 0u;
           const int ci = (int)c;
-          const unsigned char* row = tb + (size_t)(i - R0) * (4 * C);
+          const unsigned char* row = tb + (size_t)(i - R0) * ROWB;
           return (uint32_t)(row[ci >> 1] >> ((ci & 1) * 4)) & 15u;
         };
-        auto rsym = [&](int jj) -> uint8_t { return (uint8_t)coli[jj].y; };
-        auto qsym = [&](int i) -> uint8_t { return (uint8_t)(rowi[i] & 0xFF); };
-        auto qqual = [&](int i) -> uint8_t { return (uint8_t)((rowi[i] >> 8) & 0xFF); };
-        finish_alignment(m, endV, endJ, endS, qsym, qqual, ops, tbr, rsym, J.ref_start, p.tab, O, p.cig_pool,
-                         p.cig_pool_used, p.cig_pool_cap, p.err);
+        traceback_cigar(m, endV, endJ, endS, ops, tbr, J.ref_start, O, p.cig_pool, p.cig_pool_used, p.cig_pool_cap,
+                        p.err);
       }
     }
     __syncwarp();
@@ -331,22 +331,24 @@ __global__ void __launch_bounds__(32) k_align_band(AlignArgs p, BandLayout LY) {
   }
 }
 
-template <int C>
+template <int C, int G>
 static void launch_band_c(const AlignArgs& a, int num_sms, cudaStream_t st) {
-  const BandLayout LY = band_layout(a.lmax, a.nmax, C);
-  const size_t sm = LY.bytes * BJ;
-  cudaFuncSetAttribute(k_align_band<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const BandLayout LY = band_layout(a.lmax, a.nmax, G * C / 2);
+  const size_t sm = LY.bytes * (32 / G);
+  cudaFuncSetAttribute(k_align_band<C, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(32, (226 * 1024) / (sm + 1024)));
-  k_align_band<C><<<num_sms * per_sm, 32, sm, st>>>(a, LY);
+  k_align_band<C, G><<<num_sms * per_sm, 32, sm, st>>>(a, LY);
 }
 
-size_t band_smem_bytes(int lmax, int nmax) { return band_layout(lmax, nmax, 8).bytes * BJ; }
+size_t band_smem_bytes(int lmax, int nmax) { return band_layout(lmax, nmax, 32).bytes * 4; }
 
-// Columns per lane: the smallest of 2, 4, 8 with 8*C > 2*band_max + 1.
+// Columns covered per alignment G*C > 2*band_max + 1.
 void launch_align_band(const AlignArgs& a, int num_sms, int band_max, cudaStream_t st) {
-  if (2 * band_max + 2 <= 16) launch_band_c<2>(a, num_sms, st);
-  else if (2 * band_max + 2 <= 32) launch_band_c<4>(a, num_sms, st);
-  else launch_band_c<8>(a, num_sms, st);
+  static const int lanes = getenv("PBW_BAND_LANES") ? atoi(getenv("PBW_BAND_LANES")) : 8;
+  if (2 * band_max + 2 <= 16) launch_band_c<2, 8>(a, num_sms, st);
+  else if (2 * band_max + 2 <= 32) launch_band_c<4, 8>(a, num_sms, st);
+  else if (lanes == 16) launch_band_c<4, 16>(a, num_sms, st);
+  else launch_band_c<8, 8>(a, num_sms, st);
 }
 
 }  // namespace pbw

@@ -352,11 +352,8 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
         const int rr = i - R0;
         return (tb[(size_t)j * TBS + (rr >> 3)] >> ((rr & 7) * 4)) & 15u;
       };
-      auto rsym = [&](int j) -> uint8_t { return rs[j]; };
-      auto qsym = [&](int i) -> uint8_t { return qs[i]; };
-      auto qqual = [&](int i) -> uint8_t { return qq[i]; };
-      finish_alignment(m, endV, endJ, endS, qsym, qqual, ops, tbr, rsym, J.ref_start, p.tab, O, p.cig_pool,
-                       p.cig_pool_used, p.cig_pool_cap, p.err);
+      traceback_cigar(m, endV, endJ, endS, ops, tbr, J.ref_start, O, p.cig_pool, p.cig_pool_used, p.cig_pool_cap,
+                      p.err);
     }
     __syncthreads();
   }

@@ -147,6 +147,9 @@ size_t band_smem_bytes(int lmax, int nmax);  // per warp at 8 columns per lane
 // shared memory.
 void launch_align_window(const AlignArgs& a, int grid, cudaStream_t st);
 size_t window_smem_bytes(int lmax, int nmax);
+// Likelihood, log_entropy counts and edit distance of every aligned job from
+// its CIGAR (after K3b / K3w); max_jobs bounds the device job count.
+void launch_aln_stats(const AlignArgs& a, uint64_t max_jobs, cudaStream_t st);
 // per job: window symbols, gap opens, traceback ops, (lmax + 7) / 8 traceback
 // words per column; 16-byte aligned pieces
 constexpr size_t window_slab_bytes(int lmax, int nmax) {

@@ -283,9 +283,10 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
     aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, cfg.nmax);
     launch_align_window(aa, window_grid(h), st);
   }
+  launch_aln_stats(aa, (uint64_t)nr * MAX_CAND, st);
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[3], st));
-  h->stats.kernel_launches += 6;
+  h->stats.kernel_launches += 7;
   return PBW_OK;
 }
 
@@ -657,6 +658,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       launch_pair_decide(pa, st);
       const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, (uint64_t)pa.np * MAX_CROSS);
       launch_align_window(aa, std::max(gw, 1), st);
+      launch_aln_stats(aa, (uint64_t)pa.np * MAX_CROSS, st);
       launch_pair_resolve(pa, st);
       // the next batch sees the model updated by this batch's observations
       CK(cudaMemcpyAsync(h_obs, h->d_obs.p + pa.p0, (size_t)pa.np * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -664,7 +666,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       fold_insert_model(pm, h_obs, pa.np);
       *h_pm = pm;
       CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st));
-      h->stats.kernel_launches += 3;
+      h->stats.kernel_launches += 4;
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev[1], st));
