@@ -27,7 +27,41 @@ __device__ __forceinline__ uint8_t comp_ascii_s(uint8_t b) {
   }
 }
 
+// Byte cursor over one read that fetches aligned 8-byte words: one load per
+// eight bases instead of one per base. Only whole words inside the read's own
+// bytes [lo, lim) are loaded as words; the words at its two ends are put
+// together from byte loads, so no byte outside the read is touched.
+struct ByteCursor {
+  const uint8_t* lo;
+  const uint8_t* lim;
+  uintptr_t wcur;  // address of the loaded word, or 1
+  uint64_t word;
+  __device__ __forceinline__ uint8_t at(const uint8_t* ptr) {
+    const uintptr_t a = (uintptr_t)ptr;
+    const uintptr_t wa = a & ~(uintptr_t)7;
+    if (wa != wcur) {
+      wcur = wa;
+      if (wa >= (uintptr_t)lo && wa + 8 <= (uintptr_t)lim) {
+        word = *(const uint64_t*)wa;
+      } else {
+        word = 0;
+        for (int k = 0; k < 8; k++) {
+          const uintptr_t b = wa + k;
+          if (b >= (uintptr_t)lo && b < (uintptr_t)lim) word |= (uint64_t)(*(const uint8_t*)b) << (8 * k);
+        }
+      }
+    }
+    return (uint8_t)(word >> (8 * (a & 7)));
+  }
+};
+
 __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
+  __shared__ double s_llk[2][256];
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) {
+    s_llk[0][k] = p.tab->llk_match[k];
+    s_llk[1][k] = p.tab->llk_mismatch[k];
+  }
+  __syncthreads();
   const unsigned int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= *p.n_jobs) return;
   const AlnJob J = p.jobs[t];
@@ -48,58 +82,68 @@ __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
   const int m = (int)(offs[J.read + 1] - qo);
   const uint64_t rpos = O->pos;
   const int span = (int)O->span;
+  const bool fwd = p.ref_bytes || !J.rev;
+  ByteCursor cb{bases + qo, bases + qo + m, 1, 0};
+  ByteCursor cq{quals + qo, quals + qo + m, 1, 0};
+  // reference cursor: one 2-bit word and its N-mask word per 32 bases
   const uint64_t gb = p.ref_bytes ? 0 : __ldg(&p.G.cbase[J.contig]) + rpos;
+  uint64_t gword = 0;
+  uint32_t gmask = 0;
+  uint64_t gwi = ~0ull;
   auto rsym = [&](int ri) -> uint8_t {
     if (p.ref_bytes) return p.ref_bytes[rpos + ri];
-    return (uint8_t)"ACGTN"[gcode(p.G, gb + ri)];
+    const uint64_t gp = gb + (uint64_t)ri;
+    if ((gp >> 5) != gwi) {
+      gwi = gp >> 5;
+      gword = __ldg(&p.G.bits[gwi]);
+      gmask = __ldg(&p.G.nmask[gwi]);
+    }
+    if ((gmask >> (gp & 31)) & 1u) return (uint8_t)'N';
+    return (uint8_t)"ACGT"[(gword >> ((gp & 31) * 2)) & 3ull];
   };
-  auto qsym = [&](int qi) -> uint8_t {
-    if (p.ref_bytes) return bases[qo + qi];
-    if (!J.rev) return up_ascii_s(bases[qo + qi]);
-    return comp_ascii_s(up_ascii_s(bases[qo + m - 1 - qi]));
-  };
-  auto qqual = [&](int qi) -> uint8_t { return (p.ref_bytes || !J.rev) ? quals[qo + qi] : quals[qo + m - 1 - qi]; };
-  const DevTables* T = p.tab;
+  const double ln_quarter = p.tab->ln_quarter;
   double lk = 0.0;
   int qi = 0, ri = 0, cur = 0;
   int n_hq = 0, m_hq = 0, readlen = 0, indel_runs = 0, del_runs = 0, nm = 0, gc = 0, tot = 0;
-  for (uint32_t k = 0; k < nops; k++) {
-    const uint32_t w = cig[k];
-    const int op = (int)(w & 15u);
-    const int len = (int)(w >> 4);
-    indel_runs += cur != op ? 1 : 0;
-    del_runs += (op == 2 && cur != 2) ? 1 : 0;
-    cur = op;
-    if (op == 1) {
-      for (int u = 0; u < len; u++) {
-        if (qi < m) lk += T->ln_quarter;
-        qi++;
-      }
-      readlen += len;
-      nm += len;
-      continue;
+  // One operation per iteration, with the run bookkeeping inside, so that
+  // the lanes of a warp step through their different CIGARs together.
+  uint32_t k = 0;
+  int op = 0, left = 0;
+  while (true) {
+    if (left == 0) {
+      if (k == nops) break;
+      const uint32_t w = cig[k++];
+      op = (int)(w & 15u);
+      left = (int)(w >> 4);
+      indel_runs += cur != op ? 1 : 0;
+      del_runs += (op == 2 && cur != 2) ? 1 : 0;
+      cur = op;
+      if (left == 0) continue;
     }
-    for (int u = 0; u < len; u++) {
-      const uint8_t r = ri < span ? rsym(ri) : (uint8_t)0;
-      gc += (r == 'G' || r == 'C') ? 1 : 0;
-      tot += (r == 'G' || r == 'C' || r == 'A' || r == 'T') ? 1 : 0;
-      if (op == 0) {
-        if (qi < m && ri < span) {
-          const uint8_t a = qsym(qi);
-          const uint8_t q = qqual(qi);
-          lk += a == r ? T->llk_match[q] : T->llk_mismatch[q];
-          const bool hq = q >= 10;
-          n_hq += hq ? 1 : 0;
-          m_hq += (a != r && a != 'N' && r != 'N' && hq) ? 1 : 0;
-          nm += a != r ? 1 : 0;
-          readlen++;
-        }
-        qi++;
-      } else {
-        nm++;
-      }
-      ri++;
+    left--;
+    const bool isM = op == 0, isI = op == 1;
+    const uint8_t r = (!isI && ri < span) ? rsym(ri) : (uint8_t)0;
+    const bool qv = qi < m;
+    const bool mcond = isM && qv && ri < span;
+    const uint64_t qx = fwd ? qo + (uint64_t)qi : qo + (uint64_t)(m - 1 - qi);
+    uint8_t a = 0, q = 0;
+    if (mcond) {
+      a = cb.at(bases + qx);
+      if (!p.ref_bytes) a = J.rev ? comp_ascii_s(up_ascii_s(a)) : up_ascii_s(a);
+      q = cq.at(quals + qx);
     }
+    const bool mism = a != r;
+    // a D operation adds +0.0, which leaves lk unchanged (lk is never -0.0)
+    lk += mcond ? s_llk[mism ? 1 : 0][q] : ((isI && qv) ? ln_quarter : 0.0);
+    const bool hq = q >= 10;
+    n_hq += (mcond && hq) ? 1 : 0;
+    m_hq += (mcond && mism && a != 'N' && r != 'N' && hq) ? 1 : 0;
+    nm += ((mcond && mism) || !isM) ? 1 : 0;
+    readlen += (mcond || isI) ? 1 : 0;
+    gc += (r == 'G' || r == 'C') ? 1 : 0;
+    tot += (r == 'G' || r == 'C' || r == 'A' || r == 'T') ? 1 : 0;
+    qi += op != 2 ? 1 : 0;
+    ri += isI ? 0 : 1;
   }
   O->log_lk = lk;
   O->n_hq = n_hq;

@@ -140,8 +140,10 @@ struct AlignArgs {
   int* err;
 };
 // K3b, band <= band_max <= 31; grid sized from the shared memory per warp.
+// AlignArgs::tb_global must hold band_tb_slab_bytes(lmax, nmax, num_sms,
+// band_max) bytes (the per-alignment traceback rows).
 void launch_align_band(const AlignArgs& a, int num_sms, int band_max, cudaStream_t st);
-size_t band_smem_bytes(int lmax, int nmax);  // per warp at 8 columns per lane
+size_t band_tb_slab_bytes(int lmax, int nmax, int num_sms, int band_max);
 // K3w, one job per block of 8 warps; tb_global_per_warp is the global slab of
 // one block (window_slab_bytes), used by windows that do not fit the block's
 // shared memory.

@@ -104,6 +104,7 @@ static int ensure_chunk(pbw_handle* h, const ChunkCfg& c) {
   TRY(grow(h, h->d_hits_pool, OVF_POOL_HITS));
   TRY(grow(h, h->d_cl_scratch, OVF_POOL_HITS * 112));
   if (h->opt.max_indel_len > 31) TRY(ensure_window_slab(h, c.lmax, c.nmax, window_grid(h)));
+  else TRY(grow(h, h->d_tb_global, band_tb_slab_bytes(c.lmax, c.nmax, h->num_sms, (int)h->opt.max_indel_len)));
   return PBW_OK;
 }
 
@@ -272,7 +273,7 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   aa.lmax = cfg.lmax;
   aa.nmax = cfg.nmax;
   aa.tb_smem = 0;
-  aa.tb_global = nullptr;
+  aa.tb_global = h->d_tb_global.p;
   aa.tb_global_per_warp = 0;
   aa.counters = h->d_cnt64.p + 3;
   aa.err = h->d_err.p;
@@ -915,7 +916,8 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
     aa.lmax = lmax_s;
     aa.nmax = nmax_s;
     aa.tb_smem = 0;
-    aa.tb_global = nullptr;
+    TRY(grow(h, h->d_tb_global, band_tb_slab_bytes(lmax_s, nmax_s, h->num_sms, bmax_s)));
+    aa.tb_global = h->d_tb_global.p;
     aa.tb_global_per_warp = 0;
     launch_align_band(aa, h->num_sms, bmax_s, h->st);
     CK(cudaGetLastError());
