@@ -73,16 +73,6 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ uint8_t up_ascii_b(uint8_t b) { return (b >= 'a' && b <= 'z') ? (uint8_t)(b - 32) : b; }
-__device__ __forceinline__ uint8_t comp_ascii_b(uint8_t b) {
-  switch (b) {
-    case 'A': return 'T';
-    case 'T': return 'A';
-    case 'C': return 'G';
-    case 'G': return 'C';
-    default: return 'N';
-  }
-}
 
 template <int C>
 __device__ __forceinline__ void store_tb(unsigned char* row, int k, uint32_t word) {
@@ -296,10 +286,10 @@ __global__ void __launch_bounds__(32, 16) k_align_band(AlignArgs p, BandLayout L
           s = qbases[qo + i];
           q = qquals[qo + i];
         } else if (!J.rev) {
-          s = up_ascii_b(qbases[qo + i]);
+          s = up_ascii(qbases[qo + i]);
           q = qquals[qo + i];
         } else {
-          s = comp_ascii_b(up_ascii_b(qbases[qo + m - 1 - i]));
+          s = comp_ascii(up_ascii(qbases[qo + m - 1 - i]));
           q = qquals[qo + m - 1 - i];
         }
         rowi[i] = (int32_t)((uint32_t)__ldg(&p.tab->mmpen[q]) << 16) | ((int32_t)q << 8) | (int32_t)s;
@@ -310,7 +300,7 @@ __global__ void __launch_bounds__(32, 16) k_align_band(AlignArgs p, BandLayout L
         for (int j = k; j < n; j += G) coli[j] = make_int2(0, p.ref_bytes[J.ref_start + j]);
       } else {
         const uint64_t gb = __ldg(&p.G.cbase[J.contig]) + J.ref_start;
-        for (int j = k; j < n; j += G) coli[j] = make_int2(0, (int)(uint8_t)"ACGTN"[gcode(p.G, gb + j)]);
+        for (int j = k; j < n; j += G) coli[j] = make_int2(0, (int)code_ascii(gcode(p.G, gb + j)));
       }
       for (int j = k; j < B_PADC; j += G) {
         coli[-1 - j] = make_int2(0, 0);

@@ -16,44 +16,6 @@
 
 namespace pbw {
 
-__device__ __forceinline__ uint8_t up_ascii_s(uint8_t b) { return (b >= 'a' && b <= 'z') ? (uint8_t)(b - 32) : b; }
-__device__ __forceinline__ uint8_t comp_ascii_s(uint8_t b) {
-  switch (b) {
-    case 'A': return 'T';
-    case 'T': return 'A';
-    case 'C': return 'G';
-    case 'G': return 'C';
-    default: return 'N';
-  }
-}
-
-// Byte cursor over one read that fetches aligned 8-byte words: one load per
-// eight bases instead of one per base. Only whole words inside the read's own
-// bytes [lo, lim) are loaded as words; the words at its two ends are put
-// together from byte loads, so no byte outside the read is touched.
-struct ByteCursor {
-  const uint8_t* lo;
-  const uint8_t* lim;
-  uintptr_t wcur;  // address of the loaded word, or 1
-  uint64_t word;
-  __device__ __forceinline__ uint8_t at(const uint8_t* ptr) {
-    const uintptr_t a = (uintptr_t)ptr;
-    const uintptr_t wa = a & ~(uintptr_t)7;
-    if (wa != wcur) {
-      wcur = wa;
-      if (wa >= (uintptr_t)lo && wa + 8 <= (uintptr_t)lim) {
-        word = *(const uint64_t*)wa;
-      } else {
-        word = 0;
-        for (int k = 0; k < 8; k++) {
-          const uintptr_t b = wa + k;
-          if (b >= (uintptr_t)lo && b < (uintptr_t)lim) word |= (uint64_t)(*(const uint8_t*)b) << (8 * k);
-        }
-      }
-    }
-    return (uint8_t)(word >> (8 * (a & 7)));
-  }
-};
 
 __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
   __shared__ double s_llk[2][256];
@@ -83,30 +45,16 @@ __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
   const uint64_t rpos = O->pos;
   const int span = (int)O->span;
   const bool fwd = p.ref_bytes || !J.rev;
-  ByteCursor cb{bases + qo, bases + qo + m, 1, 0};
-  ByteCursor cq{quals + qo, quals + qo + m, 1, 0};
-  // reference cursor: one 2-bit word and its N-mask word per 32 bases
-  const uint64_t gb = p.ref_bytes ? 0 : __ldg(&p.G.cbase[J.contig]) + rpos;
-  uint64_t gword = 0;
-  uint32_t gmask = 0;
-  uint64_t gwi = ~0ull;
-  auto rsym = [&](int ri) -> uint8_t {
-    if (p.ref_bytes) return p.ref_bytes[rpos + ri];
-    const uint64_t gp = gb + (uint64_t)ri;
-    if ((gp >> 5) != gwi) {
-      gwi = gp >> 5;
-      gword = __ldg(&p.G.bits[gwi]);
-      gmask = __ldg(&p.G.nmask[gwi]);
-    }
-    if ((gmask >> (gp & 31)) & 1u) return (uint8_t)'N';
-    return (uint8_t)"ACGT"[(gword >> ((gp & 31) * 2)) & 3ull];
-  };
+  // gsafe: the contig's first base, read (and ignored) when the operation has no reference base
+  const uint64_t gsafe = p.ref_bytes ? 0 : __ldg(&p.G.cbase[J.contig]);
+  const uint64_t gb = gsafe + rpos;
   const double ln_quarter = p.tab->ln_quarter;
   double lk = 0.0;
   int qi = 0, ri = 0, cur = 0;
   int n_hq = 0, m_hq = 0, readlen = 0, indel_runs = 0, del_runs = 0, nm = 0, gc = 0, tot = 0;
-  // One operation per iteration, with the run bookkeeping inside, so that
-  // the lanes of a warp step through their different CIGARs together.
+  // One operation per iteration with plain loads (the reads, qualities and
+  // genome words a lane walks stay in L1): no per-lane reload branches, so the
+  // lanes of a warp step through their different CIGARs together.
   uint32_t k = 0;
   int op = 0, left = 0;
   while (true) {
@@ -122,20 +70,29 @@ __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
     }
     left--;
     const bool isM = op == 0, isI = op == 1;
-    const uint8_t r = (!isI && ri < span) ? rsym(ri) : (uint8_t)0;
+    const bool rv = !isI && ri < span;
+    uint8_t r = 0;
+    if (p.ref_bytes) {
+      r = rv ? p.ref_bytes[rpos + ri] : (uint8_t)0;
+    } else {
+      const uint64_t gp = rv ? gb + (uint64_t)ri : gsafe;
+      const unsigned long long gw = __ldg(&p.G.bits[gp >> 5]);
+      const unsigned int gm = __ldg(&p.G.nmask[gp >> 5]);
+      const uint8_t code = ((gm >> (gp & 31)) & 1u) ? 4 : (uint8_t)((gw >> ((gp & 31) * 2)) & 3ull);
+      r = rv ? code_ascii(code) : (uint8_t)0;
+    }
     const bool qv = qi < m;
     const bool mcond = isM && qv && ri < span;
-    const uint64_t qx = fwd ? qo + (uint64_t)qi : qo + (uint64_t)(m - 1 - qi);
-    uint8_t a = 0, q = 0;
-    if (mcond) {
-      a = cb.at(bases + qx);
-      if (!p.ref_bytes) a = J.rev ? comp_ascii_s(up_ascii_s(a)) : up_ascii_s(a);
-      q = cq.at(quals + qx);
-    }
+    const uint64_t qx = fwd ? qo + (uint64_t)qi : qo + (uint64_t)(m - 1 - (qv ? qi : 0));
+    uint8_t a = bases[qv ? qx : qo];
+    if (!p.ref_bytes) a = J.rev ? comp_ascii(up_ascii(a)) : up_ascii(a);
+    const uint8_t q = quals[qv ? qx : qo];
+    a = mcond ? a : (uint8_t)0;
+    const uint8_t qm = mcond ? q : (uint8_t)0;
     const bool mism = a != r;
     // a D operation adds +0.0, which leaves lk unchanged (lk is never -0.0)
-    lk += mcond ? s_llk[mism ? 1 : 0][q] : ((isI && qv) ? ln_quarter : 0.0);
-    const bool hq = q >= 10;
+    lk += mcond ? s_llk[mism ? 1 : 0][qm] : ((isI && qv) ? ln_quarter : 0.0);
+    const bool hq = qm >= 10;
     n_hq += (mcond && hq) ? 1 : 0;
     m_hq += (mcond && mism && a != 'N' && r != 'N' && hq) ? 1 : 0;
     nm += ((mcond && mism) || !isM) ? 1 : 0;

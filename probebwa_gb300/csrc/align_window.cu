@@ -51,16 +51,6 @@ size_t window_smem_bytes(int lmax, int nmax) {
   return std::min(want, std::max(WIN_SMEM_CAP, fixed + 16 * 1024));
 }
 
-__device__ __forceinline__ uint8_t up_ascii_x(uint8_t b) { return (b >= 'a' && b <= 'z') ? (uint8_t)(b - 32) : b; }
-__device__ __forceinline__ uint8_t comp_ascii_x(uint8_t b) {
-  switch (b) {
-    case 'A': return 'T';
-    case 'T': return 'A';
-    case 'C': return 'G';
-    case 'G': return 'C';
-    default: return 'N';
-  }
-}
 
 struct XBand {
   long long hint, band;
@@ -136,10 +126,10 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
         b = bases[qo + i];
         q = quals[qo + i];
       } else if (!J.rev) {
-        b = up_ascii_x(bases[qo + i]);
+        b = up_ascii(bases[qo + i]);
         q = quals[qo + i];
       } else {
-        b = comp_ascii_x(up_ascii_x(bases[qo + m - 1 - i]));
+        b = comp_ascii(up_ascii(bases[qo + m - 1 - i]));
         q = quals[qo + m - 1 - i];
       }
       qs[i] = b;
@@ -150,7 +140,7 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
       for (int j = tid; j < n; j += WIN_THREADS) rs[j] = p.ref_bytes[J.ref_start + j];
     } else {
       const uint64_t gb = __ldg(&p.G.cbase[J.contig]) + J.ref_start;
-      for (int j = tid; j < n; j += WIN_THREADS) rs[j] = (uint8_t)"ACGTN"[gcode(p.G, gb + j)];
+      for (int j = tid; j < n; j += WIN_THREADS) rs[j] = code_ascii(gcode(p.G, gb + j));
     }
     if (tid == 0) {
       s_best = 0;

@@ -516,13 +516,15 @@ void launch_read_summary(const ReadSummaryArgs& a, cudaStream_t st) {
   if (a.nr == 0) return;
   k_read_summary<<<(unsigned)(((uint64_t)a.nr + 127) / 128), 128, 0, st>>>(a);
 }
+// A batch has at most 2000 pairs of serial FP64 work, and an SM's FP64 pipe
+// takes two lanes per clock: one warp per block spreads a batch over ~60 SMs.
 void launch_pair_decide(const PairArgs& a, cudaStream_t st) {
   if (a.np == 0) return;
-  k_pair_decide<<<(a.np + 127) / 128, 128, 0, st>>>(a);
+  k_pair_decide<<<(a.np + 31) / 32, 32, 0, st>>>(a);
 }
 void launch_pair_resolve(const PairArgs& a, cudaStream_t st) {
   if (a.np == 0) return;
-  k_pair_resolve<<<(a.np + 127) / 128, 128, 0, st>>>(a);
+  k_pair_resolve<<<(a.np + 31) / 32, 32, 0, st>>>(a);
 }
 void launch_pair_cigar_gather(const PairArgs& a, const uint32_t* cig_off, const uint32_t* cig_pool, uint32_t* cigar,
                               uint64_t g0, uint32_t n, cudaStream_t st) {

@@ -44,6 +44,16 @@ __host__ __device__ inline uint8_t base_code(uint8_t b) {
 // DnaSeq::reverse_complement (src/types.rs:34-48): non-ACGT -> N.
 __host__ __device__ inline uint8_t comp_code(uint8_t c) { return c < 4 ? (uint8_t)(3 - c) : (uint8_t)4; }
 
+// ASCII of a reference code 0..4 (A C G T N) from a packed constant: no
+// memory access, so lanes with different codes stay in one instruction.
+__host__ __device__ __forceinline__ uint8_t code_ascii(uint32_t c) { return (uint8_t)(0x4E54474341ull >> (8 * c)); }
+// DnaSeq::from_ascii upper-casing and reverse_complement on ASCII (A<->T,
+// C<->G, anything else N), as selects rather than a switch.
+__host__ __device__ __forceinline__ uint8_t up_ascii(uint8_t b) { return (b >= 'a' && b <= 'z') ? (uint8_t)(b - 32) : b; }
+__host__ __device__ __forceinline__ uint8_t comp_ascii(uint8_t b) {
+  return b == 'A' ? (uint8_t)'T' : b == 'T' ? (uint8_t)'A' : b == 'C' ? (uint8_t)'G' : b == 'G' ? (uint8_t)'C' : (uint8_t)'N';
+}
+
 struct DevGenome {
   const unsigned long long* bits;
   const unsigned int* nmask;
