@@ -52,12 +52,14 @@ struct BandLayout {
 // alignments of a warp use different banks.
 __host__ __device__ inline BandLayout band_layout(int lmax, int nmax, int row_bytes) {
   BandLayout L;
-  // the window columns are dead once the DP is done: the CIGAR run stack of
-  // the traceback reuses their space
+  // The read rows and window columns are dead once the DP is done: the
+  // traceback's chunk ring and CIGAR run stack reuse their space.
   L.o_col = b16(4 * ((size_t)lmax + 2 * B_PADR));
-  L.o_runs = L.o_col;
-  L.o_ring = L.o_col + std::max(b16(8 * ((size_t)nmax + 2 * B_PADC)), b16(2 * ((size_t)lmax + nmax + 2)));
-  const size_t s = L.o_ring + 2 * TB_CH * (size_t)row_bytes;
+  const size_t dp_bytes = L.o_col + b16(8 * ((size_t)nmax + 2 * B_PADC));
+  L.o_ring = 0;
+  L.o_runs = 2 * TB_CH * (size_t)row_bytes;
+  const size_t tb_bytes = L.o_runs + b16(2 * ((size_t)lmax + nmax + 2));
+  const size_t s = std::max(dp_bytes, tb_bytes);
   L.bytes = ((s + 127) & ~(size_t)127) + 32;
   L.tb_job = (((size_t)lmax + 1 + TB_CH - 1) / TB_CH) * TB_CH * row_bytes;
   return L;
