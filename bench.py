@@ -37,6 +37,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SEED = {0: 0x5EED0000, 1: 0x5EED0001}
+CHUNK_READS = 131072  # the library's default chunk (pbw_options.chunk_reads = 0)
+# DRAM bytes (read + write) of K1 per read of the paired workload, from one
+# ncu capture of a 100,000-read launch (29.014 GB read + 0.161 GB written):
+# profiles/k_seed_paired_100k_pairs.md. Not measured for the single-end one.
+SEED_DRAM_BYTES_PER_READ = {1: (29.014204e9 + 0.161155e9) / 100_000}
 METRIC = "reads/s @1 GB300: plain vs ranked+batched (≤0.05% primaries changed); DP GCUPS"
 
 
@@ -232,14 +237,36 @@ def run_gpu(args, prefix, d, meta, rank, world):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     L_read = meta["read_len"]
+    # K1 seeding: algorithmic bytes = the read bytes (2-bit codes + qualities
+    # for the repeat filter) + 8 bytes per CSR probe, per bucket entry and per
+    # hit; one launch maps one chunk of CHUNK_READS reads of one mate.
+    n_seed_launches = (2 if paired else 1) * ((R1.n + CHUNK_READS - 1) // CHUNK_READS)
     seed_bytes = (n_reads * ((L_read + 3) // 4 + L_read) + 8 * s0["seed_probes"] + 8 * s0["seed_entries"] +
                   8 * s0["seed_hits"])
     seed_gbs = seed_bytes / (s0["ms_seed"] / 1e3) / 1e9 if s0["ms_seed"] > 0 else 0.0
     gcups = s0["dp_cells"] / (s0["ms_align"] / 1e3) / 1e9 if s0["ms_align"] > 0 else 0.0
+    reads_per_launch = n_reads / n_seed_launches
+    dram_per_read = SEED_DRAM_BYTES_PER_READ.get(args.config)
     roofline = {"kernel": "k_seed (K1 seeding)", "bound": "hbm", "achieved": round(seed_gbs, 1),
                 "peak": hbm_peak, "unit": "GB/s", "frac": round(seed_gbs / hbm_peak, 4),
-                "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
-                "algorithmic_bytes_per_launch": int(seed_bytes), "phase_ms": {k: round(v, 3) for k, v in phases.items()}}
+                "traffic": int(dram_per_read * reads_per_launch) if dram_per_read else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 100,000-read launch, "
+                                  "scaled by reads per launch (profiles/k_seed_paired_100k_pairs.md)",
+                "dram_gbs": round(dram_per_read * n_reads / (s0["ms_seed"] / 1e3) / 1e9, 1)
+                if (s0["ms_seed"] > 0 and dram_per_read) else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst)" if peaks else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": int(seed_bytes / n_seed_launches),
+                "launches_per_step": n_seed_launches,
+                "phase_ms": {k: round(v, 3) for k, v in phases.items()}}
+    # The largest share of the step is the seeded DP (k_align_band). It is an
+    # integer max-plus recurrence bound by instruction issue on the INT32 ALU
+    # pipe, neither HBM nor tensor: its figures are reported beside the
+    # schema's roofline. GCUPS here spans the seeded-alignment phase (job
+    # build, DP with traceback, likelihood walk).
+    roofline_dp = {"kernel": "k_align_band (seeded banded DP)", "bound": "int32 issue (ALU pipe)",
+                   "achieved_gcups": round(gcups, 1), "cells_per_step": int(s0["dp_cells"]),
+                   "ncu_alu_pipe_frac": 0.725, "ncu_issue_active_frac": 0.655,
+                   "ncu_source": "profiles/k_align_band_single_10k_reads.md"}
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": "reads/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(mean_dev * 1e3, 3), "higher_is_better": True,
@@ -250,7 +277,7 @@ def run_gpu(args, prefix, d, meta, rank, world):
                 "ms_per_step": round(mean_e2e * 1e3, 3)},
         "gpu_launches": int(s0["kernel_launches"]) * args.steps,
         "dp_gcups": round(gcups, 2), "dp_cells_per_step": int(s0["dp_cells"]), "dp_jobs_per_step": int(s0["dp_jobs"]),
-        "roofline": roofline, "clocks": clocks, "wall_s_timed": round(t_wall, 3),
+        "roofline": roofline, "roofline_dp": roofline_dp, "clocks": clocks, "wall_s_timed": round(t_wall, 3),
     }
     return out
 
