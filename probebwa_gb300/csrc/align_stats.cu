@@ -17,11 +17,20 @@
 namespace pbw {
 
 
+// Symbols are compared as codes: reference A0 C1 G2 T3 N4 from the 2-bit
+// words and N mask; read bytes through base_code (upper case, A C G T N, any
+// other byte 5, which equals no reference code) and, on the reverse strand,
+// complemented (3 - c for A C G T, N otherwise, as comp_ascii). Equal codes
+// are exactly equal ASCII symbols of the byte comparisons (bayesian.rs:156).
+// Explicit problems (raw bytes on both sides) compare the bytes themselves.
+template <bool EXPLICIT>
 __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
   __shared__ double s_llk[2][256];
+  __shared__ uint8_t s_code[256];
   for (int k = threadIdx.x; k < 256; k += blockDim.x) {
     s_llk[0][k] = p.tab->llk_match[k];
     s_llk[1][k] = p.tab->llk_mismatch[k];
+    s_code[k] = base_code((uint8_t)k);
   }
   __syncthreads();
   const unsigned int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -44,9 +53,13 @@ __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
   const int m = (int)(offs[J.read + 1] - qo);
   const uint64_t rpos = O->pos;
   const int span = (int)O->span;
-  const bool fwd = p.ref_bytes || !J.rev;
+  const bool rev = !EXPLICIT && J.rev;
+  // read cursor: walks the read forwards, or backwards on the reverse strand
+  const uint8_t* qb = bases + qo + (rev ? m - 1 : 0);
+  const uint8_t* qq = quals + qo + (rev ? m - 1 : 0);
+  const long long dir = rev ? -1 : 1;
   // gsafe: the contig's first base, read (and ignored) when the operation has no reference base
-  const uint64_t gsafe = p.ref_bytes ? 0 : __ldg(&p.G.cbase[J.contig]);
+  const uint64_t gsafe = EXPLICIT ? 0 : __ldg(&p.G.cbase[J.contig]);
   const uint64_t gb = gsafe + rpos;
   const double ln_quarter = p.tab->ln_quarter;
   double lk = 0.0;
@@ -71,35 +84,41 @@ __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
     left--;
     const bool isM = op == 0, isI = op == 1;
     const bool rv = !isI && ri < span;
-    uint8_t r = 0;
-    if (p.ref_bytes) {
-      r = rv ? p.ref_bytes[rpos + ri] : (uint8_t)0;
+    const bool qv = qi < m;
+    const bool mcond = isM && qv && rv;
+    uint32_t rc, ac;  // reference and read symbols (codes, or raw bytes for explicit problems)
+    if (EXPLICIT) {
+      rc = rv ? p.ref_bytes[rpos + ri] : 0u;
+      ac = mcond ? *qb : 0u;
     } else {
       const uint64_t gp = rv ? gb + (uint64_t)ri : gsafe;
       const unsigned long long gw = __ldg(&p.G.bits[gp >> 5]);
       const unsigned int gm = __ldg(&p.G.nmask[gp >> 5]);
-      const uint8_t code = ((gm >> (gp & 31)) & 1u) ? 4 : (uint8_t)((gw >> ((gp & 31) * 2)) & 3ull);
-      r = rv ? code_ascii(code) : (uint8_t)0;
+      rc = ((gm >> (gp & 31)) & 1u) ? 4u : (uint32_t)((gw >> ((gp & 31) * 2)) & 3ull);
+      const uint32_t c0 = mcond ? s_code[*qb] : 4u;
+      ac = rev ? (c0 < 4u ? 3u - c0 : 4u) : c0;
     }
-    const bool qv = qi < m;
-    const bool mcond = isM && qv && ri < span;
-    const uint64_t qx = fwd ? qo + (uint64_t)qi : qo + (uint64_t)(m - 1 - (qv ? qi : 0));
-    uint8_t a = bases[qv ? qx : qo];
-    if (!p.ref_bytes) a = J.rev ? comp_ascii(up_ascii(a)) : up_ascii(a);
-    const uint8_t q = quals[qv ? qx : qo];
-    a = mcond ? a : (uint8_t)0;
-    const uint8_t qm = mcond ? q : (uint8_t)0;
-    const bool mism = a != r;
+    const uint32_t q = mcond ? (uint32_t)*qq : 0u;
+    const uint32_t nsym = EXPLICIT ? (uint32_t)'N' : 4u;
+    const bool mism = ac != rc;
     // a D operation adds +0.0, which leaves lk unchanged (lk is never -0.0)
-    lk += mcond ? s_llk[mism ? 1 : 0][qm] : ((isI && qv) ? ln_quarter : 0.0);
-    const bool hq = qm >= 10;
+    lk += mcond ? s_llk[mism ? 1 : 0][q] : ((isI && qv) ? ln_quarter : 0.0);
+    const bool hq = q >= 10u;
     n_hq += (mcond && hq) ? 1 : 0;
-    m_hq += (mcond && mism && a != 'N' && r != 'N' && hq) ? 1 : 0;
+    m_hq += (mcond && mism && ac != nsym && rc != nsym && hq) ? 1 : 0;
     nm += ((mcond && mism) || !isM) ? 1 : 0;
     readlen += (mcond || isI) ? 1 : 0;
-    gc += (r == 'G' || r == 'C') ? 1 : 0;
-    tot += (r == 'G' || r == 'C' || r == 'A' || r == 'T') ? 1 : 0;
-    qi += op != 2 ? 1 : 0;
+    if (EXPLICIT) {
+      gc += (rv && (rc == 'G' || rc == 'C')) ? 1 : 0;
+      tot += (rv && (rc == 'G' || rc == 'C' || rc == 'A' || rc == 'T')) ? 1 : 0;
+    } else {
+      gc += (rv && (rc == 1u || rc == 2u)) ? 1 : 0;
+      tot += (rv && rc < 4u) ? 1 : 0;
+    }
+    const bool adv_q = op != 2;
+    qi += adv_q ? 1 : 0;
+    qb += adv_q ? dir : 0;
+    qq += adv_q ? dir : 0;
     ri += isI ? 0 : 1;
   }
   O->log_lk = lk;
@@ -115,7 +134,8 @@ __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
 
 void launch_aln_stats(const AlignArgs& a, uint64_t max_jobs, cudaStream_t st) {
   if (max_jobs == 0) return;
-  k_aln_stats<<<(unsigned)((max_jobs + 127) / 128), 128, 0, st>>>(a);
+  if (a.ref_bytes) k_aln_stats<true><<<(unsigned)((max_jobs + 127) / 128), 128, 0, st>>>(a);
+  else k_aln_stats<false><<<(unsigned)((max_jobs + 127) / 128), 128, 0, st>>>(a);
 }
 
 }  // namespace pbw
