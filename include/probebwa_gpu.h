@@ -175,6 +175,27 @@ int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_re
                       uint32_t* total_cand, uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,
                       double* cand_score);
 
+/* MapqCalculator::select_best + finalize_mapq (src/mapq/bayesian.rs:193-201,
+ * 251-282) for a batch of n = reads->n reads. Per read i: the candidates'
+ * log-likelihoods lks[lk_off[i] .. lk_off[i+1]) (at least one); the repeat
+ * mask of find_seed_hits, one probability per 15-mer window,
+ * repeat[win_off[i] .. win_off[i+1]); and the winning alignment: rev[i]
+ * (query = the read's reverse complement), the reference window passed to
+ * finalize_mapq refs[ref_off[i] .. ref_off[i+1]) (it starts at the
+ * alignment's first reference base) and its CIGAR cigar[cigar_off[i] ..
+ * cigar_off[i+1]) packed as in pbw_records. Outputs: mapq, posterior, the
+ * winner's index among the read's candidates (the last maximum) and sum_exp
+ * (the softmax denominator). Host buffers in and out. Reference windows
+ * of more than 1280 ACGT bases take their GC terms from the device libm. */
+int pbw_mapq_batch(pbw_handle* h, const pbw_reads* reads, const uint64_t* lk_off, const double* lks,
+                   const uint64_t* win_off, const double* repeat, const uint8_t* rev, const uint64_t* ref_off,
+                   const uint8_t* refs, const uint32_t* cigar_off, const uint32_t* cigar, uint8_t* mapq,
+                   double* posterior, uint32_t* best, double* sum_exp);
+
+/* Output sizes for a map call on these reads: the number of records (one per
+ * read) and a CIGAR capacity that always suffices (pbw_records.cigar_cap). */
+int pbw_records_reserve(const pbw_reads* reads, uint64_t* n_records, uint64_t* cigar_cap);
+
 /* Timing and counters of the last map call on this handle. */
 int pbw_last_stats(const pbw_handle* h, pbw_stats* st);
 

@@ -1972,6 +1972,44 @@ int orc_align(const uint8_t* read, const uint8_t* qual, uint64_t m, const uint8_
 }
 
 // format_sam_records (sam.rs:69-108) with format_sam (sam.rs:37-58).
+// MapqCalculator::select_best + finalize_mapq (bayesian.rs:193-201, 251-282)
+// for a batch of reads, each with its candidates' log-likelihoods, its repeat
+// mask and its winner's alignment (strand, reference window as passed to
+// finalize_mapq, CIGAR).
+int orc_mapq_batch(void* h, const orc_reads* reads, const uint64_t* lk_off, const double* lks,
+                   const uint64_t* win_off, const double* repeat, const uint8_t* rev, const uint64_t* ref_off,
+                   const uint8_t* refs, const uint32_t* cigar_off, const uint32_t* cigar, uint8_t* mapq,
+                   double* posterior, uint32_t* best, double* sum_exp) {
+  Mapper* m = (Mapper*)h;
+  for (uint64_t i = 0; i < reads->n; i++) {
+    if (lk_off[i + 1] <= lk_off[i]) return -1;
+    std::vector<double> l(lks + lk_off[i], lks + lk_off[i + 1]);
+    size_t b;
+    double se;
+    m->mq->select_best(l, b, se);
+    Read rd = make_read(reads, i);
+    std::vector<u8> qb = rev[i] ? revcomp(rd.bases) : rd.bases;
+    std::vector<u8> qq = rd.quals;
+    if (rev[i]) std::reverse(qq.begin(), qq.end());
+    std::vector<u8> rw(refs + ref_off[i], refs + ref_off[i + 1]);
+    std::vector<Cig> c;
+    for (uint32_t k = cigar_off[i]; k < cigar_off[i + 1]; k++) {
+      const uint32_t w = cigar[k];
+      const char op = "MID?S"[std::min<uint32_t>(w & 15u, 4u)];
+      c.push_back(Cig{op, w >> 4});
+    }
+    std::vector<double> mask(repeat + win_off[i], repeat + win_off[i + 1]);
+    u8 mq;
+    double post;
+    m->mq->finalize(se, rd, c, qb, qq, rw, mask, mq, post);
+    mapq[i] = mq;
+    posterior[i] = post;
+    best[i] = (uint32_t)b;
+    sum_exp[i] = se;
+  }
+  return 0;
+}
+
 int orc_write_sam(void* h, const char* path, const char* command_line, const orc_reads* reads,
                   const char* const* read_ids, const orc_records* recs) {
   Mapper* m = (Mapper*)h;

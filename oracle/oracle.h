@@ -113,6 +113,12 @@ int64_t orc_cluster_read(void* h, const uint8_t* bases, const uint8_t* quals, ui
                          uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,
                          double* cand_score, uint64_t cand_cap);
 // SmithWatermanAligner::new + align (src/align/smith_waterman.rs:113-255).
+/* MapqCalculator::select_best + finalize_mapq (src/mapq/bayesian.rs:193-201,
+ * 251-282) for a batch; see pbw_mapq_batch for the layout. */
+int orc_mapq_batch(void* h, const orc_reads* reads, const uint64_t* lk_off, const double* lks,
+                   const uint64_t* win_off, const double* repeat, const uint8_t* rev, const uint64_t* ref_off,
+                   const uint8_t* refs, const uint32_t* cigar_off, const uint32_t* cigar, uint8_t* mapq,
+                   double* posterior, uint32_t* best, double* sum_exp);
 int orc_align(const uint8_t* read, const uint8_t* qual, uint64_t m, const uint8_t* ref, uint64_t n,
               int64_t hint, uint64_t band, uint32_t gop, uint32_t gep, int32_t* score,
               uint64_t* offset, uint32_t* cigar, uint64_t cigar_cap, uint64_t* n_ops);

@@ -108,6 +108,7 @@ def lib():
         L.orc_cluster_read.argtypes = [vp, vp, vp, u64, vp, vp, vp, vp, u64]
         L.orc_cluster_read.restype = i64
         L.orc_align.argtypes = [vp, vp, u64, vp, u64, i64, u64, u32, u32, vp, vp, vp, u64, vp]
+        L.orc_mapq_batch.argtypes = [vp, C.POINTER(ReadsC), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_write_sam.argtypes = [vp, cp, cp, C.POINTER(ReadsC), C.POINTER(cp), C.POINTER(RecordsC)]
         L.orc_reads_parse.argtypes = [cp, C.c_int, C.c_uint8, cp]
         L.orc_reads_parse.restype = vp
@@ -204,6 +205,28 @@ def records_c(r: dict) -> RecordsC:
     return RecordsC(n, *[_ptr(r[k]) for k in ("contig", "pos", "mapq", "flag", "mate_contig", "mate_pos", "tlen",
                                                "log_lk", "posterior", "as_score", "nm", "cigar_off", "cigar")],
                     len(r["cigar"]))
+
+
+def pack_mapq_items(items):
+    """Flattens per-read MAPQ inputs (dicts with lks, repeat, rev, ref, cigar)
+    into the concatenated arrays of the *_mapq_batch entry points."""
+    n = len(items)
+    lk_off = np.zeros(n + 1, np.uint64)
+    win_off = np.zeros(n + 1, np.uint64)
+    ref_off = np.zeros(n + 1, np.uint64)
+    cig_off = np.zeros(n + 1, np.uint32)
+    lk_off[1:] = np.cumsum([len(it["lks"]) for it in items])
+    win_off[1:] = np.cumsum([len(it["repeat"]) for it in items])
+    ref_off[1:] = np.cumsum([len(it["ref"]) for it in items])
+    cig_off[1:] = np.cumsum([len(it["cigar"]) for it in items])
+    lks = np.concatenate([np.asarray(it["lks"], np.float64) for it in items] + [np.zeros(1)])
+    rep = np.concatenate([np.asarray(it["repeat"], np.float64) for it in items] + [np.zeros(1)])
+    rev = np.array([1 if it["rev"] else 0 for it in items], np.uint8)
+    refs = np.frombuffer(b"".join(bytes(it["ref"]) for it in items) + b"\0", np.uint8).copy()
+    cig = np.concatenate([np.asarray(it["cigar"], np.uint32) for it in items] + [np.zeros(1, np.uint32)])
+    out = {"mapq": np.zeros(n, np.uint8), "posterior": np.zeros(n, np.float64), "best": np.zeros(n, np.uint32),
+           "sum_exp": np.zeros(n, np.float64)}
+    return (lk_off, lks, win_off, rep, rev, ref_off, refs, cig_off, cig), out
 
 
 OPS = "MIDXSH"
@@ -334,6 +357,16 @@ class Mapper:
                                  C.byref(records_c(recs)))
         if rc != 0:
             raise RuntimeError(_err())
+
+    def mapq_batch(self, reads: Reads, items) -> dict:
+        """select_best + finalize_mapq per read; items as pack_mapq_items."""
+        (lk_off, lks, win_off, rep, rev, ref_off, refs, cig_off, cig), out = pack_mapq_items(items)
+        rc = lib().orc_mapq_batch(self.h, C.byref(reads.c()), _ptr(lk_off), _ptr(lks), _ptr(win_off), _ptr(rep),
+                                  _ptr(rev), _ptr(ref_off), _ptr(refs), _ptr(cig_off), _ptr(cig), _ptr(out["mapq"]),
+                                  _ptr(out["posterior"]), _ptr(out["best"]), _ptr(out["sum_exp"]))
+        if rc != 0:
+            raise RuntimeError("orc_mapq_batch failed")
+        return out
 
 
 def align(read: bytes, qual: bytes, ref: bytes, hint: int, band: int, gop=40, gep=3):

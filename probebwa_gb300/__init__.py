@@ -112,6 +112,8 @@ def lib():
             L.pbw_map_paired.argtypes = [vp, C.POINTER(InsertModelC), C.POINTER(ReadsC), C.POINTER(ReadsC),
                                          C.POINTER(RecordsC), C.POINTER(RecordsC)]
         L.pbw_align_batch.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u64]
+        L.pbw_mapq_batch.argtypes = [vp, C.POINTER(ReadsC), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.pbw_records_reserve.argtypes = [C.POINTER(ReadsC), vp, vp]
         L.pbw_seed_batch.argtypes = [vp, C.POINTER(ReadsC), vp, vp, vp, u64, vp, vp, u64]
         L.pbw_cluster_batch.argtypes = [vp, C.POINTER(ReadsC), u32, vp, vp, vp, vp, vp, vp]
         L.pbw_last_stats.argtypes = [vp, C.POINTER(StatsC)]
@@ -199,6 +201,29 @@ def records_c(r: dict) -> RecordsC:
     keep = [r[k] if r[k].size else np.zeros(1, r[k].dtype) for k, _ in RECORD_FIELDS]
     r["_keep"] = keep
     return RecordsC(n, *[_ptr(a) for a in keep], _ptr(r["cigar_off"]), _ptr(r["cigar"]), len(r["cigar"]))
+
+
+def pack_mapq_items(items):
+    """Flattens per-read MAPQ inputs (dicts with lks, repeat, rev, ref, cigar)
+    into the concatenated arrays of the *_mapq_batch entry points."""
+    n = len(items)
+    lk_off = np.zeros(n + 1, np.uint64)
+    win_off = np.zeros(n + 1, np.uint64)
+    ref_off = np.zeros(n + 1, np.uint64)
+    cig_off = np.zeros(n + 1, np.uint32)
+    lk_off[1:] = np.cumsum([len(it["lks"]) for it in items])
+    win_off[1:] = np.cumsum([len(it["repeat"]) for it in items])
+    ref_off[1:] = np.cumsum([len(it["ref"]) for it in items])
+    cig_off[1:] = np.cumsum([len(it["cigar"]) for it in items])
+    lks = np.concatenate([np.asarray(it["lks"], np.float64) for it in items] + [np.zeros(1)])
+    rep = np.concatenate([np.asarray(it["repeat"], np.float64) for it in items] + [np.zeros(1)])
+    rev = np.array([1 if it["rev"] else 0 for it in items], np.uint8)
+    refs = np.frombuffer(b"".join(bytes(it["ref"]) for it in items) + b"\0", np.uint8).copy()
+    cig = np.concatenate([np.asarray(it["cigar"], np.uint32) for it in items] + [np.zeros(1, np.uint32)])
+    out = {"mapq": np.zeros(n, np.uint8), "posterior": np.zeros(n, np.float64), "best": np.zeros(n, np.uint32),
+           "sum_exp": np.zeros(n, np.float64)}
+    return (lk_off, lks, win_off, rep, rev, ref_off, refs, cig_off, cig), out
+
 
 
 OPS = "MIDXSH"
@@ -336,6 +361,27 @@ class Mapper:
         ids = (C.c_char_p * max(reads.n, 1))(*[i.encode() for i in reads.ids])
         self._check(lib().pbw_write_sam(self.h, path.encode(), command_line.encode(), C.byref(reads.c()), ids,
                                         C.byref(records_c(recs))))
+
+    def mapq_batch(self, reads: Reads, items) -> dict:
+        """MapqCalculator::select_best + finalize_mapq (bayesian.rs:193-201,
+        251-282) per read. items: one dict per read with lks (candidate
+        log-likelihoods), repeat (per-window repeat probabilities), rev,
+        ref (the winner's reference window) and cigar (packed u32)."""
+        (lk_off, lks, win_off, rep, rev, ref_off, refs, cig_off, cig), out = pack_mapq_items(items)
+        self._check(lib().pbw_mapq_batch(self.h, C.byref(reads.c()), _ptr(lk_off), _ptr(lks), _ptr(win_off),
+                                         _ptr(rep), _ptr(rev), _ptr(ref_off), _ptr(refs), _ptr(cig_off), _ptr(cig),
+                                         _ptr(out["mapq"]), _ptr(out["posterior"]), _ptr(out["best"]),
+                                         _ptr(out["sum_exp"])))
+        return out
+
+    @staticmethod
+    def records_reserve(reads: Reads) -> tuple:
+        n = np.zeros(1, np.uint64)
+        cap = np.zeros(1, np.uint64)
+        rc = lib().pbw_records_reserve(C.byref(reads.c()), _ptr(n), _ptr(cap))
+        if rc != 0:
+            raise RuntimeError("pbw_records_reserve failed")
+        return int(n[0]), int(cap[0])
 
 
 # ---- reference-shaped API ----

@@ -309,8 +309,8 @@ static int load_hash(pbw_handle* h, const std::string& prefix) {
   CK(cudaMemcpy(&err, h->d_err.p, 4, cudaMemcpyDeviceToHost));
   unsigned int last = 0;
   CK(cudaMemcpy(&last, h->d_csr.p + NKMER, 4, cudaMemcpyDeviceToHost));
-  cudaFree(d_tab.p);
-  cudaFree(d_pos.p);
+  d_tab.release();
+  d_pos.release();
   sums.release();
   if (err) {
     h->err = "sthash: invalid table entry (code " + std::to_string(err) + ")";

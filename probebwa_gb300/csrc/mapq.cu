@@ -107,6 +107,87 @@ __global__ void k_finalize_single(FinalizeArgs p) {
   p.best[r] = (int32_t)(r * MAX_CAND + best);
 }
 
+// MapqCalculator::select_best + finalize_mapq (bayesian.rs:193-201,
+// 251-282) for explicit inputs, one thread per read: the last maximum of the
+// candidates' log-likelihoods and the sequential sum of exp(lk - max); the
+// log_entropy counts (bayesian.rs:306-357) walked over the winner's CIGAR,
+// query (the read, reverse-complemented when rev) and reference window; the
+// missing-locus probability over the read's qualities and repeat mask.
+__global__ void k_mapq_batch(MapqBatchArgs p) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const uint64_t l0 = p.lk_off[i], l1 = p.lk_off[i + 1];
+  double mx = p.lks[l0];
+  uint32_t b = 0;
+  for (uint64_t k = l0; k < l1; k++)
+    if (p.lks[k] >= mx) {
+      mx = p.lks[k];
+      b = (uint32_t)(k - l0);
+    }
+  double se = -0.0;
+  for (uint64_t k = l0; k < l1; k++) se += exp(p.lks[k] - mx);
+  const uint64_t qo = p.offs[i];
+  const int m = (int)(p.offs[i + 1] - qo);
+  const bool rev = p.rev[i] != 0;
+  const uint8_t* rw = p.refs + p.ref_off[i];
+  const uint64_t nrw = p.ref_off[i + 1] - p.ref_off[i];
+  long long n_hq = 0, m_hq = 0, readlen = 0, indel_runs = 0, del_runs = 0;
+  uint64_t refpos = 0;
+  int cur = 0;
+  for (uint64_t k = p.cig_off[i]; k < p.cig_off[i + 1]; k++) {
+    const uint32_t op = p.cigar[k] & 15u, len = p.cigar[k] >> 4;
+    if (op == 1) {
+      indel_runs += (len > 0 && cur != 1) ? 1 : 0;
+      cur = len > 0 ? 1 : cur;
+      readlen += len;
+    } else if (op == 2) {
+      if (len > 0 && cur != 2) {
+        del_runs++;
+        indel_runs++;
+      }
+      cur = len > 0 ? 2 : cur;
+      refpos += len;
+    } else if (op == 0) {
+      for (uint32_t t = 0; t < len; t++) {
+        if (cur != 0) indel_runs++;
+        cur = 0;
+        if (readlen >= m || refpos >= nrw) break;
+        const uint64_t src = rev ? qo + (uint64_t)(m - 1 - readlen) : qo + (uint64_t)readlen;
+        const uint8_t q = p.quals[src];
+        const uint8_t a = rev ? comp_ascii(up_ascii(p.bases[src])) : up_ascii(p.bases[src]);
+        const uint8_t r = rw[refpos];
+        const bool hq = q >= 10;
+        n_hq += hq ? 1 : 0;
+        m_hq += (a != r && a != 'N' && r != 'N' && hq) ? 1 : 0;
+        readlen++;
+        refpos++;
+      }
+    }
+  }
+  int gc = 0, tot = 0;
+  for (uint64_t k = 0; k < nrw; k++) {
+    const uint8_t r = rw[k];
+    gc += (r == 'G' || r == 'C') ? 1 : 0;
+    tot += (r == 'G' || r == 'C' || r == 'A' || r == 'T') ? 1 : 0;
+  }
+  EntropyIn e{(int)n_hq, (int)m_hq, (int)readlen, (int)(indel_runs - del_runs), (int)del_runs, gc, tot};
+  const double ent = log_entropy(e, p.tab, p.gc_lnb, p.gc_lnbm1, p.ln_n);
+  const double pmiss = missing_locus_mask(p.quals + qo, m, p.repeat + p.win_off[i],
+                                          (int)(p.win_off[i + 1] - p.win_off[i]), p.tab);
+  uint8_t mq;
+  double post;
+  finalize_mapq(se, ent, pmiss, p.tab, mq, post);
+  p.mapq[i] = mq;
+  p.post[i] = post;
+  p.best[i] = b;
+  p.sum_exp[i] = se;
+}
+
+void launch_mapq_batch(const MapqBatchArgs& a, cudaStream_t st) {
+  if (a.n == 0) return;
+  k_mapq_batch<<<(unsigned)((a.n + 31) / 32), 32, 0, st>>>(a);
+}
+
 __global__ void k_cigar_gather(CigarGatherArgs p) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= p.nr) return;

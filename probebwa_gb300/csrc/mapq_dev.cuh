@@ -100,6 +100,33 @@ __device__ inline double missing_phase(int phase, const uint8_t* q, int len, con
   return exp(logp);
 }
 
+// missing_phase with the repeat mask given as probabilities per window
+// (the f64 repeat_mask of find_seed_hits, seeds.rs:91-151).
+__device__ inline double missing_phase_mask(int phase, const uint8_t* q, int len, const double* mask, int nmask,
+                                            const DevTables* T) {
+  double logp = 0.0;
+  for (int st = phase; st + KMER <= len; st += KMER) {
+    const double rp = st < nmask ? mask[st] : 0.0;
+    double z = 1.0;
+    for (int t = 0; t < KMER; t++) z = z * T->ml_one_minus_q[q[st + t]];
+    double p1 = -0.0;
+    for (int t = 0; t < KMER; t++) p1 = p1 + T->ml_q_over[q[st + t]];
+    double p2 = 1.0 - z * (1.0 + p1);
+    p2 = p2 < 0.0 ? 0.0 : (p2 > 1.0 ? 1.0 : p2);
+    double pm = 1.0 - (1.0 - p2) * (1.0 - rp);
+    pm = pm < 1e-300 ? 1e-300 : (pm > 1.0 ? 1.0 : pm);
+    logp += log(pm);
+  }
+  return exp(logp);
+}
+__device__ inline double missing_locus_mask(const uint8_t* q, int len, const double* mask, int nmask,
+                                            const DevTables* T) {
+  if (len < KMER) return 0.5;
+  double s = 0.0;
+  for (int k = 0; k < 5; k++) s += missing_phase_mask(k, q, len, mask, nmask, T);
+  return fmin(s / 5.0, 0.99);
+}
+
 // Whole missing-locus probability by one thread: offset_means starts at 0.0
 // and adds phases 0..4 in order.
 __device__ inline double missing_locus_thread(const uint8_t* q, int len, const uint8_t* rep, int nwin,

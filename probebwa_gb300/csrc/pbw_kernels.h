@@ -190,6 +190,32 @@ struct FinalizeArgs {
 };
 void launch_finalize(const FinalizeArgs& a, int grid, cudaStream_t st);
 
+// ---- MapqCalculator batch (pbw_mapq_batch) ----
+struct MapqBatchArgs {
+  const DevTables* tab;
+  const double* ln_n;
+  const double* gc_lnb;
+  const double* gc_lnbm1;
+  uint64_t n;
+  const uint8_t* bases;
+  const uint8_t* quals;
+  const uint64_t* offs;
+  const uint64_t* lk_off;
+  const double* lks;
+  const uint64_t* win_off;
+  const double* repeat;
+  const uint8_t* rev;
+  const uint64_t* ref_off;
+  const uint8_t* refs;
+  const uint64_t* cig_off;
+  const uint32_t* cigar;
+  uint8_t* mapq;
+  double* post;
+  uint32_t* best;
+  double* sum_exp;
+};
+void launch_mapq_batch(const MapqBatchArgs& a, cudaStream_t st);
+
 // ---- host parameter tables (api.cu) ----
 void fill_tables(const pbw_options& opt, uint64_t total_length, DevTables& T);
 void gap_costs(uint32_t gop, uint32_t gep, int32_t& go, int32_t& ge);

@@ -966,6 +966,101 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
   return PBW_OK;
 }
 
+int pbw_records_reserve(const pbw_reads* reads, uint64_t* n_records, uint64_t* cigar_cap) {
+  if (!reads || !n_records || !cigar_cap) return PBW_ERR_ARG;
+  const uint64_t total = reads->n ? reads->offsets[reads->n] - reads->offsets[0] : 0;
+  *n_records = reads->n;
+  *cigar_cap = 2 * total + 2 * reads->n + 1;
+  return PBW_OK;
+}
+
+int pbw_mapq_batch(pbw_handle* h, const pbw_reads* reads, const uint64_t* lk_off, const double* lks,
+                   const uint64_t* win_off, const double* repeat, const uint8_t* rev, const uint64_t* ref_off,
+                   const uint8_t* refs, const uint32_t* cigar_off, const uint32_t* cigar, uint8_t* mapq,
+                   double* posterior, uint32_t* best, double* sum_exp) {
+  if (!h || !reads || !lk_off || !lks || !win_off || !rev || !ref_off || !cigar_off || !mapq || !posterior ||
+      !best || !sum_exp)
+    return PBW_ERR_ARG;
+  cudaSetDevice(h->device);
+  const uint64_t n = reads->n;
+  if (n == 0) return PBW_OK;
+  for (uint64_t i = 0; i < n; i++) {
+    if (lk_off[i + 1] <= lk_off[i]) { h->err = "pbw_mapq_batch: read without candidates"; return PBW_ERR_ARG; }
+    if (reads->offsets[i + 1] - reads->offsets[i] > PBW_MAX_READ_LEN) {
+      h->err = "pbw_mapq_batch: read longer than PBW_MAX_READ_LEN";
+      return PBW_ERR_LIMIT;
+    }
+  }
+  const uint64_t qt = reads->offsets[n], nl = lk_off[n], nw = win_off[n], nr = ref_off[n], nc = cigar_off[n];
+  DevBuf<uint8_t> d_b, d_q, d_rev, d_refs, d_mapq;
+  DevBuf<uint64_t> d_o, d_lo, d_wo, d_ro, d_co;
+  DevBuf<double> d_lk, d_rep, d_post, d_se;
+  DevBuf<uint32_t> d_cig, d_best;
+  TRY(grow(h, d_b, qt + 1));
+  TRY(grow(h, d_q, qt + 1));
+  TRY(grow(h, d_o, n + 1));
+  TRY(grow(h, d_lo, n + 1));
+  TRY(grow(h, d_lk, nl));
+  TRY(grow(h, d_wo, n + 1));
+  TRY(grow(h, d_rep, nw + 1));
+  TRY(grow(h, d_rev, n));
+  TRY(grow(h, d_ro, n + 1));
+  TRY(grow(h, d_refs, nr + 1));
+  TRY(grow(h, d_co, n + 1));
+  TRY(grow(h, d_cig, nc + 1));
+  TRY(grow(h, d_mapq, n));
+  TRY(grow(h, d_post, n));
+  TRY(grow(h, d_best, n));
+  TRY(grow(h, d_se, n));
+  std::vector<uint64_t> o(n + 1), co(n + 1);
+  for (uint64_t i = 0; i <= n; i++) {
+    o[i] = reads->offsets[i] - reads->offsets[0];
+    co[i] = cigar_off[i];
+  }
+  CK(cudaMemcpy(d_b.p, reads->bases + reads->offsets[0], qt - reads->offsets[0], cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_q.p, reads->quals + reads->offsets[0], qt - reads->offsets[0], cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_o.p, o.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_lo.p, lk_off, (n + 1) * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_lk.p, lks, nl * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_wo.p, win_off, (n + 1) * 8, cudaMemcpyHostToDevice));
+  if (nw) CK(cudaMemcpy(d_rep.p, repeat, nw * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_rev.p, rev, n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_ro.p, ref_off, (n + 1) * 8, cudaMemcpyHostToDevice));
+  if (nr) CK(cudaMemcpy(d_refs.p, refs, nr, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_co.p, co.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+  if (nc) CK(cudaMemcpy(d_cig.p, cigar, nc * 4, cudaMemcpyHostToDevice));
+  MapqBatchArgs a{};
+  a.tab = h->d_tab.p;
+  a.ln_n = h->d_ln_n.p;
+  a.gc_lnb = h->d_gc_lnb.p;
+  a.gc_lnbm1 = h->d_gc_lnbm1.p;
+  a.n = n;
+  a.bases = d_b.p;
+  a.quals = d_q.p;
+  a.offs = d_o.p;
+  a.lk_off = d_lo.p;
+  a.lks = d_lk.p;
+  a.win_off = d_wo.p;
+  a.repeat = d_rep.p;
+  a.rev = d_rev.p;
+  a.ref_off = d_ro.p;
+  a.refs = d_refs.p;
+  a.cig_off = d_co.p;
+  a.cigar = d_cig.p;
+  a.mapq = d_mapq.p;
+  a.post = d_post.p;
+  a.best = d_best.p;
+  a.sum_exp = d_se.p;
+  launch_mapq_batch(a, h->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(mapq, d_mapq.p, n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(posterior, d_post.p, n * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(best, d_best.p, n * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(sum_exp, d_se.p, n * 8, cudaMemcpyDeviceToHost));
+  return PBW_OK;
+}
+
 int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uint64_t* hits, uint32_t* hit_read_pos,
                    uint64_t hit_cap, uint64_t* win_off, double* repeat_prob, uint64_t win_cap) {
   if (!h || !reads) return PBW_ERR_ARG;
