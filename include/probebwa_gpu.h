@@ -210,6 +210,20 @@ int pbw_map_single_device(pbw_handle* h, const pbw_reads* dev_reads, pbw_records
 int pbw_write_sam(pbw_handle* h, const char* path, const char* command_line, const pbw_reads* reads,
                   const char* const* read_ids, const pbw_records* recs);
 
+/* Reads from a file: replaces read_reads_files_with_preprocessing
+ * (src/io/fastx.rs:19-48) for one path -- read_fastq (:133-147) or
+ * read_fasta_as_reads (:161-174), then strip_mate_suffix (:77-81) and, when
+ * adapter is not NULL, strip_adapter (:97-117). quality_offset is 33 or 64
+ * (--phred64). pbw_reads_get gives the reads as pbw_reads (the quality track
+ * has the sequence's length: missing scores are 30); pbw_reads_id the i-th
+ * read ID (NUL-terminated, valid until pbw_reads_free). Errors:
+ * PBW_ERR_IO (pbw_last_error(NULL) names the file). Gzip input is not read. */
+typedef struct pbw_read_set pbw_read_set;
+int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const char* adapter, pbw_read_set** out);
+int pbw_reads_get(const pbw_read_set* rs, pbw_reads* view);
+const char* pbw_reads_id(const pbw_read_set* rs, uint64_t i);
+void pbw_reads_free(pbw_read_set* rs);
+
 /* Allocation-free window alignment. No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc -- code running while a stream is
  * captured into a CUDA graph, applications whose allocator owns all device

@@ -114,6 +114,11 @@ def lib():
         L.pbw_align_batch.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u64]
         L.pbw_mapq_batch.argtypes = [vp, C.POINTER(ReadsC), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.pbw_records_reserve.argtypes = [C.POINTER(ReadsC), vp, vp]
+        L.pbw_reads_load.argtypes = [cp, C.c_int, C.c_uint8, cp, C.POINTER(vp)]
+        L.pbw_reads_get.argtypes = [vp, C.POINTER(ReadsC)]
+        L.pbw_reads_id.argtypes = [vp, u64]
+        L.pbw_reads_id.restype = cp
+        L.pbw_reads_free.argtypes = [vp]
         L.pbw_seed_batch.argtypes = [vp, C.POINTER(ReadsC), vp, vp, vp, u64, vp, vp, u64]
         L.pbw_cluster_batch.argtypes = [vp, C.POINTER(ReadsC), u32, vp, vp, vp, vp, vp, vp]
         L.pbw_last_stats.argtypes = [vp, C.POINTER(StatsC)]
@@ -233,6 +238,34 @@ def cigar_strings(r: dict) -> list:
     co, cg = r["cigar_off"], r["cigar"]
     return ["".join(f"{int(w) >> 4}{OPS[int(w) & 15]}" for w in cg[co[i]:co[i + 1]])
             for i in range(len(r["contig"]))]
+
+
+def load_reads(path: str, fasta: bool = False, quality_offset: int = 33, adapter: str | bytes | None = None) -> "Reads":
+    """read_reads_files_with_preprocessing for one file (src/io/fastx.rs:19-48)
+    through pbw_reads_load: bases, Phred scores and IDs as a Reads object."""
+    L = lib()
+    if isinstance(adapter, str):
+        adapter = adapter.encode()
+    h = C.c_void_p()
+    rc = L.pbw_reads_load(path.encode(), 1 if fasta else 0, quality_offset, adapter, C.byref(h))
+    if rc != 0:
+        raise PbwError(rc, L.pbw_last_error(None).decode())
+    try:
+        v = ReadsC()
+        L.pbw_reads_get(h, C.byref(v))
+        n = int(v.n)
+        offs = np.ctypeslib.as_array(C.cast(v.offsets, C.POINTER(C.c_uint64)), shape=(n + 1,)).copy()
+        tot = int(offs[-1])
+        if tot:
+            bases = np.ctypeslib.as_array(C.cast(v.bases, C.POINTER(C.c_uint8)), shape=(tot,)).copy()
+            quals = np.ctypeslib.as_array(C.cast(v.quals, C.POINTER(C.c_uint8)), shape=(tot,)).copy()
+        else:
+            bases = np.zeros(0, np.uint8)
+            quals = np.zeros(0, np.uint8)
+        ids = [L.pbw_reads_id(h, i).decode("utf-8", "replace") for i in range(n)]
+    finally:
+        L.pbw_reads_free(h)
+    return Reads(bases, quals, offs, ids)
 
 
 class Mapper:

@@ -1,0 +1,216 @@
+// fastx.cpp -- the input side of the mapping path: FASTQ / FASTA reads into
+// the structure-of-arrays layout the map calls take (src/io/fastx.rs).
+//
+// The file is read into memory once and split into lines with memchr; each
+// record is decoded straight into the concatenated base, quality and offset
+// arrays. Semantics follow the reference's parsers:
+//  * FASTQ (FastqParser, fastx.rs:226-305): ID = first whitespace-separated
+//    token of the header line after leading '@'s; sequence lines (trimmed)
+//    until a trimmed line starting with '+'; then quality lines (trimmed) until
+//    they cover the sequence, at least one line. Bases are upper-cased
+//    (DnaSeq::from_ascii, types.rs:12-15), qualities are the byte minus the
+//    offset, saturating at 0 (QualityScores::from_phred_ascii, types.rs:57-60).
+//  * FASTA reads (FastaAsReadsParser, fastx.rs:161-224): records start at a
+//    line beginning with '>' (lines before the first are skipped); ID = first
+//    token after leading '>'s; sequence = concatenated trimmed lines up to a
+//    trimmed line starting with '>'; every quality 40 (fastx.rs:159).
+//  * then per read: a trailing "/1" or "/2" is dropped from the ID
+//    (strip_mate_suffix, fastx.rs:77-81) and, with an adapter, the longest
+//    3' overlap of at least 6 bases with at most one mismatch per 10 bases
+//    (case-insensitive) is cut from the bases and qualities (strip_adapter,
+//    fastx.rs:97-117).
+// Whitespace is the ASCII set of Rust's str::trim for ASCII text (space, tab,
+// LF, VT, FF, CR). The quality track handed to the map calls has the
+// sequence's length: missing scores read as 30, extra ones are dropped.
+// Gzip input (flate2 in the reference) is not read.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/probebwa_gpu.h"
+#include "pbw_kernels.h"
+
+struct pbw_read_set {
+  std::vector<uint8_t> bases, quals;
+  std::vector<uint64_t> offsets{0};
+  std::vector<char> id_chars;  // NUL-terminated IDs, back to back
+  std::vector<uint64_t> id_off;
+};
+
+namespace {
+
+inline bool is_ws(uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
+inline uint8_t upper(uint8_t b) { return (b >= 'a' && b <= 'z') ? (uint8_t)(b - 32) : b; }
+
+struct Span {
+  const char* p;
+  size_t n;
+};
+Span trim(Span s) {
+  while (s.n && is_ws((uint8_t)s.p[0])) { s.p++; s.n--; }
+  while (s.n && is_ws((uint8_t)s.p[s.n - 1])) s.n--;
+  return s;
+}
+Span first_token(Span s) {
+  size_t a = 0;
+  while (a < s.n && is_ws((uint8_t)s.p[a])) a++;
+  size_t b = a;
+  while (b < s.n && !is_ws((uint8_t)s.p[b])) b++;
+  return Span{s.p + a, b - a};
+}
+Span strip_leading(Span s, char c) {
+  while (s.n && s.p[0] == c) { s.p++; s.n--; }
+  return s;
+}
+
+// Lines of a buffer; a line keeps its '\n' (as BufRead::read_line).
+struct Lines {
+  const char* p;
+  const char* end;
+  bool next(Span& line) {
+    if (p >= end) return false;
+    const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
+    const char* e = nl ? nl + 1 : end;
+    line = Span{p, (size_t)(e - p)};
+    p = e;
+    return true;
+  }
+};
+
+struct Builder {
+  pbw_read_set* rs;
+  void add(Span id) {
+    // strip_mate_suffix
+    if (id.n >= 2 && id.p[id.n - 2] == '/' && (id.p[id.n - 1] == '1' || id.p[id.n - 1] == '2')) id.n -= 2;
+    rs->id_off.push_back(rs->id_chars.size());
+    rs->id_chars.insert(rs->id_chars.end(), id.p, id.p + id.n);
+    rs->id_chars.push_back('\0');
+  }
+};
+
+// strip_adapter: returns the number of bases to keep.
+size_t adapter_keep(const uint8_t* seq, size_t rl, const std::string& ad) {
+  const size_t mo = std::min(rl, ad.size());
+  if (mo < 6) return rl;
+  for (size_t ov = mo; ov >= 6; ov--) {
+    size_t mm = 0;
+    for (size_t t = 0; t < ov; t++) mm += upper(seq[rl - ov + t]) != upper((uint8_t)ad[t]) ? 1 : 0;
+    if (mm <= ov / 10) return rl - ov;
+  }
+  return rl;
+}
+
+// Appends one read: bases upper-cased, the quality track cut or padded to the
+// (possibly adapter-trimmed) sequence length.
+void push_read(pbw_read_set* rs, const std::vector<uint8_t>& seq, const std::vector<uint8_t>& qual, const char* adapter) {
+  size_t keep = seq.size();
+  if (adapter) keep = adapter_keep(seq.data(), seq.size(), adapter);
+  for (size_t t = 0; t < keep; t++) {
+    rs->bases.push_back(upper(seq[t]));
+    rs->quals.push_back(t < qual.size() ? qual[t] : (uint8_t)30);
+  }
+  rs->offsets.push_back(rs->bases.size());
+}
+
+bool read_file(const char* path, std::vector<char>& buf) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return false;
+  char tmp[1 << 16];
+  size_t n;
+  while ((n = fread(tmp, 1, sizeof(tmp), f)) > 0) buf.insert(buf.end(), tmp, tmp + n);
+  fclose(f);
+  return true;
+}
+
+}  // namespace
+
+namespace pbw {
+void set_handleless_error(const std::string& s);
+}
+
+extern "C" {
+
+int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const char* adapter, pbw_read_set** out) {
+  if (!path || !out) return PBW_ERR_ARG;
+  *out = nullptr;
+  std::vector<char> buf;
+  if (!read_file(path, buf)) {
+    pbw::set_handleless_error(std::string("cannot open ") + path);
+    return PBW_ERR_IO;
+  }
+  pbw_read_set* rs = new pbw_read_set();
+  Builder bld{rs};
+  Lines L{buf.data(), buf.data() + buf.size()};
+  Span line;
+  std::vector<uint8_t> seq, qual;
+  if (!fasta) {
+    while (L.next(line)) {
+      bld.add(first_token(strip_leading(line, '@')));
+      seq.clear();
+      qual.clear();
+      while (L.next(line)) {
+        const Span t = trim(line);
+        if (t.n && t.p[0] == '+') break;
+        seq.insert(seq.end(), (const uint8_t*)t.p, (const uint8_t*)t.p + t.n);
+      }
+      while (L.next(line)) {
+        const Span t = trim(line);
+        for (size_t k = 0; k < t.n; k++) {
+          const uint8_t c = (uint8_t)t.p[k];
+          qual.push_back(c > quality_offset ? (uint8_t)(c - quality_offset) : (uint8_t)0);
+        }
+        if (qual.size() >= seq.size()) break;
+      }
+      push_read(rs, seq, qual, adapter);
+    }
+  } else {
+    bool have = false;
+    Span header{nullptr, 0};
+    while (true) {
+      if (!have) {
+        bool found = false;
+        while (L.next(line))
+          if (line.n && line.p[0] == '>') { found = true; break; }
+        if (!found) break;
+        header = line;
+      }
+      have = false;
+      bld.add(first_token(strip_leading(header, '>')));
+      seq.clear();
+      while (L.next(line)) {
+        const Span t = trim(line);
+        if (t.n && t.p[0] == '>') {
+          header = line;
+          have = true;
+          break;
+        }
+        seq.insert(seq.end(), (const uint8_t*)t.p, (const uint8_t*)t.p + t.n);
+      }
+      qual.assign(seq.size(), 40);
+      push_read(rs, seq, qual, adapter);
+      if (!have) break;
+    }
+  }
+  *out = rs;
+  return PBW_OK;
+}
+
+int pbw_reads_get(const pbw_read_set* rs, pbw_reads* view) {
+  if (!rs || !view) return PBW_ERR_ARG;
+  view->n = rs->offsets.size() - 1;
+  view->bases = rs->bases.data();
+  view->quals = rs->quals.data();
+  view->offsets = rs->offsets.data();
+  return PBW_OK;
+}
+
+const char* pbw_reads_id(const pbw_read_set* rs, uint64_t i) {
+  if (!rs || i >= rs->id_off.size()) return nullptr;
+  return rs->id_chars.data() + rs->id_off[i];
+}
+
+void pbw_reads_free(pbw_read_set* rs) { delete rs; }
+
+}  // extern "C"

@@ -1,0 +1,104 @@
+"""pbw_reads_load (the FASTQ / FASTA reads loader behind the C ABI) against
+the oracle's parser (src/io/fastx.rs) on the same files: bases, Phred scores,
+offsets and IDs byte for byte. Host-only: no device is touched."""
+import numpy as np
+import pytest
+
+FILES = {
+    "plain.fq": (False, "@r1 desc\nACGTACGT\n+\nIIIIIIII\n@r2\nacgtnNNa\n+r2\n!!!!####\n"),
+    "multiline.fq": (False, "@m1/1\nACGT\nTTGG\n+\nIIII\nJJJJ\n@m2/2\nGG\nCC\n+\n####\n"),
+    "crlf.fq": (False, "@c1\r\nACGT\r\n+\r\nIIII\r\n@c2 x y\r\nTTTT\r\n+\r\nABCD\r\n"),
+    "empty_seq.fq": (False, "@empty\n\n+\n\n@normal\nACGT\n+\nIIII\n"),
+    "short_qual.fq": (False, "@s1\nACGTACGT\n+\nIII\n@s2\nAC\n+\nIIIIII\n"),
+    "at_header.fq": (False, "@@doubled/2\nACGTA\n+\nIIIII\n@ \nAAAA\n+\nIIII\n"),
+    "ws.fq": (False, "@w1\n  ACGT \t\n+  \n IIII\n@w2\tname\nGGGG\n+\nIII\nI\n"),
+    "no_final_nl.fq": (False, "@n1\nACGT\n+\nIIII\n@n2\nTTTT\n+\nIIII"),
+    "plain.fa": (True, ">r1 desc\nACGT\nACGT\n>r2\nttgg\n>r3/1\n\n>r4\nNNNN\n"),
+    "leading_text.fa": (True, "junk line\n\n>a\nAC GT\n>>b\nGG\r\nCC\r\n"),
+    "empty.fa": (True, ""),
+    "header_only.fa": (True, ">x\n"),
+    "empty.fq": (False, ""),
+}
+
+ADAPTER = "AGATCGGAAGAGC"
+
+
+def _adapter_file(tmp_path):
+    recs = [
+        ("full", "ACGTTGCAACGTTGCA" + ADAPTER),
+        ("partial", "GGGGCCCCAAAATTTT" + ADAPTER[:7]),
+        ("onemm", "TTTTGGGGCCCC" + "AGATCGTAAGAGC"),
+        ("lower", "ACACACACAC" + ADAPTER.lower()[:9]),
+        ("short5", "ACGTACGTAC" + ADAPTER[:5]),
+        ("none", "ACGTACGTACGTACGT"),
+        ("tiny", "AGATC"),
+    ]
+    text = "".join(f"@{n}\n{s}\n+\n{'I' * len(s)}\n" for n, s in recs)
+    p = tmp_path / "adapt.fq"
+    p.write_text(text)
+    return p
+
+
+def _same(a, b):
+    assert a.ids == b.ids
+    assert np.array_equal(a.offsets, b.offsets)
+    tot = int(a.offsets[-1])
+    assert np.array_equal(a.bases[:tot], b.bases[:tot])
+    assert np.array_equal(a.quals[:tot], b.quals[:tot])
+
+
+@pytest.mark.parametrize("name", sorted(FILES))
+@pytest.mark.parametrize("qoff", [33, 64])
+def test_loader_matches_oracle(oracle, tmp_path, name, qoff):
+    import probebwa_gb300 as P
+    P.build()
+    fasta, text = FILES[name]
+    p = tmp_path / name
+    p.write_bytes(text.encode())
+    got = P.load_reads(str(p), fasta=fasta, quality_offset=qoff)
+    want = oracle.parse_reads(str(p), fasta=fasta, quality_offset=qoff)
+    _same(got, want)
+
+
+def test_loader_adapter_matches_oracle(oracle, tmp_path):
+    import probebwa_gb300 as P
+    P.build()
+    p = _adapter_file(tmp_path)
+    got = P.load_reads(str(p), adapter=ADAPTER)
+    want = oracle.parse_reads(str(p), adapter=ADAPTER)
+    _same(got, want)
+    lens = np.diff(got.offsets).tolist()
+    # full adapter, 7-base tail, one mismatch in 13, lower case cut; 5 bases and no adapter kept
+    assert lens[:4] == [16, 16, 12, 10]
+    assert lens[4] == 15 and lens[5] == 16
+    assert lens[6] == 5  # shorter than the 6-base minimum overlap
+
+
+def test_loader_random_fastq_matches_oracle(oracle, tmp_path):
+    import probebwa_gb300 as P
+    P.build()
+    rng = np.random.default_rng(7)
+    lines = []
+    for i in range(400):
+        n = int(rng.integers(0, 300))
+        seq = "".join(rng.choice(list("ACGTNacgtn"), n))
+        ql = n + int(rng.integers(-3, 3)) if n > 3 else n
+        qual = "".join(chr(int(c)) for c in rng.integers(33, 75, max(ql, 0)))
+        sfx = ["", "/1", "/2", " extra"][i % 4]
+        if n > 80 and i % 3 == 0:
+            seq = seq[:40] + "\n" + seq[40:]
+            qual = qual[:50] + "\n" + qual[50:]
+        lines.append(f"@read{i}{sfx}\n{seq}\n+\n{qual}\n")
+    p = tmp_path / "rand.fq"
+    p.write_text("".join(lines))
+    for adapter in (None, ADAPTER):
+        got = P.load_reads(str(p), adapter=adapter)
+        want = oracle.parse_reads(str(p), adapter=adapter)
+        _same(got, want)
+
+
+def test_loader_missing_file_raises(tmp_path):
+    import probebwa_gb300 as P
+    P.build()
+    with pytest.raises(P.PbwError):
+        P.load_reads(str(tmp_path / "absent.fq"))
