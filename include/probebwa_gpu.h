@@ -216,8 +216,11 @@ int pbw_write_sam(pbw_handle* h, const char* path, const char* command_line, con
  * adapter is not NULL, strip_adapter (:97-117). quality_offset is 33 or 64
  * (--phred64). pbw_reads_get gives the reads as pbw_reads (the quality track
  * has the sequence's length: missing scores are 30); pbw_reads_id the i-th
- * read ID (NUL-terminated, valid until pbw_reads_free). Errors:
- * PBW_ERR_IO (pbw_last_error(NULL) names the file). Gzip input is not read. */
+ * read ID (NUL-terminated, valid until pbw_reads_free). A path ending in
+ * ".gz" is gunzipped first (open_maybe_gz, :120-129; zlib is opened at run
+ * time as libz.so.1). Errors: PBW_ERR_IO (cannot open, corrupt gzip) and
+ * PBW_ERR_FORMAT (text that is not UTF-8); pbw_last_error(NULL) names the
+ * file. */
 typedef struct pbw_read_set pbw_read_set;
 int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const char* adapter, pbw_read_set** out);
 int pbw_reads_get(const pbw_read_set* rs, pbw_reads* view);

@@ -226,19 +226,66 @@ struct Genome {
 // Minimal FASTA reader (src/index/genome.rs:150-213): headers carried over
 // between records, id = first whitespace token after the leading '>'s,
 // sequence lines trimmed and concatenated.
-static bool is_ws(u8 c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
+// Whitespace is Unicode White_Space, as str::trim / split_whitespace: ASCII
+// 9-13 and 32, and U+0085 U+00A0 U+1680 U+2000-200A U+2028 U+2029 U+202F
+// U+205F U+3000 in UTF-8. ws_head / ws_tail give the byte length of such a
+// character starting at s[i] / ending at s[e-1] (0: none).
+static size_t ws_head(const std::string& s, size_t i) {
+  const u8 c = (u8)s[i];
+  if (c == ' ' || (c >= 9 && c <= 13)) return 1;
+  const size_t left = s.size() - i;
+  if (left >= 2 && c == 0xC2 && ((u8)s[i + 1] == 0x85 || (u8)s[i + 1] == 0xA0)) return 2;
+  if (left >= 3) {
+    const uint32_t cp = ((uint32_t)c << 16) | ((uint32_t)(u8)s[i + 1] << 8) | (u8)s[i + 2];
+    if (cp == 0xE19A80 || cp == 0xE38080 || cp == 0xE2819F) return 3;
+    if (cp >= 0xE28080 && cp <= 0xE2808A) return 3;
+    if (cp == 0xE280A8 || cp == 0xE280A9 || cp == 0xE280AF) return 3;
+  }
+  return 0;
+}
+static size_t ws_tail(const std::string& s, size_t a, size_t e) {
+  for (size_t k = 1; k <= 3 && k <= e - a; k++)
+    if (ws_head(s, e - k) == k && (k == 1 || (u8)s[e - k] >= 0xC0)) return k;
+  return 0;
+}
 static std::string trim(const std::string& s) {
-  size_t a = 0, b = s.size();
-  while (a < b && is_ws((u8)s[a])) a++;
-  while (b > a && is_ws((u8)s[b - 1])) b--;
+  size_t a = 0, b = s.size(), k;
+  while (a < b && (k = ws_head(s, a)) > 0) a += k;
+  while (b > a && (k = ws_tail(s, a, b)) > 0) b -= k;
   return s.substr(a, b - a);
 }
 static std::string first_token(const std::string& s) {
-  size_t a = 0;
-  while (a < s.size() && is_ws((u8)s[a])) a++;
+  size_t a = 0, k;
+  while (a < s.size() && (k = ws_head(s, a)) > 0) a += k;
   size_t b = a;
-  while (b < s.size() && !is_ws((u8)s[b])) b++;
+  while (b < s.size() && ws_head(s, b) == 0) b++;
   return s.substr(a, b - a);
+}
+// str::from_utf8 acceptance (read_line into a String rejects anything else).
+static bool utf8_ok(const std::string& s) {
+  size_t i = 0;
+  const size_t n = s.size();
+  while (i < n) {
+    const u8 c = (u8)s[i];
+    size_t need = 0;
+    u8 lo = 0x80, hi = 0xBF;
+    if (c < 0x80) { i++; continue; }
+    if (c >= 0xC2 && c <= 0xDF) need = 1;
+    else if (c == 0xE0) { need = 2; lo = 0xA0; }
+    else if ((c >= 0xE1 && c <= 0xEC) || c == 0xEE || c == 0xEF) need = 2;
+    else if (c == 0xED) { need = 2; hi = 0x9F; }
+    else if (c == 0xF0) { need = 3; lo = 0x90; }
+    else if (c >= 0xF1 && c <= 0xF3) need = 3;
+    else if (c == 0xF4) { need = 3; hi = 0x8F; }
+    else return false;
+    for (size_t j = 1; j <= need; j++) {
+      if (i + j >= n) return false;
+      const u8 cc = (u8)s[i + j];
+      if (cc < (j == 1 ? lo : 0x80) || cc > (j == 1 ? hi : 0xBF)) return false;
+    }
+    i += need + 1;
+  }
+  return true;
 }
 static std::string trim_start_char(const std::string& s, char c) {
   size_t a = 0;
@@ -250,7 +297,8 @@ struct LineReader {
   FILE* f = nullptr;
   explicit LineReader(const std::string& path) { f = fopen(path.c_str(), "rb"); }
   ~LineReader() { if (f) fclose(f); }
-  // Returns false at EOF (0 bytes read). The line keeps its '\n'.
+  // Returns false at EOF (0 bytes read). The line keeps its '\n'. A line
+  // that is not UTF-8 throws, as BufRead::read_line into a String fails.
   bool read_line(std::string& line) {
     line.clear();
     int ch;
@@ -260,6 +308,7 @@ struct LineReader {
       line.push_back((char)ch);
       if (ch == '\n') break;
     }
+    if (any && !utf8_ok(line)) throw std::runtime_error("stream did not contain valid UTF-8");
     return any;
   }
 };

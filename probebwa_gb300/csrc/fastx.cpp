@@ -1,31 +1,37 @@
 // fastx.cpp -- the input side of the mapping path: FASTQ / FASTA reads into
 // the structure-of-arrays layout the map calls take (src/io/fastx.rs).
 //
-// The file is read into memory once and split into lines with memchr; each
-// record is decoded straight into the concatenated base, quality and offset
-// arrays. Semantics follow the reference's parsers:
+// The file is read into memory once (gunzipped when its name ends in ".gz",
+// as open_maybe_gz, fastx.rs:120-129, with every gzip member decoded in turn
+// like flate2's MultiGzDecoder) and split into lines with memchr; each record
+// is decoded straight into the concatenated base, quality and offset arrays.
+// Semantics follow the reference's parsers:
+//  * the text must be UTF-8 (each line goes through BufRead::read_line into
+//    a String); anything else is an error, as there;
 //  * FASTQ (FastqParser, fastx.rs:226-305): ID = first whitespace-separated
 //    token of the header line after leading '@'s; sequence lines (trimmed)
 //    until a trimmed line starting with '+'; then quality lines (trimmed) until
 //    they cover the sequence, at least one line. Bases are upper-cased
 //    (DnaSeq::from_ascii, types.rs:12-15), qualities are the byte minus the
-//    offset, saturating at 0 (QualityScores::from_phred_ascii, types.rs:57-60).
+//    offset, saturating at 0 (QualityScores::from_phred_ascii, types.rs:57-60);
 //  * FASTA reads (FastaAsReadsParser, fastx.rs:161-224): records start at a
 //    line beginning with '>' (lines before the first are skipped); ID = first
 //    token after leading '>'s; sequence = concatenated trimmed lines up to a
-//    trimmed line starting with '>'; every quality 40 (fastx.rs:159).
+//    trimmed line starting with '>'; every quality 40 (fastx.rs:159);
 //  * then per read: a trailing "/1" or "/2" is dropped from the ID
 //    (strip_mate_suffix, fastx.rs:77-81) and, with an adapter, the longest
 //    3' overlap of at least 6 bases with at most one mismatch per 10 bases
 //    (case-insensitive) is cut from the bases and qualities (strip_adapter,
 //    fastx.rs:97-117).
-// Whitespace is the ASCII set of Rust's str::trim for ASCII text (space, tab,
-// LF, VT, FF, CR). The quality track handed to the map calls has the
-// sequence's length: missing scores read as 30, extra ones are dropped.
-// Gzip input (flate2 in the reference) is not read.
+// Whitespace (str::trim, str::split_whitespace) is Unicode White_Space: the
+// ASCII tab, LF, VT, FF, CR and space, and U+0085, U+00A0, U+1680,
+// U+2000-U+200A, U+2028, U+2029, U+202F, U+205F, U+3000 in their UTF-8
+// forms. The quality track handed to the map calls has the sequence's
+// length: missing scores read as 30, extra ones are dropped.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <dlfcn.h>
 #include <string>
 #include <vector>
 
@@ -41,24 +47,76 @@ struct pbw_read_set {
 
 namespace {
 
-inline bool is_ws(uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
 inline uint8_t upper(uint8_t b) { return (b >= 'a' && b <= 'z') ? (uint8_t)(b - 32) : b; }
 
 struct Span {
   const char* p;
   size_t n;
 };
+
+// Byte length of the White_Space character starting at p[0] (0: none).
+inline size_t ws_head(const char* p, size_t n) {
+  const uint8_t c = (uint8_t)p[0];
+  if (c == ' ' || (c >= 9 && c <= 13)) return 1;
+  if (n >= 2 && c == 0xC2 && ((uint8_t)p[1] == 0x85 || (uint8_t)p[1] == 0xA0)) return 2;
+  if (n >= 3 && c >= 0xE1 && c <= 0xE3) {
+    const uint8_t b = (uint8_t)p[1], d = (uint8_t)p[2];
+    if (c == 0xE1) return (b == 0x9A && d == 0x80) ? 3 : 0;  // U+1680
+    if (c == 0xE3) return (b == 0x80 && d == 0x80) ? 3 : 0;  // U+3000
+    if (b == 0x80 && (d <= 0x8A || d == 0xA8 || d == 0xA9 || d == 0xAF) && d >= 0x80) return 3;
+    if (b == 0x81 && d == 0x9F) return 3;  // U+205F
+  }
+  return 0;
+}
+// Byte length of the White_Space character ending at p[n-1] (0: none). In
+// valid UTF-8 a 2- or 3-byte match at the end is a whole character.
+inline size_t ws_tail(const char* p, size_t n) {
+  if (n == 0) return 0;
+  const uint8_t c = (uint8_t)p[n - 1];
+  if (c < 0x80) return (c == ' ' || (c >= 9 && c <= 13)) ? 1 : 0;
+  if (n >= 2 && ws_head(p + n - 2, 2) == 2) return 2;
+  if (n >= 3 && ws_head(p + n - 3, 3) == 3) return 3;
+  return 0;
+}
 Span trim(Span s) {
-  while (s.n && is_ws((uint8_t)s.p[0])) { s.p++; s.n--; }
-  while (s.n && is_ws((uint8_t)s.p[s.n - 1])) s.n--;
+  size_t k;
+  while (s.n && (k = ws_head(s.p, s.n)) > 0) { s.p += k; s.n -= k; }
+  while (s.n && (k = ws_tail(s.p, s.n)) > 0) s.n -= k;
   return s;
 }
+// The first split_whitespace token (empty when the span is all whitespace).
 Span first_token(Span s) {
-  size_t a = 0;
-  while (a < s.n && is_ws((uint8_t)s.p[a])) a++;
+  size_t a = 0, k;
+  while (a < s.n && (k = ws_head(s.p + a, s.n - a)) > 0) a += k;
   size_t b = a;
-  while (b < s.n && !is_ws((uint8_t)s.p[b])) b++;
+  while (b < s.n && ws_head(s.p + b, s.n - b) == 0) b++;
   return Span{s.p + a, b - a};
+}
+// std::str::from_utf8 acceptance: well-formed UTF-8 (no overlong forms,
+// surrogates or code points above U+10FFFF).
+bool valid_utf8(const char* s, size_t n) {
+  size_t i = 0;
+  while (i < n) {
+    const uint8_t c = (uint8_t)s[i];
+    if (c < 0x80) { i++; continue; }
+    size_t need;
+    uint8_t lo = 0x80, hi = 0xBF;
+    if (c >= 0xC2 && c <= 0xDF) need = 1;
+    else if (c == 0xE0) { need = 2; lo = 0xA0; }
+    else if ((c >= 0xE1 && c <= 0xEC) || c == 0xEE || c == 0xEF) need = 2;
+    else if (c == 0xED) { need = 2; hi = 0x9F; }
+    else if (c == 0xF0) { need = 3; lo = 0x90; }
+    else if (c >= 0xF1 && c <= 0xF3) need = 3;
+    else if (c == 0xF4) { need = 3; hi = 0x8F; }
+    else return false;
+    for (size_t j = 1; j <= need; j++) {
+      if (i + j >= n) return false;
+      const uint8_t cc = (uint8_t)s[i + j];
+      if (cc < (j == 1 ? lo : 0x80) || cc > (j == 1 ? hi : 0xBF)) return false;
+    }
+    i += need + 1;
+  }
+  return true;
 }
 Span strip_leading(Span s, char c) {
   while (s.n && s.p[0] == c) { s.p++; s.n--; }
@@ -124,6 +182,98 @@ bool read_file(const char* path, std::vector<char>& buf) {
   return true;
 }
 
+// zlib's stream state (the z_stream of its public API, LP64 layout); the
+// library is opened at run time so the build needs no zlib headers.
+struct ZStream {
+  const unsigned char* next_in;
+  unsigned avail_in;
+  unsigned long total_in;
+  unsigned char* next_out;
+  unsigned avail_out;
+  unsigned long total_out;
+  const char* msg;
+  void* state;
+  void* zalloc;
+  void* zfree;
+  void* opaque;
+  int data_type;
+  unsigned long adler;
+  unsigned long reserved;
+};
+
+// Decodes every gzip member of in (MultiGzDecoder); false with a message on
+// a missing zlib or corrupt data.
+bool gunzip(const std::vector<char>& in, std::vector<char>& out, std::string& err) {
+  static void* lib = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
+  if (!lib) {
+    err = "gzip input needs libz.so.1";
+    return false;
+  }
+  using VersionFn = const char* (*)();
+  using InitFn = int (*)(ZStream*, int, const char*, int);
+  using StepFn = int (*)(ZStream*, int);
+  using EndFn = int (*)(ZStream*);
+  auto version = (VersionFn)dlsym(lib, "zlibVersion");
+  auto init = (InitFn)dlsym(lib, "inflateInit2_");
+  auto step = (StepFn)dlsym(lib, "inflate");
+  auto reset = (EndFn)dlsym(lib, "inflateReset");
+  auto end = (EndFn)dlsym(lib, "inflateEnd");
+  if (!version || !init || !step || !reset || !end) {
+    err = "libz.so.1 lacks the inflate entry points";
+    return false;
+  }
+  if (in.empty()) return true;
+  ZStream z;
+  memset(&z, 0, sizeof(z));
+  if (init(&z, 15 + 16, version(), (int)sizeof(ZStream)) != 0) {
+    err = "inflateInit2 failed";
+    return false;
+  }
+  z.next_in = (const unsigned char*)in.data();
+  z.avail_in = 0;
+  size_t fed = 0;
+  std::vector<char> chunk(1 << 20);
+  bool ok = true;
+  while (true) {
+    if (z.avail_in == 0 && fed < in.size()) {
+      const size_t give = std::min<size_t>(in.size() - fed, 1u << 30);
+      z.next_in = (const unsigned char*)in.data() + fed;
+      z.avail_in = (unsigned)give;
+      fed += give;
+    }
+    z.next_out = (unsigned char*)chunk.data();
+    z.avail_out = (unsigned)chunk.size();
+    const int rc = step(&z, 0);
+    out.insert(out.end(), chunk.data(), chunk.data() + (chunk.size() - z.avail_out));
+    if (rc == 1) {  // Z_STREAM_END: a member ended; decode the next one if bytes remain
+      if (z.avail_in == 0 && fed == in.size()) break;
+      reset(&z);
+      continue;
+    }
+    if (rc == -5 && z.avail_in == 0 && fed == in.size()) {  // Z_BUF_ERROR at end: truncated stream
+      ok = false;
+      err = "corrupt deflate stream";
+      break;
+    }
+    if (rc != 0 && rc != -5) {
+      ok = false;
+      err = z.msg ? z.msg : "corrupt deflate stream";
+      break;
+    }
+  }
+  end(&z);
+  return ok;
+}
+
+bool ends_with_gz(const char* path) {
+  const size_t n = strlen(path);
+  // Path::extension() == "gz": the file name ends in ".gz" and is not ".gz" itself
+  if (n < 3 || strcmp(path + n - 3, ".gz") != 0) return false;
+  const char* base = strrchr(path, '/');
+  base = base ? base + 1 : path;
+  return strlen(base) > 3;
+}
+
 }  // namespace
 
 namespace pbw {
@@ -139,6 +289,19 @@ int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const ch
   if (!read_file(path, buf)) {
     pbw::set_handleless_error(std::string("cannot open ") + path);
     return PBW_ERR_IO;
+  }
+  if (ends_with_gz(path)) {
+    std::vector<char> raw;
+    raw.swap(buf);
+    std::string err;
+    if (!gunzip(raw, buf, err)) {
+      pbw::set_handleless_error(std::string(path) + ": " + err);
+      return PBW_ERR_IO;
+    }
+  }
+  if (!valid_utf8(buf.data(), buf.size())) {
+    pbw::set_handleless_error(std::string(path) + ": stream did not contain valid UTF-8");
+    return PBW_ERR_FORMAT;
   }
   pbw_read_set* rs = new pbw_read_set();
   Builder bld{rs};

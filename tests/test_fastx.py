@@ -18,6 +18,9 @@ FILES = {
     "empty.fa": (True, ""),
     "header_only.fa": (True, ">x\n"),
     "empty.fq": (False, ""),
+    "unicode_ws.fq": (False, "@u1\u00a0desc\nAC\u2003GT\u3000\n+\u0085\nIIII\n@\u2000u2 x\nGGCC\u00a0\n+\nIIII\n"),
+    "unicode_qual.fq": (False, "@q1\nACGT\n+\nI\u00e9I\n@q2\nAC\n+\nII\n"),
+    "unicode_ws.fa": (True, ">a\u205fb\nAC\u1680\n\u202f>b\nGG\n"),
 }
 
 ADAPTER = "AGATCGGAAGAGC"
@@ -102,3 +105,36 @@ def test_loader_missing_file_raises(tmp_path):
     P.build()
     with pytest.raises(P.PbwError):
         P.load_reads(str(tmp_path / "absent.fq"))
+
+
+@pytest.mark.parametrize("fasta", [False, True])
+def test_loader_rejects_non_utf8_like_oracle(oracle, tmp_path, fasta):
+    import probebwa_gb300 as P
+    P.build()
+    p = tmp_path / "bad.txt"
+    body = b">r1\nAC\xffGT\n" if fasta else b"@r1\nACGT\n+\nII\xc3I\n"
+    p.write_bytes(body)
+    with pytest.raises(RuntimeError):
+        oracle.parse_reads(str(p), fasta=fasta)
+    with pytest.raises(P.PbwError):
+        P.load_reads(str(p), fasta=fasta)
+
+
+def test_loader_reads_gzip_members(oracle, tmp_path):
+    """A .gz path is gunzipped (all members, as MultiGzDecoder) before parsing;
+    the oracle parses the same text uncompressed."""
+    import gzip
+    import probebwa_gb300 as P
+    P.build()
+    text = "".join(f"@g{i}/1\n{'ACGT' * (i % 7 + 1)}\n+\n{'I' * (4 * (i % 7 + 1))}\n" for i in range(300))
+    half = len(text) // 2
+    cut = text.index("@", half)
+    plain = tmp_path / "g.fq"
+    plain.write_text(text)
+    gz = tmp_path / "g.fq.gz"
+    gz.write_bytes(gzip.compress(text[:cut].encode()) + gzip.compress(text[cut:].encode()))
+    _same(P.load_reads(str(gz)), oracle.parse_reads(str(plain)))
+    corrupt = tmp_path / "c.fq.gz"
+    corrupt.write_bytes(gzip.compress(text.encode())[:-20])
+    with pytest.raises(P.PbwError):
+        P.load_reads(str(corrupt))
