@@ -206,9 +206,51 @@ int pbw_map_single_device(pbw_handle* h, const pbw_reads* dev_reads, pbw_records
 
 /* SAM text (src/io/sam.rs:69-108, format_sam :37-58) for records produced by
  * a map call: header (@HD, @SQ per contig, @PG with command_line) then one
- * line per record. read_ids[i] is the QNAME. Writes to path. */
+ * line per record. read_ids[i] is the QNAME. Writes to path. Same as
+ * pbw_sam_write with one source, no read group, unsorted. */
 int pbw_write_sam(pbw_handle* h, const char* path, const char* command_line, const pbw_reads* reads,
                   const char* const* read_ids, const pbw_records* recs);
+
+/* Header settings of a SAM stream (format_sam_records_sorted, sam.rs:83-108). */
+typedef struct {
+  const char* command_line;  /* @PG CL: (main.rs:154, argv joined by ' ') */
+  const char* read_group;    /* --readgroup "ID:id,TAG:value,..." (ReadGroup::parse,
+                                sam.rs:17-32) or NULL: adds the @RG line and an
+                                RG:Z:<id> tag on every record */
+  int32_t coordinate_sorted; /* @HD SO:coordinate instead of SO:unsorted */
+} pbw_sam_options;
+
+/* Records of one map call with the reads they came from. */
+typedef struct {
+  const pbw_reads* reads;       /* SEQ / QUAL: the input reads, one per record */
+  const char* const* read_ids;  /* QNAME per record */
+  const pbw_records* recs;
+} pbw_sam_source;
+
+/* Selected records as SAM text, formatted on the device. n_src is 1 (single-
+ * end) or 2 (pairs: source 0 = mate 1, source 1 = mate 2, the output order of
+ * map_paired, lib.rs:171-181). Records are numbered r * n_src + s (record r of
+ * source s): sel lists the records to write, in output order (the records
+ * kept by --labelfilter, main.rs:158-160, or a pbw_sort_coordinate order);
+ * sel == NULL writes every record in number order. pbw_sam_write writes the
+ * stream to path ("-" = standard output). pbw_sam_format puts it in out
+ * (capacity cap bytes) and sets *len to its length; with out == NULL it only
+ * sets *len. Errors: PBW_ERR_ARG (bad read-group spec, mismatched sources,
+ * a selection entry naming no record), PBW_ERR_CAPACITY (cap < *len),
+ * PBW_ERR_IO. */
+int pbw_sam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
+                  const uint64_t* sel, uint64_t n_sel, const char* path);
+int pbw_sam_format(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
+                   const uint64_t* sel, uint64_t n_sel, char* out, uint64_t cap, uint64_t* len);
+
+/* Coordinate order of the selected records (sort_for_coordinate_order,
+ * sam.rs:114-124): stable sort by (index of the contig's name, the last
+ * index when names repeat; position), unmapped records (pos 0) last, on the
+ * device. sel / n_sel / numbering as pbw_sam_write (sel must not be NULL when
+ * n_sel > 0); sorted[n_sel] receives the record numbers in order. Only
+ * recs->contig and recs->pos of the sources are read. */
+int pbw_sort_coordinate(pbw_handle* h, uint32_t n_src, const pbw_sam_source* src, const uint64_t* sel,
+                        uint64_t n_sel, uint64_t* sorted);
 
 /* Reads from a file: replaces read_reads_files_with_preprocessing
  * (src/io/fastx.rs:19-48) for one path -- read_fastq (:133-147) or

@@ -2059,50 +2059,135 @@ int orc_mapq_batch(void* h, const orc_reads* reads, const uint64_t* lk_off, cons
   return 0;
 }
 
-int orc_write_sam(void* h, const char* path, const char* command_line, const orc_reads* reads,
-                  const char* const* read_ids, const orc_records* recs) {
-  Mapper* m = (Mapper*)h;
-  std::string out;
-  out += "@HD\tVN:1.6\tSO:unsorted\n";
+}  // extern "C"
+
+// One SAM line without its '\n' (format_sam, sam.rs:37-58). SEQ/QUAL in the
+// aligned orientation (reverse-complemented and reversed for a reverse-strand
+// mapped record); QUAL is the raw Phred scores as bytes (sam.rs:52).
+static void sam_line(std::string& out, const Mapper* m, const orc_reads* reads, const char* const* read_ids,
+                     const orc_records* recs, uint64_t i, const std::string* rg_id) {
+  out += read_ids[i];
+  out += "\t" + std::to_string(recs->flag[i]) + "\t";
+  int32_t c = recs->contig[i];
+  out += c >= 0 ? m->genome.contigs[c].name : std::string("*");
+  out += "\t" + std::to_string(recs->pos[i]) + "\t" + std::to_string((unsigned)recs->mapq[i]) + "\t";
+  std::string cs;
+  for (uint32_t k = recs->cigar_off[i]; k < recs->cigar_off[i + 1]; k++) {
+    uint32_t w = recs->cigar[k];
+    static const char OPS[] = "MIDXSH";
+    cs += std::to_string(w >> 4);
+    cs.push_back(OPS[w & 15]);
+  }
+  out += cs.empty() ? std::string("*") : cs;
+  out += "\t";
+  int32_t mc = recs->mate_contig[i];
+  out += mc >= 0 ? m->genome.contigs[mc].name : std::string("*");
+  out += "\t" + std::to_string(recs->mate_pos[i]) + "\t" + std::to_string(recs->tlen[i]) + "\t";
+  uint64_t a = reads->offsets[i], b = reads->offsets[i + 1];
+  std::vector<u8> seq(reads->bases + a, reads->bases + b), qual(reads->quals + a, reads->quals + b);
+  for (auto& x : seq) x = ascii_upper(x);
+  if (recs->pos[i] != 0 && (recs->flag[i] & 0x10)) {
+    seq = revcomp(seq);
+    std::reverse(qual.begin(), qual.end());
+  }
+  utf8_lossy_append(out, seq.data(), seq.size());
+  out += "\t";
+  utf8_lossy_append(out, qual.data(), qual.size());
+  if (rg_id) out += "\tRG:Z:" + *rg_id;
+}
+
+// ReadGroup::parse (sam.rs:17-32).
+static bool parse_read_group(const std::string& spec, std::string& id, std::string& header_line) {
+  std::vector<std::string> fields;
+  bool have = false;
+  size_t a = 0;
+  while (true) {
+    size_t e = spec.find(',', a);
+    std::string pair = spec.substr(a, e == std::string::npos ? std::string::npos : e - a);
+    size_t c = pair.find(':');
+    if (c == std::string::npos) { g_err = "--readgroup: expected TAG:VALUE, got '" + pair + "'"; return false; }
+    std::string tag = pair.substr(0, c), value = pair.substr(c + 1);
+    if (tag == "ID") { id = value; have = true; }
+    fields.push_back(tag + ":" + value);
+    if (e == std::string::npos) break;
+    a = e + 1;
+  }
+  if (!have) { g_err = "--readgroup must set at least an ID tag"; return false; }
+  header_line = "@RG";
+  for (auto& f : fields) header_line += "\t" + f;
+  return true;
+}
+
+// format_sam_records_sorted (sam.rs:83-108) over the records numbered
+// r * n_src + s (record r of source s) listed in sel.
+static bool sam_text(const Mapper* m, const char* command_line, const char* read_group, bool coordinate_sorted,
+                     uint32_t n_src, const orc_reads* const* reads, const char* const* const* ids,
+                     const orc_records* const* recs, const uint64_t* sel, uint64_t n_sel, std::string& out) {
+  std::string rg_id, rg_line;
+  if (read_group && !parse_read_group(read_group, rg_id, rg_line)) return false;
+  out += std::string("@HD\tVN:1.6\tSO:") + (coordinate_sorted ? "coordinate" : "unsorted") + "\n";
   for (auto& c : m->genome.contigs) out += "@SQ\tSN:" + c.name + "\tLN:" + std::to_string(c.length) + "\n";
   out += std::string("@PG\tID:probebwa\tPN:probebwa\tVN:0.1.0\tCL:") + command_line + "\n";
-  for (uint64_t i = 0; i < recs->n; i++) {
-    out += read_ids[i];
-    out += "\t" + std::to_string(recs->flag[i]) + "\t";
-    int32_t c = recs->contig[i];
-    out += c >= 0 ? m->genome.contigs[c].name : std::string("*");
-    out += "\t" + std::to_string(recs->pos[i]) + "\t" + std::to_string((unsigned)recs->mapq[i]) + "\t";
-    std::string cs;
-    for (uint32_t k = recs->cigar_off[i]; k < recs->cigar_off[i + 1]; k++) {
-      uint32_t w = recs->cigar[k];
-      static const char OPS[] = "MIDXSH";
-      cs += std::to_string(w >> 4);
-      cs.push_back(OPS[w & 15]);
-    }
-    out += cs.empty() ? std::string("*") : cs;
-    out += "\t";
-    int32_t mc = recs->mate_contig[i];
-    out += mc >= 0 ? m->genome.contigs[mc].name : std::string("*");
-    out += "\t" + std::to_string(recs->mate_pos[i]) + "\t" + std::to_string(recs->tlen[i]) + "\t";
-    // SEQ/QUAL in the aligned orientation (reverse-complemented and reversed
-    // for a reverse-strand mapped record); QUAL is the raw Phred scores as
-    // bytes (sam.rs:52).
-    uint64_t a = reads->offsets[i], b = reads->offsets[i + 1];
-    std::vector<u8> seq(reads->bases + a, reads->bases + b), qual(reads->quals + a, reads->quals + b);
-    for (auto& x : seq) x = ascii_upper(x);
-    if (recs->pos[i] != 0 && (recs->flag[i] & 0x10)) {
-      seq = revcomp(seq);
-      std::reverse(qual.begin(), qual.end());
-    }
-    utf8_lossy_append(out, seq.data(), seq.size());
-    out += "\t";
-    utf8_lossy_append(out, qual.data(), qual.size());
+  if (read_group) out += rg_line + "\n";
+  for (uint64_t k = 0; k < n_sel; k++) {
+    const uint32_t s = (uint32_t)(sel[k] % n_src);
+    const uint64_t r = sel[k] / n_src;
+    sam_line(out, m, reads[s], ids[s], recs[s], r, read_group ? &rg_id : nullptr);
     out += "\n";
   }
-  FILE* f = fopen(path, "wb");
-  if (!f) { g_err = "cannot write sam"; return -1; }
-  fwrite(out.data(), 1, out.size(), f);
-  fclose(f);
+  return true;
+}
+
+// sort_for_coordinate_order (sam.rs:114-124): stable, by (HashMap name ->
+// contig index, built in contig order so a repeated name keeps its last
+// index; position), unmapped (position 0) last.
+static void sort_coordinate(const Mapper* m, uint32_t n_src, const orc_records* const* recs, std::vector<uint64_t>& sel) {
+  std::unordered_map<std::string, size_t> index;
+  for (size_t i = 0; i < m->genome.contigs.size(); i++) index[m->genome.contigs[i].name] = i;
+  auto key = [&](uint64_t g) {
+    const orc_records* R = recs[g % n_src];
+    const uint64_t r = g / n_src;
+    if (R->pos[r] == 0) return std::make_pair(SIZE_MAX, SIZE_MAX);
+    size_t ci = SIZE_MAX;
+    if (R->contig[r] >= 0) {
+      auto it = index.find(m->genome.contigs[R->contig[r]].name);
+      if (it != index.end()) ci = it->second;
+    }
+    return std::make_pair(ci, (size_t)R->pos[r]);
+  };
+  std::stable_sort(sel.begin(), sel.end(), [&](uint64_t x, uint64_t y) { return key(x) < key(y); });
+}
+
+extern "C" {
+
+int orc_write_sam(void* h, const char* path, const char* command_line, const orc_reads* reads,
+                  const char* const* read_ids, const orc_records* recs) {
+  std::vector<uint64_t> sel(recs->n);
+  for (uint64_t i = 0; i < recs->n; i++) sel[i] = i;
+  return orc_sam_write(h, command_line, nullptr, 0, 1, &reads, &read_ids, &recs, sel.data(), sel.size(), path);
+}
+
+int orc_sam_write(void* h, const char* command_line, const char* read_group, int coordinate_sorted, uint32_t n_src,
+                  const orc_reads* const* reads, const char* const* const* ids, const orc_records* const* recs,
+                  const uint64_t* sel, uint64_t n_sel, const char* path) {
+  std::string out;
+  if (!sam_text((Mapper*)h, command_line, read_group, coordinate_sorted != 0, n_src, reads, ids, recs, sel, n_sel,
+                out))
+    return -1;
+  FILE* f = strcmp(path, "-") == 0 ? stdout : fopen(path, "wb");
+  if (!f) { g_err = std::string("cannot write ") + path; return -1; }
+  bool ok = fwrite(out.data(), 1, out.size(), f) == out.size();
+  if (f == stdout) ok = fflush(f) == 0 && ok;
+  else ok = fclose(f) == 0 && ok;
+  if (!ok) { g_err = std::string("short write to ") + path; return -1; }
+  return 0;
+}
+
+int orc_sort_coordinate(void* h, uint32_t n_src, const orc_records* const* recs, const uint64_t* sel, uint64_t n_sel,
+                        uint64_t* out) {
+  std::vector<uint64_t> v(sel, sel + n_sel);
+  sort_coordinate((Mapper*)h, n_src, recs, v);
+  std::copy(v.begin(), v.end(), out);
   return 0;
 }
 
@@ -2144,3 +2229,319 @@ const char* orc_reads_id(void* rh, uint64_t i) { return ((ReadSet*)rh)->reads[i]
 void orc_reads_free(void* rh) { delete (ReadSet*)rh; }
 
 }  // extern "C"
+
+// ===========================================================================
+// The `probebwa` command line (src/main.rs), restated over this oracle.
+// ===========================================================================
+namespace {
+
+struct UsageError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+// One option of the clap grammar of main.rs:31-111.
+struct OptSpec {
+  const char* long_name;
+  char short_name;
+  bool takes_value;
+};
+
+// clap-style parse: "--name value", "--name=value", "-x value", "-xvalue",
+// "-x=value"; flags take no value; a value may not start with '-' (clap's
+// default without allow_hyphen_values) except the lone "-"; a repeated
+// single-value option is an error; -M takes one or two values per
+// occurrence and occurrences append.
+struct Parsed {
+  std::map<std::string, std::string> val;
+  std::map<std::string, bool> flag;
+  std::vector<std::string> multi;
+};
+
+Parsed parse_args(int argc, char** argv, int first, const std::vector<OptSpec>& specs, const char* multi_short) {
+  Parsed p;
+  auto find_long = [&](const std::string& n) -> const OptSpec* {
+    for (auto& s : specs)
+      if (s.long_name && n == s.long_name) return &s;
+    return nullptr;
+  };
+  auto find_short = [&](char c) -> const OptSpec* {
+    for (auto& s : specs)
+      if (s.short_name == c) return &s;
+    return nullptr;
+  };
+  auto is_value = [](const char* t) { return t[0] != '-' || t[1] == '\0'; };
+  auto set = [&](const OptSpec* s, const std::string& v) {
+    std::string key = s->long_name ? s->long_name : std::string(1, s->short_name);
+    if (p.val.count(key)) throw UsageError("the argument '--" + key + "' cannot be used multiple times");
+    p.val[key] = v;
+  };
+  for (int i = first; i < argc; i++) {
+    std::string t = argv[i];
+    if (multi_short && t.size() >= 2 && t[0] == '-' && t[1] == multi_short[0] && (t.size() == 2 || t[1] != '-')) {
+      std::vector<std::string> vals;
+      if (t.size() > 2) vals.push_back(t.substr(t[2] == '=' ? 3 : 2));
+      while (vals.size() < 2 && i + 1 < argc && is_value(argv[i + 1])) vals.push_back(argv[++i]);
+      if (vals.empty()) throw UsageError(std::string("a value is required for '-") + multi_short[0] + "'");
+      for (auto& v : vals) p.multi.push_back(v);
+      continue;
+    }
+    const OptSpec* s = nullptr;
+    std::string inline_val;
+    bool has_inline = false;
+    if (t.rfind("--", 0) == 0 && t.size() > 2) {
+      size_t eq = t.find('=');
+      std::string name = t.substr(2, eq == std::string::npos ? std::string::npos : eq - 2);
+      s = find_long(name);
+      if (!s) throw UsageError("unexpected argument '" + t + "' found");
+      if (eq != std::string::npos) { inline_val = t.substr(eq + 1); has_inline = true; }
+    } else if (t.size() >= 2 && t[0] == '-' && t[1] != '-') {
+      s = find_short(t[1]);
+      if (!s) throw UsageError("unexpected argument '" + t + "' found");
+      if (t.size() > 2) {
+        inline_val = t.substr(t[2] == '=' ? 3 : 2);
+        has_inline = true;
+      }
+    } else {
+      throw UsageError("unexpected argument '" + t + "' found");
+    }
+    if (!s->takes_value) {
+      if (has_inline) throw UsageError("unexpected value for a flag in '" + t + "'");
+      std::string key = s->long_name;
+      if (p.flag[key]) throw UsageError("the argument '--" + key + "' cannot be used multiple times");
+      p.flag[key] = true;
+      continue;
+    }
+    if (has_inline) {
+      set(s, inline_val);
+    } else {
+      if (i + 1 >= argc || !is_value(argv[i + 1])) throw UsageError("a value is required for '" + t + "'");
+      set(s, argv[++i]);
+    }
+  }
+  return p;
+}
+
+// Rust's u32/usize from_str: optional '+', decimal digits only.
+uint64_t parse_uint(const std::string& s, uint64_t max, const char* what) {
+  size_t i = s.size() && s[0] == '+' ? 1 : 0;
+  if (i == s.size()) throw UsageError(std::string("invalid value '") + s + "' for '" + what + "'");
+  uint64_t v = 0;
+  for (; i < s.size(); i++) {
+    if (s[i] < '0' || s[i] > '9') throw UsageError(std::string("invalid value '") + s + "' for '" + what + "'");
+    v = v * 10 + (uint64_t)(s[i] - '0');
+    if (v > max) throw UsageError(std::string("invalid value '") + s + "' for '" + what + "'");
+  }
+  return v;
+}
+// f64::from_str: decimal or exponent notation, inf / infinity / nan; no
+// surrounding whitespace, no hexadecimal.
+double parse_f64(const std::string& s, const char* what) {
+  const std::string bad = std::string("invalid value '") + s + "' for '" + what + "'";
+  if (s.empty() || isspace((unsigned char)s[0])) throw UsageError(bad);
+  std::string low;
+  for (char c : s) low.push_back((char)tolower((unsigned char)c));
+  size_t k = (low[0] == '+' || low[0] == '-') ? 1 : 0;
+  if (low.compare(k, std::string::npos, "0x", 0, 2) == 0) throw UsageError(bad);
+  const std::string body = low.substr(k);
+  if (body == "inf" || body == "infinity") return low[0] == '-' ? -INFINITY : INFINITY;
+  if (body == "nan") return NAN;
+  for (char c : body)
+    if (!(isdigit((unsigned char)c) || c == '.' || c == 'e' || c == '+' || c == '-')) throw UsageError(bad);
+  char* end = nullptr;
+  double v = strtod(s.c_str(), &end);
+  if (end != s.c_str() + s.size()) throw UsageError(bad);
+  return v;
+}
+
+struct RecordSet {
+  std::vector<int32_t> contig, mate_contig, as_score, nm;
+  std::vector<uint64_t> pos, mate_pos;
+  std::vector<uint8_t> mapq;
+  std::vector<uint16_t> flag;
+  std::vector<int64_t> tlen;
+  std::vector<double> log_lk, posterior;
+  std::vector<uint32_t> cigar_off, cigar;
+  orc_records c{};
+  void alloc(uint64_t n, uint64_t bases) {
+    contig.resize(n); mate_contig.resize(n); as_score.resize(n); nm.resize(n);
+    pos.resize(n); mate_pos.resize(n); mapq.resize(n); flag.resize(n); tlen.resize(n);
+    log_lk.resize(n); posterior.resize(n); cigar_off.resize(n + 1);
+    cigar.resize(2 * bases + 2 * n + 16);
+    c = orc_records{n, contig.data(), pos.data(), mapq.data(), flag.data(), mate_contig.data(), mate_pos.data(),
+                    tlen.data(), log_lk.data(), posterior.data(), as_score.data(), nm.data(), cigar_off.data(),
+                    cigar.data(), cigar.size()};
+  }
+};
+
+struct ReadSoA {
+  std::vector<u8> bases, quals;
+  std::vector<uint64_t> offsets{0};
+  std::vector<std::string> ids;
+  std::vector<const char*> id_ptrs;
+  orc_reads c{};
+  void from(const std::vector<Read>& rs) {
+    for (auto& r : rs) {
+      for (size_t t = 0; t < r.bases.size(); t++) {
+        bases.push_back(r.bases[t]);
+        quals.push_back(t < r.quals.size() ? r.quals[t] : 30);
+      }
+      offsets.push_back(bases.size());
+      ids.push_back(r.id);
+    }
+    for (auto& s : ids) id_ptrs.push_back(s.c_str());
+    c = orc_reads{rs.size(), bases.data(), quals.data(), offsets.data()};
+  }
+};
+
+std::vector<Read> load_reads(const std::string& path, bool fasta, u8 qoff, const std::string* adapter) {
+  std::vector<Read> rs = fasta ? read_fasta_reads(path) : read_fastq(path, qoff);
+  preprocess(rs, adapter);
+  return rs;
+}
+
+int cli_map(int argc, char** argv) {
+  static const std::vector<OptSpec> specs = {
+      {"genome", 'g', true},       {"hash", 'h', true},        {"substitution-rate", 's', true},
+      {"threads", 't', true},      {"gapopen", 0, true},       {"gapextend", 0, true},
+      {"svprior", 0, true},        {"phred64", 0, false},      {"inputformat", 0, true},
+      {"readgroup", 0, true},      {"outputformat", 'f', true}, {"output", 'o', true},
+      {"labelfilter", 0, true},    {"casava8", 0, false},      {"adapter-strip", 0, true},
+      {"index", 0, false}};
+  Parsed p = parse_args(argc, argv, 2, specs, "M");
+  if (!p.val.count("genome")) throw UsageError("the following required arguments were not provided: --genome");
+  if (!p.val.count("hash")) throw UsageError("the following required arguments were not provided: --hash");
+  orc_options o;
+  orc_default_options(&o);
+  if (p.val.count("substitution-rate")) o.substitution_rate = parse_f64(p.val["substitution-rate"], "--substitution-rate");
+  if (p.val.count("threads")) o.threads = (int32_t)parse_uint(p.val["threads"], 1u << 20, "--threads");
+  if (p.val.count("gapopen")) o.gap_open_phred = (uint32_t)parse_uint(p.val["gapopen"], 0xFFFFFFFFu, "--gapopen");
+  if (p.val.count("gapextend")) o.gap_extend_phred = (uint32_t)parse_uint(p.val["gapextend"], 0xFFFFFFFFu, "--gapextend");
+  if (p.val.count("svprior")) o.sv_prior_phred = parse_f64(p.val["svprior"], "--svprior");
+  const u8 qoff = p.flag["phred64"] ? 64 : 33;
+  const std::string informat = p.val.count("inputformat") ? p.val["inputformat"] : "fastq";
+  if (informat != "fasta" && informat != "fastq")
+    throw std::runtime_error("--inputformat must be 'fastq' or 'fasta', got '" + informat + "'");
+  const std::string outformat = p.val.count("outputformat") ? p.val["outputformat"] : "sam";
+  if (outformat != "sam" && outformat != "bam")
+    throw std::runtime_error("--outputformat must be 'sam' or 'bam', got '" + outformat + "'");
+  const char* rg = p.val.count("readgroup") ? p.val["readgroup"].c_str() : nullptr;
+  if (rg) {
+    std::string id, line;
+    if (!parse_read_group(rg, id, line)) throw std::runtime_error(g_err);
+  }
+  std::string cl;
+  for (int i = 0; i < argc; i++) cl += (i ? " " : "") + std::string(argv[i]);
+  std::unique_ptr<Mapper> m(new Mapper());
+  if (!m->open(p.val["genome"], p.val["hash"], o)) throw std::runtime_error(g_err);
+  const bool fasta = informat == "fasta";
+  std::string adapter = p.val.count("adapter-strip") ? p.val["adapter-strip"] : "";
+  const std::string* ad = p.val.count("adapter-strip") ? &adapter : nullptr;
+  // map_reads_with_format (lib.rs:65-104): two files = pairs, else single-end over all files
+  const bool paired = p.multi.size() == 2;
+  ReadSoA R[2];
+  RecordSet S[2];
+  uint32_t n_src = paired ? 2 : 1;
+  if (paired) {
+    R[0].from(load_reads(p.multi[0], fasta, qoff, ad));
+    R[1].from(load_reads(p.multi[1], fasta, qoff, ad));
+    if (R[0].c.n != R[1].c.n)
+      throw std::runtime_error("paired-end input files have different read counts (" + std::to_string(R[0].c.n) +
+                               " vs " + std::to_string(R[1].c.n) + ")");
+    S[0].alloc(R[0].c.n, R[0].bases.size());
+    S[1].alloc(R[1].c.n, R[1].bases.size());
+    orc_insert_model im{o.insert_size_mean, o.insert_size_sd, 0};
+    if (orc_map_paired(m.get(), &im, &R[0].c, &R[1].c, &S[0].c, &S[1].c) != 0) throw std::runtime_error(g_err);
+  } else {
+    std::vector<Read> all;
+    for (auto& f : p.multi) {
+      auto rs = load_reads(f, fasta, qoff, ad);
+      all.insert(all.end(), rs.begin(), rs.end());
+    }
+    R[0].from(all);
+    S[0].alloc(R[0].c.n, R[0].bases.size());
+    if (orc_map_single(m.get(), &R[0].c, &S[0].c) != 0) throw std::runtime_error(g_err);
+  }
+  // record order: pairs interleaved (lib.rs:171-181)
+  std::vector<uint64_t> sel;
+  const uint64_t n = R[0].c.n;
+  for (uint64_t i = 0; i < n * n_src; i++) {
+    if (p.val.count("labelfilter")) {
+      const std::string& id = R[i % n_src].ids[i / n_src];
+      if (id.rfind(p.val["labelfilter"], 0) != 0) continue;
+    }
+    sel.push_back(i);
+  }
+  const bool index = p.flag["index"];
+  if (index) {
+    if (outformat != "bam") throw std::runtime_error("--index requires --outputformat=bam");
+    if (!p.val.count("output"))
+      throw std::runtime_error("--index requires --output FILE (an index needs a real file to index)");
+    const orc_records* rp[2] = {&S[0].c, &S[1].c};
+    sort_coordinate(m.get(), n_src, rp, sel);
+  }
+  if (outformat == "bam") throw std::runtime_error("BAM output is not built (SAM only)");
+  const orc_reads* rp[2] = {&R[0].c, &R[1].c};
+  const char* const* ip[2] = {R[0].id_ptrs.data(), R[1].id_ptrs.data()};
+  const orc_records* sp[2] = {&S[0].c, &S[1].c};
+  const std::string out = p.val.count("output") ? p.val["output"] : "-";
+  if (orc_sam_write(m.get(), cl.c_str(), rg, index ? 1 : 0, n_src, rp, ip, sp, sel.data(), sel.size(), out.c_str()) != 0)
+    throw std::runtime_error(g_err);
+  return 0;
+}
+
+int cli_build_genome(int argc, char** argv) {
+  static const std::vector<OptSpec> specs = {{"species", 's', true}, {"assembly", 'a', true}, {nullptr, 'G', true}};
+  // positional FASTA files follow the options
+  std::vector<char*> opts{argv[0], argv[1]};
+  std::vector<std::string> files;
+  for (int i = 2; i < argc; i++) {
+    if (argv[i][0] == '-' && argv[i][1] != '\0') {
+      opts.push_back(argv[i]);
+      std::string t = argv[i];
+      bool inline_v = (t.rfind("--", 0) == 0) ? t.find('=') != std::string::npos : t.size() > 2;
+      if (!inline_v && i + 1 < argc) opts.push_back(argv[++i]);
+    } else {
+      files.push_back(argv[i]);
+    }
+  }
+  Parsed p = parse_args((int)opts.size(), opts.data(), 2, specs, nullptr);
+  for (const char* k : {"species", "assembly", "G"})
+    if (!p.val.count(k)) throw UsageError(std::string("the following required arguments were not provided: ") + k);
+  printf("Building genome index for %s %s...\n", p.val["species"].c_str(), p.val["assembly"].c_str());
+  std::vector<const char*> fp;
+  for (auto& f : files) fp.push_back(f.c_str());
+  if (orc_build_genome(p.val["G"].c_str(), p.val["species"].c_str(), p.val["assembly"].c_str(), (int)fp.size(),
+                       fp.data()) != 0)
+    throw std::runtime_error(g_err);
+  printf("Done. Index written to %s.stidx\n", p.val["G"].c_str());
+  return 0;
+}
+
+int cli_build_hash(int argc, char** argv) {
+  static const std::vector<OptSpec> specs = {{"genome", 'g', true}, {nullptr, 'H', true}};
+  Parsed p = parse_args(argc, argv, 2, specs, nullptr);
+  if (!p.val.count("genome") || !p.val.count("H")) throw UsageError("--genome and -H are required");
+  printf("Building 15-mer hash table...\n");
+  if (orc_build_hash(p.val["genome"].c_str(), p.val["H"].c_str(), 15, 5, 300) != 0) throw std::runtime_error(g_err);
+  printf("Done. Hash table written to %s.sthash\n", p.val["H"].c_str());
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int orc_cli_main(int argc, char** argv) {
+  try {
+    if (argc < 2) throw UsageError("a subcommand is required: map, build-genome, build-hash");
+    const std::string cmd = argv[1];
+    if (cmd == "map") return cli_map(argc, argv);
+    if (cmd == "build-genome") return cli_build_genome(argc, argv);
+    if (cmd == "build-hash") return cli_build_hash(argc, argv);
+    throw UsageError("unrecognized subcommand '" + cmd + "'");
+  } catch (UsageError& e) {
+    fprintf(stderr, "error: %s\n", e.what());
+    return 2;
+  } catch (std::exception& e) {
+    fprintf(stderr, "Error: %s\n", e.what());
+    return 1;
+  }
+}

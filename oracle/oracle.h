@@ -125,6 +125,21 @@ int orc_align(const uint8_t* read, const uint8_t* qual, uint64_t m, const uint8_
 // SAM text for a record set (src/io/sam.rs:37-143). Writes to path.
 int orc_write_sam(void* h, const char* path, const char* command_line, const orc_reads* reads,
                   const char* const* read_ids, const orc_records* recs);
+// SAM stream of the records numbered r * n_src + s (record r of source s;
+// n_src 2 = mates 1 and 2) listed in sel, with an optional --readgroup spec
+// and the SO:coordinate header (format_sam_records_sorted, sam.rs:83-108).
+// path "-" = standard output.
+int orc_sam_write(void* h, const char* command_line, const char* read_group, int coordinate_sorted, uint32_t n_src,
+                  const orc_reads* const* reads, const char* const* const* ids, const orc_records* const* recs,
+                  const uint64_t* sel, uint64_t n_sel, const char* path);
+// sort_for_coordinate_order (sam.rs:114-124) of the numbered records in sel.
+int orc_sort_coordinate(void* h, uint32_t n_src, const orc_records* const* recs, const uint64_t* sel, uint64_t n_sel,
+                        uint64_t* out);
+// The `probebwa map` command (src/main.rs:51-111, 130-189) restated over this
+// oracle: same flags, same SAM stream; argv[1] must be "map". Returns the exit
+// status (0; 1 on an error, reported on stderr as "Error: ..."; 2 on a usage
+// error).
+int orc_cli_main(int argc, char** argv);
 
 // ---- FASTQ / FASTA reads (src/io/fastx.rs) ----
 // Parses a file into an internal buffer; returns a handle with n reads.

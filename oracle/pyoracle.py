@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 
+CLI_PATH = os.path.join(HERE, "_build", "probebwa_oracle")
+
+
 def build(quiet: bool = True) -> str:
     """Compile the oracle with its Makefile (make is incremental)."""
     out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
@@ -110,6 +113,8 @@ def lib():
         L.orc_align.argtypes = [vp, vp, u64, vp, u64, i64, u64, u32, u32, vp, vp, vp, u64, vp]
         L.orc_mapq_batch.argtypes = [vp, C.POINTER(ReadsC), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_write_sam.argtypes = [vp, cp, cp, C.POINTER(ReadsC), C.POINTER(cp), C.POINTER(RecordsC)]
+        L.orc_sam_write.argtypes = [vp, cp, cp, C.c_int, u32, vp, vp, vp, vp, u64, cp]
+        L.orc_sort_coordinate.argtypes = [vp, u32, vp, vp, u64, vp]
         L.orc_reads_parse.argtypes = [cp, C.c_int, C.c_uint8, cp]
         L.orc_reads_parse.restype = vp
         L.orc_reads_count.argtypes = [vp]
@@ -350,6 +355,50 @@ class Mapper:
         if n < 0:
             raise RuntimeError(f"candidate capacity exceeded ({-n})")
         return cc[:n], cp[:n], cs[:n], sc[:n]
+
+    def _sources(self, sources):
+        keep = []
+        rp = (C.c_void_p * len(sources))()
+        ip = (C.c_void_p * len(sources))()
+        sp = (C.c_void_p * len(sources))()
+        for k, (reads, recs) in enumerate(sources):
+            rc_ = reads.c()
+            ids = (C.c_char_p * max(reads.n, 1))(*[i.encode() for i in reads.ids])
+            cr = records_c(recs)
+            keep += [rc_, ids, cr]
+            rp[k] = C.addressof(rc_)
+            ip[k] = C.addressof(ids)
+            sp[k] = C.addressof(cr)
+        return rp, ip, sp, keep
+
+    def sam_text(self, path: str, sources, sel=None, command_line="probebwa map", read_group=None,
+                 coordinate_sorted=False) -> bytes:
+        """format_sam_records_sorted (sam.rs:83-108) over the records numbered
+        r * len(sources) + s listed in sel (all, in number order, by default);
+        written to path and returned."""
+        rp, ip, sp, keep = self._sources(sources)
+        if sel is None:
+            sel = np.arange(len(sources[0][1]["contig"]) * len(sources), dtype=np.uint64)
+        sel = np.ascontiguousarray(sel, dtype=np.uint64)
+        selk = sel if sel.size else np.zeros(1, np.uint64)
+        rc = lib().orc_sam_write(self.h, command_line.encode(), read_group.encode() if read_group is not None else None,
+                                 1 if coordinate_sorted else 0, len(sources), rp, ip, sp, _ptr(selk), sel.size,
+                                 path.encode())
+        if rc != 0:
+            raise RuntimeError(_err())
+        with open(path, "rb") as f:
+            return f.read()
+
+    def sort_coordinate(self, sources, sel=None) -> np.ndarray:
+        """sort_for_coordinate_order (sam.rs:114-124) of record numbers."""
+        rp, ip, sp, keep = self._sources(sources)
+        if sel is None:
+            sel = np.arange(len(sources[0][1]["contig"]) * len(sources), dtype=np.uint64)
+        sel = np.ascontiguousarray(sel, dtype=np.uint64)
+        out = np.zeros(max(sel.size, 1), np.uint64)
+        selk = sel if sel.size else np.zeros(1, np.uint64)
+        lib().orc_sort_coordinate(self.h, len(sources), sp, _ptr(selk), sel.size, _ptr(out))
+        return out[:sel.size]
 
     def write_sam(self, path: str, reads: Reads, recs: dict, command_line="probebwa map"):
         ids = (C.c_char_p * reads.n)(*[i.encode() for i in reads.ids])

@@ -62,6 +62,14 @@ class RecordsC(C.Structure):
         "cigar_off", "cigar")] + [("cigar_cap", C.c_uint64)]
 
 
+class SamOptionsC(C.Structure):
+    _fields_ = [("command_line", C.c_char_p), ("read_group", C.c_char_p), ("coordinate_sorted", C.c_int32)]
+
+
+class SamSourceC(C.Structure):
+    _fields_ = [("reads", C.POINTER(ReadsC)), ("read_ids", C.POINTER(C.c_char_p)), ("recs", C.POINTER(RecordsC))]
+
+
 class InsertModelC(C.Structure):
     _fields_ = [("mean", C.c_double), ("sd", C.c_double), ("n_observed", C.c_uint64)]
 
@@ -123,6 +131,9 @@ def lib():
         L.pbw_cluster_batch.argtypes = [vp, C.POINTER(ReadsC), u32, vp, vp, vp, vp, vp, vp]
         L.pbw_last_stats.argtypes = [vp, C.POINTER(StatsC)]
         L.pbw_write_sam.argtypes = [vp, cp, cp, C.POINTER(ReadsC), C.POINTER(cp), C.POINTER(RecordsC)]
+        L.pbw_sam_write.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, cp]
+        L.pbw_sam_format.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, vp, u64, vp]
+        L.pbw_sort_coordinate.argtypes = [vp, u32, C.POINTER(SamSourceC), vp, u64, vp]
         if hasattr(L, "pbw_align_noalloc"):
             L.pbw_align_noalloc.argtypes = [u64, vp, vp, vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, u32, vp]
         _lib = L
@@ -394,6 +405,50 @@ class Mapper:
         ids = (C.c_char_p * max(reads.n, 1))(*[i.encode() for i in reads.ids])
         self._check(lib().pbw_write_sam(self.h, path.encode(), command_line.encode(), C.byref(reads.c()), ids,
                                         C.byref(records_c(recs))))
+
+    def _sam_sources(self, sources):
+        """sources: [(Reads, records dict)] -- one (single-end) or two (mates)."""
+        keep = []
+        arr = (SamSourceC * len(sources))()
+        for k, (reads, recs) in enumerate(sources):
+            rc_ = reads.c()
+            ids = (C.c_char_p * max(reads.n, 1))(*[i.encode() for i in reads.ids])
+            cr = records_c(recs)
+            keep += [rc_, ids, cr]
+            arr[k] = SamSourceC(C.pointer(rc_), ids, C.pointer(cr))
+        return arr, keep
+
+    def sam_text(self, sources, sel=None, command_line: str = "probebwa map", read_group: str | None = None,
+                 coordinate_sorted: bool = False) -> bytes:
+        """SAM stream of the selected records (format_sam_records_sorted,
+        sam.rs:83-108), formatted on the device. Record r of source s is
+        number r * len(sources) + s; sel=None takes all in number order."""
+        arr, keep = self._sam_sources(sources)
+        o = SamOptionsC(command_line.encode(), read_group.encode() if read_group is not None else None,
+                        1 if coordinate_sorted else 0)
+        sp, ns = (None, 0)
+        if sel is not None:
+            # an empty selection still passes a list: NULL means every record
+            sel = np.ascontiguousarray(sel, dtype=np.uint64)
+            keep.append(sel if sel.size else np.zeros(1, np.uint64))
+            sp, ns = (_ptr(keep[-1]), int(sel.size))
+        n = C.c_uint64(0)
+        self._check(lib().pbw_sam_format(self.h, C.byref(o), len(sources), arr, sp, ns, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(max(n.value, 1))
+        self._check(lib().pbw_sam_format(self.h, C.byref(o), len(sources), arr, sp, ns, buf, n.value, C.byref(n)))
+        return buf.raw[:n.value]
+
+    def sort_coordinate(self, sources, sel=None) -> np.ndarray:
+        """sort_for_coordinate_order (sam.rs:114-124) of the selected record
+        numbers, on the device."""
+        arr, keep = self._sam_sources(sources)
+        if sel is None:
+            sel = np.arange(len(sources[0][1]["contig"]) * len(sources), dtype=np.uint64)
+        sel = np.ascontiguousarray(sel, dtype=np.uint64)
+        out = np.zeros(max(sel.size, 1), np.uint64)
+        self._check(lib().pbw_sort_coordinate(self.h, len(sources), arr, _ptr(sel) if sel.size else None,
+                                              int(sel.size), _ptr(out)))
+        return out[:sel.size]
 
     def mapq_batch(self, reads: Reads, items) -> dict:
         """MapqCalculator::select_best + finalize_mapq (bayesian.rs:193-201,

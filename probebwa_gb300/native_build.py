@@ -66,11 +66,30 @@ def build(verbose: bool = False) -> str:
                 sys.stderr.write(log)
     newest = max(os.path.getmtime(o) for o in objs)
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli()
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "cli", "probebwa.cpp")
+CLI = os.path.join(LIBDIR, "probebwa")
+
+
+def build_cli() -> str:
+    """The `probebwa` command line (host C++ over the C ABI), linked against
+    the library in the same folder."""
+    deps = [CLI_SRC, LIB, os.path.join(os.path.dirname(HERE), "include", "probebwa_gpu.h")]
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(p) for p in deps):
+        return CLI
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", "-o", CLI, CLI_SRC, "-L" + LIBDIR,
+           "-lprobebwa_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":
