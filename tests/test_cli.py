@@ -192,7 +192,7 @@ def test_cli_sam_matches_oracle_cli(oracle, tmp_path, clis):
         ["map", "-g", prefix, "-h", prefix, "--inputformat", "fasta", "--adapter-strip", "ACGTACGTAC", "-M", fa],
         ["map", "-g", prefix, "-h", prefix, "-M", p1, p2],
         ["map", "-g", prefix, "-h", prefix, "--svprior", "40", "--labelfilter", "pair1", "-M", p1, "-M", p2],
-        ["map", "-g", prefix, "-h", prefix, "-M", fq, fq, "-M", fa, "--inputformat", "fastq"],
+        ["map", "-g", prefix, "-h", prefix, "-M", fq, fq, "-M", fq64, "--inputformat", "fastq"],
     ]
     for args in runs:
         mine = _run(clis[0], args)
