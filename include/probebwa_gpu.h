@@ -269,6 +269,25 @@ int pbw_reads_get(const pbw_read_set* rs, pbw_reads* view);
 const char* pbw_reads_id(const pbw_read_set* rs, uint64_t i);
 void pbw_reads_free(pbw_read_set* rs);
 
+/* build-genome (GenomeIndexBuilder, src/index/genome.rs:98-148): the FASTA
+ * files (gunzipped when a name ends in ".gz") into out_prefix.stidx, one contig
+ * per record, in file order. Host code; no device is used. Errors:
+ * PBW_ERR_IO, PBW_ERR_FORMAT (text that is not UTF-8), described by
+ * pbw_last_error(NULL). */
+int pbw_build_genome(const char* out_prefix, const char* species, const char* assembly, uint32_t n_files,
+                     const char* const* fasta_paths);
+
+/* build-hash (HashTableBuilder::build + save, src/index/hashtable.rs:81-87,
+ * 248-322) on the given CUDA device: the occurrence table of
+ * genome_prefix.stidx written to out_prefix.sthash -- forward and reverse-
+ * complement windows every stride bases, windows with a non-ACGT base
+ * skipped, the first max_count occurrences of each hash in scan order, groups
+ * in ascending hash order. The reference's defaults are k 15, stride 5,
+ * max_count 300. Limits: 1 <= k <= 32, fewer than 2^32 windows
+ * (PBW_ERR_LIMIT). Errors are described by pbw_last_error(NULL). */
+int pbw_build_hash(const char* genome_prefix, const char* out_prefix, uint64_t k, uint64_t stride,
+                   uint64_t max_count, int32_t device);
+
 /* Allocation-free window alignment. No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc -- code running while a stream is
  * captured into a CUDA graph, applications whose allocator owns all device

@@ -134,6 +134,8 @@ def lib():
         L.pbw_sam_write.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, cp]
         L.pbw_sam_format.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, vp, u64, vp]
         L.pbw_sort_coordinate.argtypes = [vp, u32, C.POINTER(SamSourceC), vp, u64, vp]
+        L.pbw_build_genome.argtypes = [cp, cp, cp, u32, C.POINTER(cp)]
+        L.pbw_build_hash.argtypes = [cp, cp, u64, u64, u64, C.c_int32]
         if hasattr(L, "pbw_align_noalloc"):
             L.pbw_align_noalloc.argtypes = [u64, vp, vp, vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, u32, vp]
         _lib = L
@@ -277,6 +279,26 @@ def load_reads(path: str, fasta: bool = False, quality_offset: int = 33, adapter
     finally:
         L.pbw_reads_free(h)
     return Reads(bases, quals, offs, ids)
+
+
+def build_genome(out_prefix: str, fasta_paths, species: str = "species", assembly: str = "assembly") -> None:
+    """build-genome (GenomeIndexBuilder, src/index/genome.rs:98-148) through
+    pbw_build_genome: FASTA files -> out_prefix.stidx."""
+    L = lib()
+    arr = (C.c_char_p * max(len(fasta_paths), 1))(*[p.encode() for p in fasta_paths])
+    rc = L.pbw_build_genome(out_prefix.encode(), species.encode(), assembly.encode(), len(fasta_paths), arr)
+    if rc != 0:
+        raise PbwError(rc, L.pbw_last_error(None).decode())
+
+
+def build_hash(genome_prefix: str, out_prefix: str, k: int = 15, stride: int = 5, max_count: int = 300,
+               device: int = 0) -> None:
+    """build-hash (HashTableBuilder, src/index/hashtable.rs:248-322) on the
+    GPU through pbw_build_hash: genome_prefix.stidx -> out_prefix.sthash."""
+    L = lib()
+    rc = L.pbw_build_hash(genome_prefix.encode(), out_prefix.encode(), k, stride, max_count, device)
+    if rc != 0:
+        raise PbwError(rc, L.pbw_last_error(None).decode())
 
 
 class Mapper:

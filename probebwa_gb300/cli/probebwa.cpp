@@ -2,7 +2,8 @@
 // (include/probebwa_gpu.h): the drop-in for the reference binary's `map`
 // subcommand (src/main.rs:51-111, 130-189).
 //
-// Same flags, same checks in the same order, same SAM stream:
+// Subcommands map, build-genome and build-hash. For map: same flags, same
+// checks in the same order, same SAM stream:
 //   probebwa map -g|--genome PREFIX -h|--hash PREFIX [-s|--substitution-rate F]
 //     [-t|--threads N] [--gapopen N] [--gapextend N] [--svprior F] [--phred64]
 //     [--inputformat fastq|fasta] [--readgroup ID:x,...] [-f|--outputformat sam]
@@ -14,11 +15,14 @@
 // in the reference either (fastx.rs:29-41). BAM output (-f bam, and --index,
 // which needs it) is not built: the command stops with an error after the
 // same argument checks as the reference. Errors: usage errors exit 2, others
-// print "Error: ..." and exit 1.
+// print "Error: ..." and exit 1. build-genome / build-hash write the same
+// index files as the reference's subcommands (the hash table is built on the
+// GPU).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -50,11 +54,14 @@ const Flag MAP_FLAGS[] = {
     {"labelfilter", 0, true},   {"casava8", 0, false},       {"adapter-strip", 0, true},
     {"index", 0, false},
 };
+const Flag GENOME_FLAGS[] = {{"species", 's', true}, {"assembly", 'a', true}, {"", 'G', true}};
+const Flag HASH_FLAGS[] = {{"genome", 'g', true}, {"", 'H', true}};
 
 struct Args {
   std::map<std::string, std::string> opt;
   std::map<std::string, bool> on;
   std::vector<std::string> reads;  // -M values, appended over occurrences
+  std::vector<std::string> files;  // positional arguments
   bool has(const char* k) const { return opt.count(k) != 0; }
   std::string get(const char* k, const char* dflt) const {
     auto it = opt.find(k);
@@ -64,12 +71,13 @@ struct Args {
 
 bool looks_like_value(const char* t) { return t[0] != '-' || t[1] == '\0'; }
 
-Args parse(int argc, char** argv) {
+// flags: the subcommand's options; with_m: -M takes one or two values per
+// occurrence; positional: bare arguments are collected in files.
+Args parse(int argc, char** argv, const Flag* flags, size_t n_flags, bool with_m, bool positional) {
   Args a;
   for (int i = 2; i < argc; i++) {
     const std::string t = argv[i];
-    if (t.size() >= 2 && t[0] == '-' && t[1] == 'M') {
-      // -M takes one or two values per occurrence
+    if (with_m && t.size() >= 2 && t[0] == '-' && t[1] == 'M') {
       int got = 0;
       if (t.size() > 2) {
         a.reads.push_back(t.substr(t[2] == '=' ? 3 : 2));
@@ -82,44 +90,52 @@ Args parse(int argc, char** argv) {
       if (!got) throw Usage("a value is required for '-M <READS>...' but none was supplied");
       continue;
     }
+    if (positional && looks_like_value(argv[i])) {
+      a.files.push_back(t);
+      continue;
+    }
     const Flag* f = nullptr;
     bool inline_v = false;
     std::string v;
     if (t.size() > 2 && t[0] == '-' && t[1] == '-') {
       const size_t eq = t.find('=');
       const std::string name = t.substr(2, eq == std::string::npos ? std::string::npos : eq - 2);
-      for (const Flag& x : MAP_FLAGS)
-        if (name == x.name) f = &x;
+      for (size_t q = 0; q < n_flags; q++)
+        if (flags[q].name[0] && name == flags[q].name) f = &flags[q];
       if (eq != std::string::npos) {
         inline_v = true;
         v = t.substr(eq + 1);
       }
     } else if (t.size() >= 2 && t[0] == '-' && t[1] != '-') {
-      for (const Flag& x : MAP_FLAGS)
-        if (x.short_name && x.short_name == t[1]) f = &x;
+      for (size_t q = 0; q < n_flags; q++)
+        if (flags[q].short_name && flags[q].short_name == t[1]) f = &flags[q];
       if (t.size() > 2) {
         inline_v = true;
         v = t.substr(t[2] == '=' ? 3 : 2);
       }
     }
     if (!f) throw Usage("unexpected argument '" + t + "' found");
+    const std::string key = f->name[0] ? f->name : std::string(1, f->short_name);
     if (!f->value) {
-      if (inline_v) throw Usage("unexpected value for '--" + std::string(f->name) + "'");
-      if (a.on[f->name]) throw Usage("the argument '--" + std::string(f->name) + "' cannot be used multiple times");
-      a.on[f->name] = true;
+      if (inline_v) throw Usage("unexpected value for '--" + key + "'");
+      if (a.on[key]) throw Usage("the argument '--" + key + "' cannot be used multiple times");
+      a.on[key] = true;
       continue;
     }
     if (!inline_v) {
       if (i + 1 >= argc || !looks_like_value(argv[i + 1]))
-        throw Usage("a value is required for '--" + std::string(f->name) + "' but none was supplied");
+        throw Usage("a value is required for '--" + key + "' but none was supplied");
       v = argv[++i];
     }
-    if (a.has(f->name)) throw Usage("the argument '--" + std::string(f->name) + "' cannot be used multiple times");
-    a.opt[f->name] = v;
+    if (a.has(key.c_str())) throw Usage("the argument '--" + key + "' cannot be used multiple times");
+    a.opt[key] = v;
   }
-  if (!a.has("genome")) throw Usage("the following required arguments were not provided: --genome <GENOME>");
-  if (!a.has("hash")) throw Usage("the following required arguments were not provided: --hash <HASH>");
   return a;
+}
+
+void require(const Args& a, std::initializer_list<const char*> keys) {
+  for (const char* k : keys)
+    if (!a.has(k)) throw Usage(std::string("the following required arguments were not provided: ") + k);
 }
 
 // u32 / usize as Rust's from_str: optional '+', then decimal digits.
@@ -257,7 +273,8 @@ struct Handle {
 };
 
 int run_map(int argc, char** argv) {
-  const Args a = parse(argc, argv);
+  const Args a = parse(argc, argv, MAP_FLAGS, sizeof(MAP_FLAGS) / sizeof(MAP_FLAGS[0]), true, false);
+  require(a, {"genome", "hash"});
   pbw_options o;
   pbw_default_options(&o);
   if (a.has("substitution-rate")) o.substitution_rate = to_f64(a.get("substitution-rate", ""), "substitution-rate");
@@ -332,13 +349,44 @@ int run_map(int argc, char** argv) {
   return 0;
 }
 
+// build-genome (main.rs:33-41, 118-123): FASTA files -> PREFIX.stidx.
+int run_build_genome(int argc, char** argv) {
+  const Args a = parse(argc, argv, GENOME_FLAGS, 3, false, true);
+  require(a, {"species", "assembly", "G"});
+  printf("Building genome index for %s %s...\n", a.get("species", "").c_str(), a.get("assembly", "").c_str());
+  fflush(stdout);
+  std::vector<const char*> files;
+  for (const std::string& f : a.files) files.push_back(f.c_str());
+  if (pbw_build_genome(a.get("G", "").c_str(), a.get("species", "").c_str(), a.get("assembly", "").c_str(),
+                       (uint32_t)files.size(), files.data()) != PBW_OK)
+    throw Fail(pbw_last_error(nullptr));
+  printf("Done. Index written to %s.stidx\n", a.get("G", "").c_str());
+  return 0;
+}
+
+// build-hash (main.rs:43-49, 124-128): PREFIX.stidx -> OUT.sthash, built on
+// the GPU with the reference's k 15, stride 5, 300 occurrences per hash.
+int run_build_hash(int argc, char** argv) {
+  const Args a = parse(argc, argv, HASH_FLAGS, 2, false, false);
+  require(a, {"genome", "H"});
+  printf("Building 15-mer hash table...\n");
+  fflush(stdout);
+  if (pbw_build_hash(a.get("genome", "").c_str(), a.get("H", "").c_str(), 15, 5, 300, 0) != PBW_OK)
+    throw Fail(pbw_last_error(nullptr));
+  printf("Done. Hash table written to %s.sthash\n", a.get("H", "").c_str());
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   try {
-    if (argc < 2) throw Usage("a subcommand is required (map)");
-    if (std::string(argv[1]) != "map") throw Usage("unrecognized subcommand '" + std::string(argv[1]) + "'");
-    return run_map(argc, argv);
+    if (argc < 2) throw Usage("a subcommand is required (map, build-genome, build-hash)");
+    const std::string cmd = argv[1];
+    if (cmd == "map") return run_map(argc, argv);
+    if (cmd == "build-genome") return run_build_genome(argc, argv);
+    if (cmd == "build-hash") return run_build_hash(argc, argv);
+    throw Usage("unrecognized subcommand '" + cmd + "'");
   } catch (const Usage& e) {
     fprintf(stderr, "error: %s\n", e.what());
     return 2;

@@ -177,7 +177,7 @@ static int build_tables(pbw_handle* h) {
 }
 
 // GenomeIndex::load (src/index/genome.rs:80-86) into the device layout.
-static int load_genome(pbw_handle* h, const std::string& prefix) {
+int load_genome(pbw_handle* h, const std::string& prefix) {
   FileReader fr(prefix + ".stidx");
   if (!fr.f) { h->err = "cannot open " + prefix + ".stidx"; return PBW_ERR_IO; }
   uint64_t nc;

@@ -10,12 +10,8 @@
 // every named contig and before the unmapped ones.
 //
 // Keys are packed into one integer, rank * (max_pos + 1) + pos, with the
-// unmapped key above every mapped one, and sorted least-significant digit
-// first, 8 bits per pass, as many passes as the largest key needs. Each pass:
-// per-tile digit histograms (tiles of 4096 keys), an exclusive scan of the
-// digit-major histogram table, and a scatter in which every tile ranks its
-// keys in input order (warp match on the digit, then per-digit prefixes over
-// the warps of the block), which keeps the sort stable.
+// unmapped key above every mapped one, and sorted by the stable LSD radix
+// sort of radix_sort.cu, as many 8-bit passes as the largest key needs.
 #include <algorithm>
 #include <string>
 #include <unordered_map>
@@ -28,8 +24,6 @@
 namespace pbw {
 
 namespace {
-
-constexpr int RS_T = 256, RS_ROUNDS = 16, RS_TILE = RS_T * RS_ROUNDS, RS_WARPS = RS_T / 32;
 
 struct KeyArgs {
   const int32_t* contig[2];
@@ -56,61 +50,6 @@ __global__ void k_coord_keys(KeyArgs a) {
   const unsigned long long rk = (c >= 0 && (uint32_t)c < a.n_contigs) ? a.rank[c] : a.n_contigs;
   a.key[i] = p == 0 ? a.unmapped : rk * a.span + p;
   a.val[i] = g;
-}
-
-__global__ void __launch_bounds__(RS_T) k_radix_hist(const unsigned long long* key, uint64_t n, int shift,
-                                                     unsigned int* hist, uint32_t nb) {
-  __shared__ unsigned int cnt[256];
-  cnt[threadIdx.x] = 0;
-  __syncthreads();
-  const uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
-  for (int j = 0; j < RS_ROUNDS; j++) {
-    const uint64_t i = base + (uint64_t)j * RS_T + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(unsigned)(key[i] >> shift) & 255u], 1u);
-  }
-  __syncthreads();
-  hist[(uint64_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
-}
-
-__global__ void __launch_bounds__(RS_T) k_radix_scatter(const unsigned long long* key, const unsigned long long* val,
-                                                        uint64_t n, int shift, const unsigned int* start, uint32_t nb,
-                                                        unsigned long long* key_out, unsigned long long* val_out) {
-  __shared__ unsigned int base[256];
-  __shared__ unsigned int wcnt[RS_WARPS][257];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  base[threadIdx.x] = start[(uint64_t)threadIdx.x * nb + blockIdx.x];
-  const uint64_t tile = (uint64_t)blockIdx.x * RS_TILE;
-  const unsigned int lt = (1u << lane) - 1u;
-  for (int j = 0; j < RS_ROUNDS; j++) {
-    for (int k = threadIdx.x; k < RS_WARPS * 257; k += RS_T) (&wcnt[0][0])[k] = 0;
-    __syncthreads();
-    const uint64_t i = tile + (uint64_t)j * RS_T + threadIdx.x;
-    const bool ok = i < n;
-    const unsigned long long kk = ok ? key[i] : 0ull;
-    const unsigned int d = ok ? (unsigned)(kk >> shift) & 255u : 256u;
-    const unsigned int peers = __match_any_sync(0xffffffffu, d);
-    const unsigned int rank = __popc(peers & lt);
-    if (rank == 0) wcnt[w][d] = __popc(peers);
-    __syncthreads();
-    {
-      // per digit: exclusive prefix over the warps, on top of the running base
-      const unsigned int dd = threadIdx.x;
-      unsigned int run = base[dd];
-      for (int q = 0; q < RS_WARPS; q++) {
-        const unsigned int t = wcnt[q][dd];
-        wcnt[q][dd] = run;
-        run += t;
-      }
-      base[dd] = run;
-    }
-    __syncthreads();
-    if (ok) {
-      const unsigned int p = wcnt[w][d] + rank;
-      key_out[p] = kk;
-      val_out[p] = val[i];
-    }
-    __syncthreads();
-  }
 }
 
 #define RCK(call)                                                  \
@@ -166,8 +105,7 @@ extern "C" int pbw_sort_coordinate(pbw_handle* h, uint32_t n_src, const pbw_sam_
   int bits = 0;
   while (bits < 64 && (unmapped >> bits) != 0) bits++;
   const int passes = (bits + 7) / 8;
-  const uint32_t nb = (uint32_t)((n_sel + RS_TILE - 1) / RS_TILE);
-  const uint64_t nh = (uint64_t)nb * 256;
+  const uint64_t nh = radix_hist_entries(n_sel);
   cudaStream_t st = h->st;
   int rc = PBW_OK;
   std::vector<void*> mem;
@@ -211,16 +149,13 @@ extern "C" int pbw_sort_coordinate(pbw_handle* h, uint32_t n_src, const pbw_sam_
   ka.key = k0;
   ka.val = v0;
   k_coord_keys<<<(unsigned)((n_sel + 255) / 256), 256, 0, st>>>(ka);
-  for (int p = 0; p < passes; p++) {
-    const int shift = 8 * p;
-    k_radix_hist<<<nb, RS_T, 0, st>>>(k0, n_sel, shift, hist, nb);
-    launch_scan_excl(hist, nh, nullptr, sums, nullptr, nullptr, st);
-    k_radix_scatter<<<nb, RS_T, 0, st>>>(k0, v0, n_sel, shift, hist, nb, k1, v1);
-    std::swap(k0, k1);
-    std::swap(v0, v1);
+  {
+    unsigned long long* kb[2] = {k0, k1};
+    unsigned long long* vb[2] = {v0, v1};
+    const int which = radix_sort_pairs(kb, vb, n_sel, 0, passes, hist, sums, st);
+    RCK(cudaGetLastError());
+    RCK(cudaMemcpyAsync(sorted, vb[which], n_sel * 8, cudaMemcpyDeviceToHost, st));
   }
-  RCK(cudaGetLastError());
-  RCK(cudaMemcpyAsync(sorted, v0, n_sel * 8, cudaMemcpyDeviceToHost, st));
   RCK(cudaStreamSynchronize(st));
 done:
   cudaStreamSynchronize(st);

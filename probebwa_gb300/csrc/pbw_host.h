@@ -39,4 +39,13 @@ uint64_t scan_blocks(uint64_t n);
 void launch_scan_excl(unsigned int* a, uint64_t n, unsigned int* out, unsigned int* block_sums, unsigned int* total,
                       const unsigned int* base_in, cudaStream_t st);
 
+// Stable LSD radix sort of n (key, value) pairs by key bits
+// [8 * first_digit, 8 * (first_digit + passes)). Input in k[0] / v[0]; the
+// passes ping-pong with k[1] / v[1]; returns the index of the buffers that
+// hold the result. hist holds radix_hist_entries(n) entries, sums
+// scan_blocks(radix_hist_entries(n)) + 2.
+uint64_t radix_hist_entries(uint64_t n);
+int radix_sort_pairs(unsigned long long* k[2], unsigned long long* v[2], uint64_t n, int first_digit, int passes,
+                     unsigned int* hist, unsigned int* sums, cudaStream_t st);
+
 }  // namespace pbw

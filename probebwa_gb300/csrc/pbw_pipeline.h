@@ -134,3 +134,8 @@ struct pbw_handle {
 namespace pbw {
 int pipeline_init(pbw_handle* h);
 }
+
+// GenomeIndex::load (src/index/genome.rs:80-86) of prefix.stidx into the
+// handle's device genome (2-bit words, N mask, contig bases and lengths) and
+// its contig names and lengths.
+int load_genome(pbw_handle* h, const std::string& prefix);
