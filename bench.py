@@ -333,6 +333,210 @@ def run_reference(args, prefix, d, meta):
             "e2e": {"value": round(v, 1), "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------------------
+# stages around the mapping path: index build, SAM output, the command line
+# ---------------------------------------------------------------------------
+def _stage_line(stage, meta, value, unit, extra):
+    out = {"stage": stage, "metric": f"{stage} throughput", "value": round(value, 3), "unit": unit, "n_gpus": 1,
+           "higher_is_better": True, "data": "synthetic (seeded)", "config": meta}
+    out.update(extra)
+    return out
+
+
+def _sha(path):
+    import hashlib
+    h = hashlib.sha256()
+    with open(path, "rb") as f:
+        for b in iter(lambda: f.read(1 << 24), b""):
+            h.update(b)
+    return h.hexdigest()
+
+
+def run_stage_index(args, prefix, meta):
+    """build-hash of the workload's genome: pbw_build_hash (GPU) against the
+    oracle's builder (one host thread); the two .sthash files must be equal."""
+    import probebwa_gb300 as P
+    from oracle import pyoracle as O
+    P.build()
+    O.build()
+    out = os.path.join(args.cache, "stage_index_gpu")
+    for _ in range(max(1, args.warmup)):
+        P.build_hash(prefix, out)
+    times = []
+    for _ in range(args.steps):
+        t = time.time()
+        P.build_hash(prefix, out)
+        times.append(time.time() - t)
+    ref = os.path.join(args.cache, "stage_index_cpu")
+    t = time.time()
+    O.build_hash(prefix, ref)
+    t_cpu = time.time() - t
+    same = _sha(out + ".sthash") == _sha(ref + ".sthash")
+    bp = meta["genome_bp"]
+    v = bp / statistics.mean(times)
+    return _stage_line("index", meta, v / 1e6, "Mbp/s", {
+        "wall_s": [round(x, 3) for x in times], "sthash_bytes": os.path.getsize(out + ".sthash"),
+        "parity": "sthash byte-identical to the oracle's" if same else "MISMATCH",
+        "timed": "whole pbw_build_hash call: .stidx read + upload, device build, table download, .sthash write",
+        "cpu_baseline": {"value": round(bp / t_cpu / 1e6, 3), "unit": "Mbp/s", "cores": 1, "kind": "port",
+                         "sample": "whole genome, oracle/ HashTableBuilder restatement"}})
+
+
+def _map_records(P, m, d, meta, opts):
+    import ctypes as C
+    R1 = P.Reads(d["b1"], d["q1"], d["o1"])
+    R2 = P.Reads(d["b2"], d["q2"], d["o2"]) if meta["paired"] else None
+    R1.ids = [f"p{i}" for i in range(R1.n)]
+    O1 = P.alloc_records(R1.n, len(R1.bases))
+    if R2 is not None:
+        R2.ids = R1.ids
+        O2 = P.alloc_records(R2.n, len(R2.bases))
+        mdl = P.InsertModelC(opts.insert_size_mean, opts.insert_size_sd, 0)
+        m._check(P.lib().pbw_map_paired(m.h, C.byref(mdl), C.byref(R1.c()), C.byref(R2.c()),
+                                        C.byref(P.records_c(O1)), C.byref(P.records_c(O2))))
+        return [(R1, O1), (R2, O2)]
+    m._check(P.lib().pbw_map_single(m.h, C.byref(R1.c()), C.byref(P.records_c(O1))))
+    return [(R1, O1)]
+
+
+def run_stage_sam(args, prefix, d, meta):
+    """SAM text of every record of one map call: pbw_sam_format (device
+    formatting, inputs up and text down inside the timing) against the
+    oracle's SAM writer on a sample."""
+    import ctypes as C
+    import probebwa_gb300 as P
+    from oracle import pyoracle as O
+    P.build()
+    O.build()
+    opts = P.MapperOptions()
+    m = P.Mapper(prefix, options=opts)
+    sources = _map_records(P, m, d, meta, opts)
+    arr, keep = m._sam_sources(sources)
+    so = P.SamOptionsC(b"probebwa map", None, 0)
+    n = C.c_uint64(0)
+    L = P.lib()
+    m._check(L.pbw_sam_format(m.h, C.byref(so), len(sources), arr, None, 0, None, 0, C.byref(n)))
+    buf = pinned(np.zeros(n.value, np.uint8))
+    n_rec = sum(len(o["contig"]) for _, o in sources)
+
+    def once():
+        m._check(L.pbw_sam_format(m.h, C.byref(so), len(sources), arr, None, 0, None, 0, C.byref(n)))
+        m._check(L.pbw_sam_format(m.h, C.byref(so), len(sources), arr, None, 0, _ptr_np(buf), buf.size, C.byref(n)))
+
+    for _ in range(max(1, args.warmup)):
+        once()
+    times = []
+    for _ in range(args.steps):
+        t = time.time()
+        once()
+        times.append(time.time() - t)
+    v = n_rec / statistics.mean(times)
+    # oracle on a sample of the records
+    k = min(100_000, len(sources[0][1]["contig"]))
+    om = O.Mapper(prefix)
+    sub = []
+    for R, rec in sources:
+        o = R.offsets[:k + 1]
+        Rs = O.Reads(R.bases[:int(o[-1])], R.quals[:int(o[-1])], o, R.ids[:k])
+        rs = {key: (val[:k] if key not in ("cigar_off", "cigar") else val) for key, val in rec.items()
+              if not key.startswith("_")}
+        rs["cigar_off"] = rec["cigar_off"][:k + 1]
+        sub.append((Rs, rs))
+    path = os.path.join(args.cache, "stage_sam_cpu.sam")
+    t = time.time()
+    text = om.sam_text(path, sub)
+    t_cpu = time.time() - t
+    gpu_sample = m.sam_text(sources, np.arange(k * len(sources), dtype=np.uint64))
+    om.close()
+    m.close()
+    return _stage_line("sam", meta, v, "records/s", {
+        "sam_bytes": int(n.value), "gb_per_s": round(n.value / statistics.mean(times) / 1e9, 3),
+        "wall_s": [round(x, 4) for x in times],
+        "parity": ("first %d records byte-identical to the oracle's SAM" % (k * len(sources)))
+        if gpu_sample == text else "MISMATCH",
+        "timed": "pbw_sam_format sizing + formatting calls: records, reads and IDs up, text down",
+        "cpu_baseline": {"value": round(k * len(sources) / t_cpu, 1), "unit": "records/s", "cores": 1, "kind": "port",
+                         "sample": f"first {k * len(sources)} records, oracle/ format_sam_records restatement"}})
+
+
+def _ptr_np(a):
+    return a.ctypes.data
+
+
+def _write_fastq(path, b, q, o, tag):
+    """Fixed-length reads as FASTQ with fixed-width IDs (Phred+33)."""
+    n = len(o) - 1
+    L = int(o[1] - o[0]) if n else 0
+    if n and not np.all(np.diff(o) == L):
+        raise ValueError("fixed-length reads expected")
+    ids = np.char.encode(np.char.add(f"@{tag}", np.char.zfill(np.arange(n).astype(str), 8)))
+    w = len(ids[0]) if n else 0
+    rec = np.empty((n, w + 1 + L + 3 + L + 1), np.uint8)
+    rec[:, :w] = np.frombuffer(b"".join(ids.tolist()), np.uint8).reshape(n, w)
+    rec[:, w] = 10
+    rec[:, w + 1:w + 1 + L] = b[:n * L].reshape(n, L)
+    rec[:, w + 1 + L:w + 4 + L] = np.frombuffer(b"\n+\n", np.uint8)
+    rec[:, w + 4 + L:w + 4 + 2 * L] = q[:n * L].reshape(n, L) + 33
+    rec[:, -1] = 10
+    with open(path, "wb") as f:
+        f.write(rec.tobytes())
+
+
+def run_stage_cli(args, prefix, d, meta):
+    """`probebwa map` end to end (process start, index load, FASTQ parse,
+    mapping, SAM written to a file) against the oracle's command line on a
+    sample of the same reads."""
+    import probebwa_gb300 as P
+    from oracle import pyoracle as O
+    from probebwa_gb300 import native_build
+    P.build()
+    O.build()
+    paired = meta["paired"]
+    files = [os.path.join(args.cache, f"stage_cli_r{m}.fq") for m in ((1, 2) if paired else (1,))]
+    for mate, fp in zip((1, 2), files):
+        if not os.path.exists(fp):
+            _write_fastq(fp, d[f"b{mate}"], d[f"q{mate}"], d[f"o{mate}"], "r")
+    n_reads = (len(d["o1"]) - 1) * len(files)
+    out = os.path.join(args.cache, "stage_cli_gpu.sam")
+    cmd = ["probebwa", "map", "-g", prefix, "-h", prefix, "-o", out, "-M", *files]
+    for _ in range(max(1, min(args.warmup, 1))):
+        subprocess.run(cmd, executable=native_build.CLI, check=True)
+    times = []
+    for _ in range(args.steps):
+        t = time.time()
+        subprocess.run(cmd, executable=native_build.CLI, check=True)
+        times.append(time.time() - t)
+    # the oracle's command line on the first k reads (pairs) of the same files
+    k = 20_000 if paired else 10_000
+    rec_len = os.path.getsize(files[0]) // (len(d["o1"]) - 1)
+    small = []
+    for fp in files:
+        sp = fp.replace(".fq", f".first{k}.fq")
+        if not os.path.exists(sp):
+            with open(fp, "rb") as f, open(sp, "wb") as g:
+                g.write(f.read(rec_len * k))
+        small.append(sp)
+    ref_out = os.path.join(args.cache, "stage_cli_cpu.sam")
+    threads = os.cpu_count() or 1
+    rcmd = ["probebwa", "map", "-g", prefix, "-h", prefix, "-t", str(threads), "-o", ref_out, "-M", *small]
+    t = time.time()
+    subprocess.run(rcmd, executable=O.CLI_PATH, check=True)
+    t_cpu = time.time() - t
+    gcmd = ["probebwa", "map", "-g", prefix, "-h", prefix, "-t", str(threads), "-o", ref_out + ".gpu", "-M", *small]
+    subprocess.run(gcmd, executable=native_build.CLI, check=True)
+    same = ([x for x in open(ref_out, "rb").read().split(b"\n") if not x.startswith(b"@PG")] ==
+            [x for x in open(ref_out + ".gpu", "rb").read().split(b"\n") if not x.startswith(b"@PG")])
+    v = n_reads / statistics.mean(times)
+    return _stage_line("cli", meta, v, "reads/s", {
+        "wall_s": [round(x, 2) for x in times], "sam_bytes": os.path.getsize(out),
+        "parity": (f"SAM of the first {k * len(files)} reads identical to the oracle CLI's (the @PG line, which "
+                   "echoes each argv, excluded)") if same else "MISMATCH",
+        "timed": "wall time of the whole command, index load included",
+        "cpu_baseline": {"value": round(k * len(files) / t_cpu, 1), "unit": "reads/s", "cores": threads,
+                         "kind": "port", "sample": f"oracle command line on the first {k * len(files)} reads "
+                                                   f"({'pairs' if paired else 'reads'}), index load included"}})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -343,6 +547,9 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="override read / pair count")
     ap.add_argument("--cache", default=os.environ.get("PBW_BENCH_CACHE", "/tmp/pbw_bench_cache"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stage", default="map", choices=["map", "index", "sam", "cli"],
+                    help="map: the mapping path (default); index / sam / cli: build-hash, SAM output and the "
+                         "command line, each against the oracle")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
@@ -352,6 +559,14 @@ def main():
             return
         prefix, d, meta = workload(args.config, args.cache, args.n)
         print(json.dumps(run_reference(args, prefix, d, meta)), flush=True)
+        return
+    if args.stage != "map":
+        if rank != 0:
+            return
+        prefix, d, meta = workload(args.config, args.cache, args.n)
+        fn = {"index": lambda: run_stage_index(args, prefix, meta), "sam": lambda: run_stage_sam(args, prefix, d, meta),
+              "cli": lambda: run_stage_cli(args, prefix, d, meta)}[args.stage]
+        print(json.dumps(fn()), flush=True)
         return
     if world > 1:
         import torch

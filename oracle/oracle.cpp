@@ -2431,6 +2431,9 @@ int cli_map(int argc, char** argv) {
   }
   std::string cl;
   for (int i = 0; i < argc; i++) cl += (i ? " " : "") + std::string(argv[i]);
+  // map_paired runs its batches on rayon's global pool (all cores) whatever
+  // --threads says (lib.rs:145-185); single-end honours --threads (lib.rs:97-104)
+  if (p.multi.size() == 2) o.threads = 0;
   std::unique_ptr<Mapper> m(new Mapper());
   if (!m->open(p.val["genome"], p.val["hash"], o)) throw std::runtime_error(g_err);
   const bool fasta = informat == "fasta";
