@@ -2,7 +2,8 @@
  *
  * Plain C types only: pointers, sizes and status codes. Every call returns
  * PBW_OK (0) or a negative PBW_ERR_* code; pbw_last_error(h) (or
- * pbw_last_error(NULL) for a failed pbw_open) describes the failure. No C++
+ * pbw_last_error(NULL) for a call without a handle, such as a failed
+ * pbw_open, on the calling thread) describes the failure. No C++
  * exception or CUDA error crosses this boundary.
  *
  * Each entry point names the reference interface it replaces
@@ -287,6 +288,53 @@ int pbw_build_genome(const char* out_prefix, const char* species, const char* as
  * (PBW_ERR_LIMIT). Errors are described by pbw_last_error(NULL). */
 int pbw_build_hash(const char* genome_prefix, const char* out_prefix, uint64_t k, uint64_t stride,
                    uint64_t max_count, int32_t device);
+
+/* Learned candidate ranker (no counterpart in the reference): a small MLP
+ * (12 seed features -> 64 -> 64 -> 1, BF16 weights, FP32 accumulation on the
+ * tensor cores) that scores each of a read's candidates before the seeded
+ * DP and prunes the ones it expects neither to win nor to enter the MAPQ
+ * posterior. Reads whose best score is below the threshold, or whose hits
+ * overflowed the per-read buffer, keep every candidate.
+ *
+ * pbw_ranker_train maps r1 (and r2 as mates, or NULL) once with the plain
+ * path, labels every aligned candidate (the read's select_best winner, or
+ * exp(lk - lk_max) >= 2^-60), trains the model on the GPU and sets the keep
+ * threshold so that `recall` of the positive training candidates is kept.
+ * pbw_ranker_enable switches pruning on or off for later map calls on the
+ * handle (and clears the counters); pbw_ranker_counters returns candidates
+ * kept and pruned and reads kept whole since then. pbw_ranker_export /
+ * pbw_ranker_import move a trained model (2*12 normalisation values, 5057
+ * weights, the threshold) between handles. */
+typedef struct {
+  uint32_t epochs;          /* passes over the training candidates (3) */
+  uint32_t batch;           /* candidates per Adam step (8192) */
+  double lr;                /* Adam learning rate (2e-3) */
+  double recall;            /* fraction of positive training candidates kept (0.9995) */
+  double positive_weight;   /* extra loss weight of positives over class balance (4) */
+  uint64_t seed;            /* weight initialisation */
+} pbw_ranker_train_options;
+
+typedef struct {
+  uint64_t samples;         /* aligned training candidates */
+  uint64_t positives;
+  double loss_first, loss_last;  /* mean weighted loss, first and last epoch */
+  double tau;               /* logit threshold */
+  double train_recall;      /* positives kept on the training candidates */
+  double train_prune;       /* negatives pruned on the training candidates */
+  double ms_collect, ms_train;
+} pbw_ranker_report;
+
+void pbw_ranker_default_options(pbw_ranker_train_options* o);
+int pbw_ranker_train(pbw_handle* h, const pbw_reads* r1, const pbw_reads* r2, const pbw_ranker_train_options* opt,
+                     pbw_ranker_report* rep);
+int pbw_ranker_enable(pbw_handle* h, int32_t on);
+int pbw_ranker_counters(pbw_handle* h, uint64_t* kept, uint64_t* pruned, uint64_t* reads_whole);
+int pbw_ranker_export(const pbw_handle* h, float* out, uint64_t cap, uint64_t* n);
+/* The trained model's logits for n caller feature rows (12 floats each, the
+ * layout above), on the tensor-core inference kernel: the stage entry point
+ * of the ranker. */
+int pbw_ranker_score(pbw_handle* h, const float* feat, uint64_t n, float* logit);
+int pbw_ranker_import(pbw_handle* h, const float* in, uint64_t n);
 
 /* Allocation-free window alignment. No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc -- code running while a stream is

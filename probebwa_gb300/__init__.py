@@ -70,6 +70,17 @@ class SamSourceC(C.Structure):
     _fields_ = [("reads", C.POINTER(ReadsC)), ("read_ids", C.POINTER(C.c_char_p)), ("recs", C.POINTER(RecordsC))]
 
 
+class RankerOptionsC(C.Structure):
+    _fields_ = [("epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_double), ("recall", C.c_double),
+                ("positive_weight", C.c_double), ("seed", C.c_uint64)]
+
+
+class RankerReportC(C.Structure):
+    _fields_ = [("samples", C.c_uint64), ("positives", C.c_uint64), ("loss_first", C.c_double),
+                ("loss_last", C.c_double), ("tau", C.c_double), ("train_recall", C.c_double),
+                ("train_prune", C.c_double), ("ms_collect", C.c_double), ("ms_train", C.c_double)]
+
+
 class InsertModelC(C.Structure):
     _fields_ = [("mean", C.c_double), ("sd", C.c_double), ("n_observed", C.c_uint64)]
 
@@ -135,6 +146,14 @@ def lib():
         L.pbw_sam_format.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, vp, u64, vp]
         L.pbw_sort_coordinate.argtypes = [vp, u32, C.POINTER(SamSourceC), vp, u64, vp]
         L.pbw_build_genome.argtypes = [cp, cp, cp, u32, C.POINTER(cp)]
+        L.pbw_ranker_default_options.argtypes = [C.POINTER(RankerOptionsC)]
+        L.pbw_ranker_train.argtypes = [vp, C.POINTER(ReadsC), C.POINTER(ReadsC), C.POINTER(RankerOptionsC),
+                                       C.POINTER(RankerReportC)]
+        L.pbw_ranker_enable.argtypes = [vp, C.c_int32]
+        L.pbw_ranker_counters.argtypes = [vp, vp, vp, vp]
+        L.pbw_ranker_export.argtypes = [vp, vp, u64, vp]
+        L.pbw_ranker_import.argtypes = [vp, vp, u64]
+        L.pbw_ranker_score.argtypes = [vp, vp, u64, vp]
         L.pbw_build_hash.argtypes = [cp, cp, u64, u64, u64, C.c_int32]
         if hasattr(L, "pbw_align_noalloc"):
             L.pbw_align_noalloc.argtypes = [u64, vp, vp, vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, u32, vp]
@@ -471,6 +490,43 @@ class Mapper:
         self._check(lib().pbw_sort_coordinate(self.h, len(sources), arr, _ptr(sel) if sel.size else None,
                                               int(sel.size), _ptr(out)))
         return out[:sel.size]
+
+    def ranker_train(self, r1: Reads, r2: Reads | None = None, **kw) -> dict:
+        """Trains the candidate ranker on these reads (pairs when r2 is given)
+        with labels from the plain path; returns the training report."""
+        o = RankerOptionsC()
+        lib().pbw_ranker_default_options(C.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        rep = RankerReportC()
+        c2 = C.byref(r2.c()) if r2 is not None else None
+        self._check(lib().pbw_ranker_train(self.h, C.byref(r1.c()), c2, C.byref(o), C.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in RankerReportC._fields_}
+
+    def ranker_enable(self, on: bool = True):
+        self._check(lib().pbw_ranker_enable(self.h, 1 if on else 0))
+
+    def ranker_counters(self) -> dict:
+        v = [C.c_uint64(0) for _ in range(3)]
+        self._check(lib().pbw_ranker_counters(self.h, *[C.byref(x) for x in v]))
+        return {"kept": v[0].value, "pruned": v[1].value, "reads_whole": v[2].value}
+
+    def ranker_export(self) -> np.ndarray:
+        n = C.c_uint64(0)
+        self._check(lib().pbw_ranker_export(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        self._check(lib().pbw_ranker_export(self.h, _ptr(out), n.value, C.byref(n)))
+        return out
+
+    def ranker_import(self, model: np.ndarray):
+        model = np.ascontiguousarray(model, dtype=np.float32)
+        self._check(lib().pbw_ranker_import(self.h, _ptr(model), model.size))
+
+    def ranker_score(self, feat: np.ndarray) -> np.ndarray:
+        feat = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, 12)
+        out = np.zeros(max(len(feat), 1), np.float32)
+        self._check(lib().pbw_ranker_score(self.h, _ptr(feat) if len(feat) else None, len(feat), _ptr(out)))
+        return out[:len(feat)]
 
     def mapq_batch(self, reads: Reads, items) -> dict:
         """MapqCalculator::select_best + finalize_mapq (bayesian.rs:193-201,

@@ -18,6 +18,7 @@
 // print "Error: ..." and exit 1. build-genome / build-hash write the same
 // index files as the reference's subcommands (the hash table is built on the
 // GPU).
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -26,6 +27,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/probebwa_gpu.h"
@@ -187,6 +189,19 @@ void check_read_group(const std::string& spec) {
   if (!id) throw Fail("--readgroup must set at least an ID tag");
 }
 
+// Phase wall times on stderr when PROBEBWA_TIMING is set (no effect on output).
+struct Timer {
+  const char* what;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  explicit Timer(const char* w) : what(w) {}
+  ~Timer() {
+    static const bool on = getenv("PROBEBWA_TIMING") != nullptr;
+    if (on)
+      fprintf(stderr, "[probebwa] %s: %.3f s\n", what,
+              std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+  }
+};
+
 // ---- reads and records ----
 struct ReadFile {
   pbw_read_set* rs = nullptr;
@@ -257,13 +272,6 @@ struct Records {
   }
 };
 
-void load(const std::string& path, bool fasta, uint8_t qoff, const char* adapter, Reads& into) {
-  ReadFile* f = new ReadFile();
-  into.files.push_back(f);
-  if (pbw_reads_load(path.c_str(), fasta ? 1 : 0, qoff, adapter, &f->rs) != PBW_OK) throw Fail(pbw_last_error(nullptr));
-  pbw_reads_get(f->rs, &f->view);
-}
-
 struct Handle {
   pbw_handle* h = nullptr;
   ~Handle() { pbw_close(h); }
@@ -295,19 +303,42 @@ int run_map(int argc, char** argv) {
   std::string cl;
   for (int i = 0; i < argc; i++) cl += (i ? " " : "") + std::string(argv[i]);
 
-  Handle H;
-  if (pbw_open(a.get("genome", "").c_str(), a.get("hash", "").c_str(), &o, &H.h) != PBW_OK)
-    throw Fail(pbw_last_error(nullptr));
+  // The index load (pbw_open) and the read files are independent: they run on
+  // their own threads, then mapping starts.
   const bool fasta = informat == "fasta";
   const std::string adapter = a.get("adapter-strip", "");
   const char* ad = a.has("adapter-strip") ? adapter.c_str() : nullptr;
   const bool paired = a.reads.size() == 2;
   const uint32_t n_src = paired ? 2 : 1;
+  Handle H;
   Reads R[2];
   Records S[2];
+  std::vector<ReadFile*> files(a.reads.size(), nullptr);
+  for (auto& f : files) f = new ReadFile();
+  for (size_t i = 0; i < files.size(); i++) R[paired ? i : 0].files.push_back(files[i]);
+  std::vector<int> load_rc(files.size(), PBW_OK);
+  std::vector<std::string> load_err(files.size());
+  int open_rc = PBW_OK;
+  std::string open_err;
+  {
+    Timer tm("load (index + reads, concurrent)");
+    std::vector<std::thread> th;
+    th.emplace_back([&] {
+      open_rc = pbw_open(a.get("genome", "").c_str(), a.get("hash", "").c_str(), &o, &H.h);
+      if (open_rc != PBW_OK) open_err = pbw_last_error(nullptr);
+    });
+    for (size_t i = 0; i < files.size(); i++)
+      th.emplace_back([&, i] {
+        load_rc[i] = pbw_reads_load(a.reads[i].c_str(), fasta ? 1 : 0, qoff, ad, &files[i]->rs);
+        if (load_rc[i] == PBW_OK) pbw_reads_get(files[i]->rs, &files[i]->view);
+        else load_err[i] = pbw_last_error(nullptr);
+      });
+    for (auto& t : th) t.join();
+  }
+  if (open_rc != PBW_OK) throw Fail(open_err);
+  for (size_t i = 0; i < files.size(); i++)
+    if (load_rc[i] != PBW_OK) throw Fail(load_err[i]);
   if (paired) {
-    load(a.reads[0], fasta, qoff, ad, R[0]);
-    load(a.reads[1], fasta, qoff, ad, R[1]);
     R[0].finish();
     R[1].finish();
     if (R[0].n() != R[1].n())
@@ -316,11 +347,12 @@ int run_map(int argc, char** argv) {
     S[0].alloc(R[0].view);
     S[1].alloc(R[1].view);
     pbw_insert_model m{o.insert_size_mean, o.insert_size_sd, 0};
+    Timer tm("map (pairs)");
     H.check(pbw_map_paired(H.h, &m, &R[0].view, &R[1].view, &S[0].view, &S[1].view));
   } else {
-    for (const std::string& f : a.reads) load(f, fasta, qoff, ad, R[0]);
     R[0].finish();
     S[0].alloc(R[0].view);
+    Timer tm("map (single-end)");
     H.check(pbw_map_single(H.h, &R[0].view, &S[0].view));
   }
   // --labelfilter (main.rs:158-160)
@@ -344,6 +376,7 @@ int run_map(int argc, char** argv) {
   if (outformat == "bam") throw Fail("BAM output is not built (SAM only)");
   pbw_sam_options so{cl.c_str(), have_rg ? rg.c_str() : nullptr, index ? 1 : 0};
   const uint64_t none = 0;  // an empty selection still passes a list (NULL means every record)
+  Timer tm("SAM (format on the GPU + write)");
   H.check(pbw_sam_write(H.h, &so, n_src, src, sel.empty() ? &none : sel.data(), sel.size(),
                         a.get("output", "-").c_str()));
   return 0;

@@ -26,7 +26,7 @@
 
 using namespace pbw;
 
-static std::string g_open_err;
+static thread_local std::string g_open_err;  // per thread: loaders may run concurrently
 
 namespace pbw {
 // Errors of calls without a handle (a failed pbw_open, handle-free entry

@@ -139,7 +139,7 @@ size_t cluster_smem(uint32_t hmax, int threads) {
 // NP = next_pow2(H) or more elements.
 __device__ void cluster_read(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
                              unsigned char* base, uint32_t NP, uint32_t* wtmp32, unsigned long long* wtmp64,
-                             uint32_t& sh_G, uint32_t& sh_C) {
+                             uint32_t& sh_G, uint32_t& sh_C, bool list_mode) {
   unsigned long long* keys = (unsigned long long*)base;
   unsigned long long* pre = keys + NP;           // NP + 1
   uint32_t* vals = (uint32_t*)(pre + NP + 1);
@@ -160,6 +160,12 @@ __device__ void cluster_read(const ClusterArgs& p, uint32_t r, uint32_t H, const
   }
   __syncthreads();
   bitonic_kv(keys, vals, n);
+  if (p.sorted_hits && !list_mode) {
+    for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+      p.sorted_hits[(size_t)r * p.hcap + i] = keys[i];
+      p.hit_src[(size_t)r * p.hcap + i] = (uint16_t)vals[i];
+    }
+  }
   // boundaries
   for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
     unsigned long long k = keys[i];
@@ -297,7 +303,9 @@ __device__ void cluster_read(const ClusterArgs& p, uint32_t r, uint32_t H, const
     cd.contig = gk >> 1;
     cd.strand = (uint8_t)(gk & 1u);
     cd.score = cnt;
+    cd.pad[0] = 1;
     p.cand[(size_t)r * p.max_out + i] = cd;
+    if (p.cand_span) p.cand_span[(size_t)r * p.max_out + i] = list_mode ? 0xFFFFFFFFu : (s | (e << 16));
   }
   if (threadIdx.x == 0) {
     p.n_cand[r] = nout;
@@ -322,7 +330,7 @@ __global__ void k_cluster(ClusterArgs p, uint32_t np_max) {
       }
       continue;
     }
-    cluster_read(p, r, H, p.hits + (size_t)r * p.hcap, smem_raw, np_max, wtmp32, wtmp64, sh_G, sh_C);
+    cluster_read(p, r, H, p.hits + (size_t)r * p.hcap, smem_raw, np_max, wtmp32, wtmp64, sh_G, sh_C, false);
   }
 }
 
@@ -337,7 +345,7 @@ __global__ void k_cluster_list(ClusterArgs p) {
     const uint32_t H = p.need[r];
     const unsigned long long off = p.list_hoff[w];
     uint32_t NP = next_pow2(H);
-    cluster_read(p, r, H, p.hits_pool + off, p.scratch + 2 * off * 56, NP, wtmp32, wtmp64, sh_G, sh_C);
+    cluster_read(p, r, H, p.hits_pool + off, p.scratch + 2 * off * 56, NP, wtmp32, wtmp64, sh_G, sh_C, true);
   }
 }
 

@@ -74,14 +74,20 @@ size_t adapter_keep(const uint8_t* seq, size_t rl, const std::string& ad) {
 
 // Appends one read: bases upper-cased, the quality track cut or padded to the
 // (possibly adapter-trimmed) sequence length.
-void push_read(pbw_read_set* rs, const std::vector<uint8_t>& seq, const std::vector<uint8_t>& qual, const char* adapter) {
-  size_t keep = seq.size();
-  if (adapter) keep = adapter_keep(seq.data(), seq.size(), adapter);
-  for (size_t t = 0; t < keep; t++) {
-    rs->bases.push_back(upper(seq[t]));
-    rs->quals.push_back(t < qual.size() ? qual[t] : (uint8_t)30);
-  }
-  rs->offsets.push_back(rs->bases.size());
+void push_read(pbw_read_set* rs, const std::vector<uint8_t>& seq, const std::vector<uint8_t>& qual,
+               const std::string* adapter) {
+  const size_t n = seq.size();
+  const size_t keep = adapter ? adapter_keep(seq.data(), n, *adapter) : n;
+  const size_t b0 = rs->bases.size();
+  rs->bases.resize(b0 + keep);
+  rs->quals.resize(b0 + keep);
+  uint8_t* ob = rs->bases.data() + b0;
+  uint8_t* oq = rs->quals.data() + b0;
+  for (size_t t = 0; t < keep; t++) ob[t] = upper(seq[t]);
+  const size_t m = std::min(keep, qual.size());
+  if (m) memcpy(oq, qual.data(), m);
+  if (keep > m) memset(oq + m, 30, keep - m);
+  rs->offsets.push_back(b0 + keep);
 }
 
 }  // namespace
@@ -103,6 +109,11 @@ int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const ch
     return lrc;
   }
   pbw_read_set* rs = new pbw_read_set();
+  // sequence bytes are at most half of a FASTQ file, at most all of a FASTA one
+  rs->bases.reserve(fasta ? buf.size() : buf.size() / 2 + 64);
+  rs->quals.reserve(rs->bases.capacity());
+  const std::string ad_s = adapter ? adapter : "";
+  const std::string* ad = adapter ? &ad_s : nullptr;
   Builder bld{rs};
   Lines L{buf.data(), buf.data() + buf.size()};
   Span line;
@@ -119,13 +130,16 @@ int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const ch
       }
       while (L.next(line)) {
         const Span t = trim(line);
+        const size_t q0 = qual.size();
+        qual.resize(q0 + t.n);
+        uint8_t* o = qual.data() + q0;
         for (size_t k = 0; k < t.n; k++) {
           const uint8_t c = (uint8_t)t.p[k];
-          qual.push_back(c > quality_offset ? (uint8_t)(c - quality_offset) : (uint8_t)0);
+          o[k] = c > quality_offset ? (uint8_t)(c - quality_offset) : (uint8_t)0;
         }
         if (qual.size() >= seq.size()) break;
       }
-      push_read(rs, seq, qual, adapter);
+      push_read(rs, seq, qual, ad);
     }
   } else {
     bool have = false;
@@ -151,7 +165,7 @@ int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const ch
         seq.insert(seq.end(), (const uint8_t*)t.p, (const uint8_t*)t.p + t.n);
       }
       qual.assign(seq.size(), 40);
-      push_read(rs, seq, qual, adapter);
+      push_read(rs, seq, qual, ad);
       if (!have) break;
     }
   }

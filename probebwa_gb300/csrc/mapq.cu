@@ -23,6 +23,7 @@ __global__ void k_make_jobs_single(MakeJobsArgs p) {
     const Cand c = p.cand[(size_t)r * MAX_CAND + i];
     const uint32_t slot = r * MAX_CAND + i;
     p.out[slot].n_ops = 0;  // marks a skipped candidate
+    if (p.prune && !c.pad[0]) continue;  // pruned by the candidate ranker
     const unsigned long long clen = p.G.clen[c.contig];
     // left pad 10, right pad max(max_indel_len, 10) (single.rs:109-118)
     const unsigned long long rs = c.pos >= 10 ? c.pos - 10 : 0;

@@ -21,6 +21,7 @@ struct MakeJobsArgs {
   unsigned int* n_jobs;
   AlnOut* out;
   uint8_t mate;             // read set of the jobs (AlnJob::mate)
+  uint8_t prune;            // skip candidates whose Cand::pad[0] (ranker keep flag) is 0
 };
 
 struct CigarGatherArgs {

@@ -26,6 +26,7 @@ struct SeedArgs {
   uint8_t* rep;             // nr * wcap: 0 none, 1 neighbour repetitive, 2 exact repetitive
   uint32_t wcap;
   uint16_t* hit_rpos;       // optional nr * hcap read positions (parity tests)
+  uint16_t* hit_info;       // optional nr * hcap: read position | log2 exact bucket << 10 | neighbour << 15
   unsigned long long* counters;  // probes, entries, hits
   // overflow handling: reads with more than hcap hits are queued with their
   // exact hit count and seeded again in list mode into a pool
@@ -73,6 +74,11 @@ struct ClusterArgs {
   const unsigned long long* hits_pool;
   const uint32_t* need;
   unsigned char* scratch;   // 2 * 56 bytes per pooled hit
+  // optional, for the candidate ranker: sorted hits written back in place,
+  // their emission slots, and each kept candidate's range in that order
+  unsigned long long* sorted_hits;  // nr * hcap (the hits array itself)
+  uint16_t* hit_src;                // nr * hcap
+  uint32_t* cand_span;              // nr * max_out: first | end << 16; 0xFFFFFFFF for list-mode reads
 };
 size_t cluster_smem(uint32_t hmax, int threads);
 void launch_cluster(const ClusterArgs& a, uint32_t hmax, int threads, cudaStream_t st);

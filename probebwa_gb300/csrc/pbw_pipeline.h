@@ -121,6 +121,23 @@ struct pbw_handle {
   pbw::DevBuf<pbw::PairModel> d_model;
   pbw::DevBuf<double> d_obs;
   pbw::DevBuf<pbw::AlnJob> d_xjobs;
+  // learned candidate ranker (ranker.cu): model, per-chunk scratch and the
+  // training-data collection of pbw_ranker_train
+  struct Ranker {
+    bool trained = false;
+    bool enabled = false;     // prune candidates in map calls
+    bool collect = false;     // write features and labels of every slot (plain path)
+    float tau = 0.f;          // keep a candidate whose logit >= tau
+    pbw::DevBuf<float> d_norm, d_w, d_m, d_v, d_g, d_loss;
+    pbw::DevBuf<uint32_t> d_wb;
+    pbw::DevBuf<uint16_t> d_hit_info, d_hit_src;
+    pbw::DevBuf<uint32_t> d_span;
+    pbw::DevBuf<float> d_feat, d_logit;               // 2 read sets x chunk slots
+    pbw::DevBuf<unsigned long long> d_counters;       // kept, pruned, reads kept whole
+    pbw::DevBuf<float> c_feat;                        // collection: slot-indexed
+    pbw::DevBuf<uint8_t> c_label;
+    uint64_t c_slots = 0;                             // slots per read set in the collection
+  } rk;
   pbw::HostBuf h_stage;
   pbw::HostBuf h_fold;  // one batch's insert-size observations + the model
   std::vector<cudaEvent_t> events;

@@ -12,6 +12,7 @@
 #include "pbw_kernels.h"
 #include "pbw_pipeline.h"
 #include "paired.h"
+#include "ranker.h"
 
 namespace pbw {
 
@@ -153,15 +154,37 @@ struct MateBufs {
   uint8_t mate;
 };
 
-// K1 -> K2 -> jobs -> K3 for reads [r0, r0+nr) of one read set. Events
-// ev[0..3] mark seed / cluster / align boundaries. reset_pool clears the
-// CIGAR pool (the first read set of a chunk).
-static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
-                          const uint64_t* offs, uint32_t r0, uint32_t nr, const MateBufs& mb,
-                          cudaEvent_t* ev, bool reset_pool) {
+// Ranker buffers of one chunk (ranked or collecting map calls).
+static int ensure_ranker_chunk(pbw_handle* h, const ChunkCfg& c) {
+  TRY(grow(h, h->rk.d_hit_info, (size_t)c.ch * c.hcap));
+  TRY(grow(h, h->rk.d_hit_src, (size_t)c.ch * c.hcap));
+  TRY(grow(h, h->rk.d_span, (size_t)c.ch * MAX_CAND));
+  TRY(grow(h, h->rk.d_feat, 2 * (size_t)c.ch * MAX_CAND * RK_F));
+  TRY(grow(h, h->rk.d_logit, 2 * (size_t)c.ch * MAX_CAND));
+  TRY(grow(h, h->rk.d_counters, 4));
+  return PBW_OK;
+}
+
+// Where read set `mate` of a chunk keeps its candidate features: the chunk
+// scratch when ranking, the slot-indexed collection when collecting, none
+// otherwise.
+static float* rank_feat(pbw_handle* h, uint32_t ch, int mate, uint32_t r0) {
+  if (h->rk.collect) return h->rk.c_feat.p + ((size_t)mate * h->rk.c_slots + (size_t)r0 * MAX_CAND) * RK_F;
+  if (h->rk.enabled) return h->rk.d_feat.p + (size_t)mate * ch * MAX_CAND * RK_F;
+  return nullptr;
+}
+static uint8_t* rank_label(pbw_handle* h, int mate, uint32_t r0) {
+  return h->rk.collect ? h->rk.c_label.p + (size_t)mate * h->rk.c_slots + (size_t)r0 * MAX_CAND : nullptr;
+}
+
+// K1 -> K2 for reads [r0, r0+nr) of one read set; with feat, also the
+// ranker's hit-level candidate features. Events ev[0..2] mark the start and
+// the seed / cluster boundaries.
+static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
+                        const uint64_t* offs, uint32_t r0, uint32_t nr, const MateBufs& mb, cudaEvent_t* ev,
+                        float* feat) {
   cudaStream_t st = h->st;
   unsigned int* c32 = h->d_cnt32.p;
-  CK(cudaMemsetAsync(c32, 0, (reset_pool ? 3 : 2) * sizeof(unsigned int), st));  // n_jobs, next_job[, cig_pool_used]
   CK(cudaMemsetAsync(mb.n_cand, 0, nr * sizeof(uint32_t), st));
   CK(cudaEventRecord(ev[0], st));
   SeedArgs sa{};
@@ -180,6 +203,7 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   sa.rep = mb.rep;
   sa.wcap = cfg.wcap;
   sa.hit_rpos = nullptr;
+  sa.hit_info = feat ? h->rk.d_hit_info.p : nullptr;
   sa.counters = h->d_cnt64.p;
   sa.need = h->d_need.p;
   sa.ovf_list = h->d_ovf_list.p;
@@ -219,6 +243,11 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   ca.n_cand = mb.n_cand;
   ca.total_cand = h->d_total_cand.p;
   ca.err = h->d_err.p;
+  if (feat) {
+    ca.sorted_hits = h->d_hits.p;
+    ca.hit_src = h->rk.d_hit_src.p;
+    ca.cand_span = h->rk.d_span.p;
+  }
   ca.h_lo = 0;
   ca.h_hi = 512;
   launch_cluster(ca, 512, 64, st);
@@ -233,8 +262,65 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   ca.scratch = h->d_cl_scratch.p;
   launch_cluster_list(ca, h->num_sms, st);
   h->stats.kernel_launches += 1;
+  if (feat) {
+    RankFeatArgs fa{};
+    fa.hits = h->d_hits.p;
+    fa.hit_src = h->rk.d_hit_src.p;
+    fa.hit_info = h->rk.d_hit_info.p;
+    fa.hcap = cfg.hcap;
+    fa.cand = mb.cand;
+    fa.n_cand = mb.n_cand;
+    fa.span = h->rk.d_span.p;
+    fa.quals = quals;
+    fa.offs = offs;
+    fa.r0 = r0;
+    fa.nr = nr;
+    fa.feat = feat;
+    launch_rank_features(fa, h->num_sms * 8, st);
+    h->stats.kernel_launches += 1;
+  }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[2], st));
+  return PBW_OK;
+}
+
+// Keep flags of one read set's candidates from the trained model.
+static void rank_decide(pbw_handle* h, const float* feat, float* logit, const MateBufs& mb, uint32_t nr) {
+  RankModelDev md{h->rk.d_norm.p, h->rk.d_wb.p, h->rk.d_w.p};
+  launch_rank_infer(feat, (uint64_t)nr * MAX_CAND, md, logit, h->num_sms * 8, h->st);
+  RankDecideArgs da{};
+  da.logit = logit;
+  da.feat = feat;
+  da.cand = mb.cand;
+  da.n_cand = mb.n_cand;
+  da.nr = nr;
+  da.tau = h->rk.tau;
+  da.counters = h->rk.d_counters.p;
+  launch_rank_decide(da, h->st);
+  h->stats.kernel_launches += 2;
+}
+
+// Mate-consistency features of both read sets of a chunk of pairs.
+static void rank_mate_features(pbw_handle* h, const MateBufs& m1, const MateBufs& m2, const uint64_t* of1,
+                               const uint64_t* of2, uint32_t r0, uint32_t nr, float* f1, float* f2, double mean,
+                               double sd) {
+  RankMateArgs ma{m1.cand, m1.n_cand, of1, m2.cand, m2.n_cand, of2, r0, nr, mean, sd, f1};
+  launch_rank_mate(ma, h->st);
+  RankMateArgs mb{m2.cand, m2.n_cand, of2, m1.cand, m1.n_cand, of1, r0, nr, mean, sd, f2};
+  launch_rank_mate(mb, h->st);
+  h->stats.kernel_launches += 2;
+}
+
+// Candidates -> jobs -> K3 -> alignment statistics for one read set (with
+// the keep flags when prune), and the training labels when labels is set.
+// ev[3] marks the end. reset_pool clears the CIGAR pool (the first read set
+// of a chunk).
+static int align_candidates(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
+                            const uint64_t* offs, uint32_t r0, uint32_t nr, const MateBufs& mb, cudaEvent_t* ev,
+                            bool reset_pool, bool prune, uint8_t* labels) {
+  cudaStream_t st = h->st;
+  unsigned int* c32 = h->d_cnt32.p;
+  CK(cudaMemsetAsync(c32, 0, (reset_pool ? 3 : 2) * sizeof(unsigned int), st));  // n_jobs, next_job[, cig_pool_used]
   MakeJobsArgs ma{};
   ma.G = h->G;
   ma.offs = offs;
@@ -250,6 +336,7 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
   ma.n_jobs = c32 + 0;
   ma.out = mb.aln;
   ma.mate = 0;
+  ma.prune = prune ? 1 : 0;
   launch_make_jobs_single(ma, st);
   AlignArgs aa{};
   aa.G = h->G;
@@ -285,10 +372,27 @@ static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bas
     launch_align_window(aa, window_grid(h), st);
   }
   launch_aln_stats(aa, (uint64_t)nr * MAX_CAND, st);
+  if (labels) {
+    RankLabelArgs la{mb.aln, mb.n_cand, nr, labels};
+    launch_rank_label(la, st);
+    h->stats.kernel_launches += 1;
+  }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[3], st));
-  h->stats.kernel_launches += 7;
+  h->stats.kernel_launches += 4;
   return PBW_OK;
+}
+
+// K1 -> K2 -> [ranker] -> jobs -> K3 for reads [r0, r0+nr) of one read set
+// (the single-end chunk; pairs run the halves separately when ranking).
+static int run_seed_align(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
+                          const uint64_t* offs, uint32_t r0, uint32_t nr, const MateBufs& mb,
+                          cudaEvent_t* ev, bool reset_pool) {
+  float* feat = rank_feat(h, cfg.ch, 0, r0);
+  TRY(seed_cluster(h, cfg, bases, quals, offs, r0, nr, mb, ev, feat));
+  const bool prune = h->rk.enabled && !h->rk.collect;
+  if (prune) rank_decide(h, feat, h->rk.d_logit.p, mb, nr);
+  return align_candidates(h, cfg, bases, quals, offs, r0, nr, mb, ev, reset_pool, prune, rank_label(h, 0, r0));
 }
 
 // One chunk of single-end reads: seeding through finalize and CIGAR gather.
@@ -424,6 +528,7 @@ static int map_single_dev(pbw_handle* h, const uint8_t* d_bases, const uint8_t* 
                           uint64_t n, uint64_t total_bases, int lmax, pbw_records* out) {
   ChunkCfg cfg = chunk_cfg(h, n, lmax);
   TRY(ensure_chunk(h, cfg));
+  if (h->rk.enabled || h->rk.collect) TRY(ensure_ranker_chunk(h, cfg));
   TRY(ensure_outputs(h, std::max<uint64_t>(n, 1), 2 * total_bases + 2 * n + 16));
   CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * sizeof(unsigned int), h->st));
   CK(cudaMemsetAsync(h->d_cnt64.p, 0, 16 * sizeof(unsigned long long), h->st));
@@ -503,6 +608,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   ChunkCfg cfg = chunk_cfg(h, std::min<uint64_t>(n, S), lmax);
   cfg.ch = (uint32_t)std::min<uint64_t>(n, S);
   TRY(ensure_chunk(h, cfg));
+  if (h->rk.enabled || h->rk.collect) TRY(ensure_ranker_chunk(h, cfg));
   const uint32_t ch = cfg.ch;
   TRY(grow(h, h->d_cand2, (size_t)ch * MAX_CAND));
   TRY(grow(h, h->d_n_cand2, ch));
@@ -556,16 +662,39 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     // phase A: both mates through K1-K3 and the per-read summaries
     MateBufs m1{h->d_cand.p, h->d_n_cand.p, h->d_aln.p, h->d_rep.p, 0};
     MateBufs m2{h->d_cand2.p, h->d_n_cand2.p, h->d_aln2.p, h->d_rep2.p, 0};
-    TRY(run_seed_align(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, true));
-    CK(cudaEventSynchronize(ev[3]));
-    t_seed += ms_between(ev[0], ev[1]);
-    t_cl += ms_between(ev[1], ev[2]);
-    t_al += ms_between(ev[2], ev[3]);
-    TRY(run_seed_align(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev, false));
-    CK(cudaEventSynchronize(ev[3]));
-    t_seed += ms_between(ev[0], ev[1]);
-    t_cl += ms_between(ev[1], ev[2]);
-    t_al += ms_between(ev[2], ev[3]);
+    if (!(h->rk.enabled || h->rk.collect)) {
+      TRY(run_seed_align(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, true));
+      CK(cudaEventSynchronize(ev[3]));
+      t_seed += ms_between(ev[0], ev[1]);
+      t_cl += ms_between(ev[1], ev[2]);
+      t_al += ms_between(ev[2], ev[3]);
+      TRY(run_seed_align(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev, false));
+      CK(cudaEventSynchronize(ev[3]));
+      t_seed += ms_between(ev[0], ev[1]);
+      t_cl += ms_between(ev[1], ev[2]);
+      t_al += ms_between(ev[2], ev[3]);
+    } else {
+      // ranker: both read sets' candidates first (the mate features need
+      // both), then pruning and the seeded DP of each read set
+      cudaEvent_t* ev2 = &h->events[10];
+      float* f1 = rank_feat(h, ch, 0, (uint32_t)a);
+      float* f2 = rank_feat(h, ch, 1, (uint32_t)a);
+      TRY(seed_cluster(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, f1));
+      TRY(seed_cluster(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev2, f2));
+      rank_mate_features(h, m1, m2, of1, of2, (uint32_t)a, nr, f1, f2, h_pm->mean, h_pm->sd);
+      const bool prune = h->rk.enabled && !h->rk.collect;
+      if (prune) {
+        rank_decide(h, f1, h->rk.d_logit.p, m1, nr);
+        rank_decide(h, f2, h->rk.d_logit.p + (size_t)ch * MAX_CAND, m2, nr);
+      }
+      TRY(align_candidates(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, true, prune, rank_label(h, 0, (uint32_t)a)));
+      TRY(align_candidates(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev2, false, prune,
+                           rank_label(h, 1, (uint32_t)a)));
+      CK(cudaEventSynchronize(ev2[3]));
+      t_seed += ms_between(ev[0], ev[1]) + ms_between(ev2[0], ev2[1]);
+      t_cl += ms_between(ev[1], ev[2]) + ms_between(ev2[1], ev2[2]);
+      t_al += ms_between(ev2[2], ev2[3]);
+    }
     CK(cudaEventRecord(ev[0], st));
     for (int mate = 0; mate < 2; mate++) {
       ReadSummaryArgs ra{};

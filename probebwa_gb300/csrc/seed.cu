@@ -261,6 +261,12 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
           if (slot < hcap) {
             hits[slot] = word;
             if (p.hit_rpos && !list_mode) p.hit_rpos[(size_t)r * p.hcap + slot] = (uint16_t)s_w;
+            if (p.hit_info && !list_mode) {
+              const uint32_t wc = wcnt[s_w];
+              const uint32_t l2 = min(32u - (uint32_t)__clz(wc), 31u);
+              p.hit_info[(size_t)r * p.hcap + slot] =
+                  (uint16_t)(((uint32_t)s_w & 0x3FFu) | (l2 << 10) | (s_nb ? 0x8000u : 0u));
+            }
           }
           n_hit++;
         }

@@ -85,7 +85,7 @@ def build_cli() -> str:
     if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(p) for p in deps):
         return CLI
     cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", "-o", CLI, CLI_SRC, "-L" + LIBDIR,
-           "-lprobebwa_gb300", "-Wl,-rpath,$ORIGIN"]
+           "-lprobebwa_gb300", "-Wl,-rpath,$ORIGIN", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
