@@ -212,6 +212,9 @@ def run_gpu(args, prefix, d, meta, rank, world):
     torch.cuda.synchronize()
     t_wall = time.time() - t_wall
     clocks = clk.stop()
+    ranked = None
+    if args.ranked and paired and world == 1:
+        ranked = run_ranked(args, m, opts, step, O1, O2, meta, n_reads, dev)
     # device time of a step: the pipeline's CUDA events, without the input copy
     dev_ms = [s["ms_seed"] + s["ms_cluster"] + s["ms_align"] + s["ms_pair"] + s["ms_finalize"] + s["ms_d2h"]
               for s in stats]
@@ -279,7 +282,90 @@ def run_gpu(args, prefix, d, meta, rank, world):
         "dp_gcups": round(gcups, 2), "dp_cells_per_step": int(s0["dp_cells"]), "dp_jobs_per_step": int(s0["dp_jobs"]),
         "roofline": roofline, "roofline_dp": roofline_dp, "clocks": clocks, "wall_s_timed": round(t_wall, 3),
     }
+    if ranked is not None:
+        ranked["speedup_vs_plain"] = round(ranked["value"] / value, 3)
+        out["ranked"] = ranked
     return out
+
+
+def _primary_changes(a, b):
+    """Reads whose primary (contig, POS, FLAG, CIGAR) and whose MAPQ differ."""
+    n = len(a["contig"])
+    prim = (a["contig"][:n] != b["contig"][:n]) | (a["pos"][:n] != b["pos"][:n]) | (a["flag"][:n] != b["flag"][:n])
+    ca, cb = a["cigar_off"], b["cigar_off"]
+    la, lb = np.diff(ca[:n + 1].astype(np.int64)), np.diff(cb[:n + 1].astype(np.int64))
+    same_len = la == lb
+    idx = np.flatnonzero(same_len & ~prim)
+    # compare CIGAR words of equal-length CIGARs in one pass
+    if idx.size:
+        ra = np.repeat(ca[idx].astype(np.int64), la[idx]) + (np.arange(la[idx].sum()) -
+                                                            np.repeat(np.cumsum(la[idx]) - la[idx], la[idx]))
+        rb = np.repeat(cb[idx].astype(np.int64), la[idx]) + (np.arange(la[idx].sum()) -
+                                                            np.repeat(np.cumsum(la[idx]) - la[idx], la[idx]))
+        bad = a["cigar"][ra] != b["cigar"][rb]
+        owner = np.repeat(idx, la[idx])
+        prim[np.unique(owner[bad])] = True
+    prim |= ~same_len
+    mq = a["mapq"][:n] != b["mapq"][:n]
+    return int(prim.sum()), int(mq.sum())
+
+
+def run_ranked(args, m, opts, step, O1, O2, meta, n_reads, dev):
+    """The ranked path on the same reads: train the candidate ranker on fresh
+    pairs of the same genome (plain-path labels), then time the same steps
+    with pruning on and count the reads whose primary or MAPQ changed against
+    the plain path's records."""
+    import torch
+    import probebwa_gb300 as P
+    from probebwa_gb300 import synth
+    plain = [{k: v.copy() for k, v in O.items() if not k.startswith("_")} for O in (O1, O2)]
+    prefix = os.path.join(args.cache, f"cfg{args.config}")
+    t = time.time()
+    tr_path = prefix + f".train{args.train_pairs}.npz"
+    if not os.path.exists(tr_path):
+        contigs = synth.read_stidx_contigs(prefix)
+        b1, q1, o1, b2, q2, o2 = synth.reads_paired_fast(SEED[args.config] + 99, contigs, args.train_pairs, L=150,
+                                                         mean=350.0, sd=50.0, sub=0.005, indel=0.0005)
+        np.savez(tr_path, b1=b1, q1=q1, o1=o1, b2=b2, q2=q2, o2=o2)
+    tr = dict(np.load(tr_path))
+    t_gen = time.time() - t
+    T1 = P.Reads(tr["b1"], tr["q1"], tr["o1"])
+    T2 = P.Reads(tr["b2"], tr["q2"], tr["o2"])
+    rep = m.ranker_train(T1, T2)
+    m.ranker_enable(True)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    m.ranker_enable(True)  # counters from here
+    stats = [step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    cnt = m.ranker_counters()
+    m.ranker_enable(False)
+    dev_ms = [s["ms_seed"] + s["ms_cluster"] + s["ms_align"] + s["ms_pair"] + s["ms_finalize"] + s["ms_d2h"]
+              for s in stats]
+    e2e_ms = [s["ms_total"] for s in stats]
+    ch_p = ch_m = 0
+    for O, Pl in zip((O1, O2), plain):
+        a, b = _primary_changes(O, Pl)
+        ch_p += a
+        ch_m += b
+    s0 = stats[-1]
+    tot = cnt["kept"] + cnt["pruned"]
+    return {"value": round(n_reads / (statistics.mean(dev_ms) / 1e3), 1),
+            "e2e": {"value": round(n_reads / (statistics.mean(e2e_ms) / 1e3), 1), "unit": "reads/s"},
+            "ms_per_step": round(statistics.mean(dev_ms), 3),
+            "phase_ms": {"seed": round(s0["ms_seed"], 3), "cluster": round(s0["ms_cluster"], 3),
+                         "align_seeded": round(s0["ms_align"], 3), "pair": round(s0["ms_pair"], 3)},
+            "dp_jobs_per_step": int(s0["dp_jobs"]),
+            "changed_primary_frac": ch_p / n_reads, "changed_mapq_frac": ch_m / n_reads,
+            "changed_primaries": ch_p, "changed_mapqs": ch_m,
+            "candidates_pruned_frac": round(cnt["pruned"] / tot, 4) if tot else 0.0,
+            "reads_kept_whole": cnt["reads_whole"],
+            "train": {"pairs": args.train_pairs, "samples": rep["samples"], "positives": rep["positives"],
+                      "loss_first": round(rep["loss_first"], 5), "loss_last": round(rep["loss_last"], 5),
+                      "train_recall": round(rep["train_recall"], 6), "train_prune": round(rep["train_prune"], 4),
+                      "ms_collect": round(rep["ms_collect"], 1), "ms_train": round(rep["ms_train"], 1),
+                      "s_generate": round(t_gen, 1), "reads": "fresh pairs of the same genome (seed + 99)"}}
 
 
 # ---------------------------------------------------------------------------
@@ -547,6 +633,8 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="override read / pair count")
     ap.add_argument("--cache", default=os.environ.get("PBW_BENCH_CACHE", "/tmp/pbw_bench_cache"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ranked", type=int, default=1, help="also time the ranked path (pairs, 1 GPU)")
+    ap.add_argument("--train-pairs", type=int, default=250_000, help="fresh pairs the ranker is trained on")
     ap.add_argument("--stage", default="map", choices=["map", "index", "sam", "cli"],
                     help="map: the mapping path (default); index / sam / cli: build-hash, SAM output and the "
                          "command line, each against the oracle")

@@ -241,6 +241,44 @@ def pack_contig(codes: np.ndarray):
     return packed, runs
 
 
+def read_stidx_contigs(prefix: str):
+    """Contigs of a .stidx file as (name, codes) with codes A0 C1 G2 T3 N4
+    (Contig::slice, src/index/genome.rs:48-68, for whole contigs)."""
+    data = open(prefix + ".stidx", "rb").read()
+    p = 0
+
+    def u64():
+        nonlocal p
+        v = struct.unpack_from("<Q", data, p)[0]
+        p += 8
+        return v
+
+    def string():
+        nonlocal p
+        n = u64()
+        v = data[p:p + n].decode()
+        p += n
+        return v
+
+    string()
+    string()
+    out = []
+    for _ in range(u64()):
+        name = string()
+        npk = u64()
+        packed = np.frombuffer(data, np.uint8, npk, p)
+        p += npk
+        nr = u64()
+        runs = np.frombuffer(data, np.uint32, 2 * nr, p).reshape(-1, 2)
+        p += 8 * nr
+        length = u64()
+        codes = np.stack([(packed >> (2 * k)) & 3 for k in range(4)], axis=1).reshape(-1)[:length].astype(np.uint8)
+        for a, b in runs:
+            codes[a:min(b, length)] = 4
+        out.append((name, codes))
+    return out
+
+
 def write_stidx(prefix: str, contigs, species="synthetic", assembly="synthetic"):
     with open(prefix + ".stidx", "wb") as f:
         def s(x: str):
