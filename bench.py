@@ -212,6 +212,7 @@ def run_gpu(args, prefix, d, meta, rank, world):
     torch.cuda.synchronize()
     t_wall = time.time() - t_wall
     clocks = clk.stop()
+    tuning = m.tuning()
     ranked = None
     if args.ranked and paired and world == 1:
         ranked = run_ranked(args, m, opts, step, O1, O2, meta, n_reads, dev)
@@ -282,6 +283,9 @@ def run_gpu(args, prefix, d, meta, rank, world):
         "dp_gcups": round(gcups, 2), "dp_cells_per_step": int(s0["dp_cells"]), "dp_jobs_per_step": int(s0["dp_jobs"]),
         "roofline": roofline, "roofline_dp": roofline_dp, "clocks": clocks, "wall_s_timed": round(t_wall, 3),
     }
+    out["batching"] = {"band_dp_lanes_by_length_class": dict(zip(("<=128", "<=256", ">256"), tuning["chosen_lanes"])),
+                       "band_dp_tuned_ms_8_16": dict(zip(("<=128", "<=256", ">256"), tuning["tuned_ms"])),
+                       "length_bins": bool(tuning["length_bins"]), "pair_graphs": bool(tuning["pair_graphs"])}
     if ranked is not None:
         ranked["speedup_vs_plain"] = round(ranked["value"] / value, 3)
         out["ranked"] = ranked

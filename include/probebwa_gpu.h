@@ -289,6 +289,33 @@ int pbw_build_genome(const char* out_prefix, const char* species, const char* as
 int pbw_build_hash(const char* genome_prefix, const char* out_prefix, uint64_t k, uint64_t stride,
                    uint64_t max_count, int32_t device);
 
+/* Batching settings of a handle (no counterpart in the reference).
+ * autotune: the seeded band DP exists with 8 lanes per alignment (8 band
+ *   columns each) and 16 lanes (4 each); with autotune the first chunk of
+ *   each read-length class (<= 128, <= 256, longer bases) runs both on the
+ *   same alignments and the faster form is kept for the class (the results
+ *   are the same either way). band_lanes 8 or 16 forces a form; 0 leaves it
+ *   to the tuner (8 without it).
+ * length_bins: in a chunk whose reads differ in length, the seeded DP's work
+ *   queue is ordered by 16-base length bins, longest first.
+ * pair_graphs: each batch of pairs (decide, cross-alignment DP, statistics,
+ *   resolve, observation copy) is one CUDA graph launch, captured once per
+ *   chunk of pairs.
+ * chosen_lanes / tuned_ms are outputs of pbw_get_tuning: the form chosen
+ * per read-length class (0 = not tuned yet) and the two timings (8 lanes,
+ * 16 lanes, ms) that chose it. All settings are on by default.
+ * pbw_set_tuning reads the four inputs and clears the tuned choices. */
+typedef struct {
+  int32_t autotune;
+  int32_t band_lanes;
+  int32_t length_bins;
+  int32_t pair_graphs;
+  int32_t chosen_lanes[3];
+  float tuned_ms[3][2];
+} pbw_tuning;
+int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t);
+int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t);
+
 /* Learned candidate ranker (no counterpart in the reference): a small MLP
  * (12 seed features -> 64 -> 64 -> 1, BF16 weights, FP32 accumulation on the
  * tensor cores) that scores each of a read's candidates before the seeded

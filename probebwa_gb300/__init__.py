@@ -81,6 +81,11 @@ class RankerReportC(C.Structure):
                 ("train_prune", C.c_double), ("ms_collect", C.c_double), ("ms_train", C.c_double)]
 
 
+class TuningC(C.Structure):
+    _fields_ = [("autotune", C.c_int32), ("band_lanes", C.c_int32), ("length_bins", C.c_int32),
+                ("pair_graphs", C.c_int32), ("chosen_lanes", C.c_int32 * 3), ("tuned_ms", (C.c_float * 2) * 3)]
+
+
 class InsertModelC(C.Structure):
     _fields_ = [("mean", C.c_double), ("sd", C.c_double), ("n_observed", C.c_uint64)]
 
@@ -146,6 +151,8 @@ def lib():
         L.pbw_sam_format.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, vp, u64, vp]
         L.pbw_sort_coordinate.argtypes = [vp, u32, C.POINTER(SamSourceC), vp, u64, vp]
         L.pbw_build_genome.argtypes = [cp, cp, cp, u32, C.POINTER(cp)]
+        L.pbw_get_tuning.argtypes = [vp, C.POINTER(TuningC)]
+        L.pbw_set_tuning.argtypes = [vp, C.POINTER(TuningC)]
         L.pbw_ranker_default_options.argtypes = [C.POINTER(RankerOptionsC)]
         L.pbw_ranker_train.argtypes = [vp, C.POINTER(ReadsC), C.POINTER(ReadsC), C.POINTER(RankerOptionsC),
                                        C.POINTER(RankerReportC)]
@@ -490,6 +497,22 @@ class Mapper:
         self._check(lib().pbw_sort_coordinate(self.h, len(sources), arr, _ptr(sel) if sel.size else None,
                                               int(sel.size), _ptr(out)))
         return out[:sel.size]
+
+    def tuning(self) -> dict:
+        """Batching settings and the band-DP forms the tuner chose (pbw_get_tuning)."""
+        t = TuningC()
+        self._check(lib().pbw_get_tuning(self.h, C.byref(t)))
+        return {"autotune": t.autotune, "band_lanes": t.band_lanes, "length_bins": t.length_bins,
+                "pair_graphs": t.pair_graphs, "chosen_lanes": list(t.chosen_lanes),
+                "tuned_ms": [list(r) for r in t.tuned_ms]}
+
+    def set_tuning(self, **kw):
+        """pbw_set_tuning: autotune, band_lanes (0, 8, 16), length_bins, pair_graphs."""
+        t = TuningC()
+        self._check(lib().pbw_get_tuning(self.h, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(lib().pbw_set_tuning(self.h, C.byref(t)))
 
     def ranker_train(self, r1: Reads, r2: Reads | None = None, **kw) -> dict:
         """Trains the candidate ranker on these reads (pairs when r2 is given)

@@ -489,23 +489,47 @@ static void launch_band_c(const AlignArgs& a, int num_sms, cudaStream_t st) {
   k_align_band<C, G, TSTAR><<<band_grid<C, G>(LY, num_sms), 32, sm, st>>>(a, LY);
 }
 
-// Global traceback slab that launch_align_band needs in AlignArgs::tb_global.
+// Global traceback slab that launch_align_band needs in AlignArgs::tb_global:
+// enough for either lane count (8 or 16 lanes per alignment).
 size_t band_tb_slab_bytes(int lmax, int nmax, int num_sms, int band_max) {
   const int C = band_c(band_max);
-  const BandLayout LY = band_layout(lmax, nmax, 8 * C / 2);
-  const int grid = C == 2 ? band_grid<2, 8>(LY, num_sms) : (C == 4 ? band_grid<4, 8>(LY, num_sms) : band_grid<8, 8>(LY, num_sms));
-  return (size_t)grid * 4 * LY.tb_job;
+  const BandLayout L8 = band_layout(lmax, nmax, 8 * C / 2);
+  const int g8 = C == 2 ? band_grid<2, 8>(L8, num_sms) : (C == 4 ? band_grid<4, 8>(L8, num_sms) : band_grid<8, 8>(L8, num_sms));
+  size_t need = (size_t)g8 * 4 * L8.tb_job;
+  if (C >= 4) {
+    // 16 lanes with half the columns per lane
+    const BandLayout L16 = band_layout(lmax, nmax, 16 * (C / 2) / 2);
+    const int g16 = C == 4 ? band_grid<2, 16>(L16, num_sms) : band_grid<4, 16>(L16, num_sms);
+    need = std::max(need, (size_t)g16 * 2 * L16.tb_job);
+  }
+  return need;
 }
 
-// 8 lanes per alignment, C columns per lane with 8*C > 2*band_max + 1; the
-// fast form is compiled for column 2*band_max + 1 at lane position TSTAR
+// Whether a 16-lane form exists for the band (a band of at least 8 columns
+// per 8 lanes, i.e. C >= 4).
+bool band_has_lanes16(int band_max) { return band_c(band_max) >= 4; }
+
+// lanes lanes per alignment, C columns per lane with lanes*C > 2*band_max + 1;
+// the fast form is compiled for column 2*band_max + 1 at lane position TSTAR
 // (odd, as 2*band + 1 is odd and C even); alignments of other bands in the
-// same launch use the masked form throughout.
-void launch_align_band(const AlignArgs& a, int num_sms, int band_max, cudaStream_t st) {
+// same launch use the masked form throughout. lanes 16 halves C (bands with
+// C >= 4 only).
+void launch_align_band_lanes(const AlignArgs& a, int num_sms, int band_max, int lanes, cudaStream_t st) {
   const int cstar = 2 * band_max + 1;
-  if (band_c(band_max) == 2) {
+  const int C = band_c(band_max);
+  if (lanes == 16 && C >= 4) {
+    if (C == 4) {
+      launch_band_c<2, 16, 1>(a, num_sms, st);
+    } else if (cstar % 4 == 1) {
+      launch_band_c<4, 16, 1>(a, num_sms, st);
+    } else {
+      launch_band_c<4, 16, 3>(a, num_sms, st);
+    }
+    return;
+  }
+  if (C == 2) {
     launch_band_c<2, 8, 1>(a, num_sms, st);
-  } else if (band_c(band_max) == 4) {
+  } else if (C == 4) {
     if (cstar % 4 == 1) launch_band_c<4, 8, 1>(a, num_sms, st);
     else launch_band_c<4, 8, 3>(a, num_sms, st);
   } else {
@@ -516,6 +540,10 @@ void launch_align_band(const AlignArgs& a, int num_sms, int band_max, cudaStream
       default: launch_band_c<8, 8, 7>(a, num_sms, st); break;
     }
   }
+}
+
+void launch_align_band(const AlignArgs& a, int num_sms, int band_max, cudaStream_t st) {
+  launch_align_band_lanes(a, num_sms, band_max, 8, st);
 }
 
 }  // namespace pbw

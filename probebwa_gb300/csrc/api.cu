@@ -386,6 +386,39 @@ const char* pbw_contig_name(const pbw_handle* h, uint64_t i) {
 }
 uint64_t pbw_contig_length(const pbw_handle* h, uint64_t i) { return (h && i < h->lens.size()) ? h->lens[i] : 0; }
 
+int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t) {
+  if (!h || !t) return PBW_ERR_ARG;
+  const auto& T = h->tune;
+  t->autotune = T.autotune;
+  t->band_lanes = T.band_lanes;
+  t->length_bins = T.length_bins;
+  t->pair_graphs = T.pair_graphs;
+  for (int c = 0; c < 3; c++) {
+    t->chosen_lanes[c] = T.chosen[c];
+    t->tuned_ms[c][0] = T.ms[c][0];
+    t->tuned_ms[c][1] = T.ms[c][1];
+  }
+  return PBW_OK;
+}
+
+int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t) {
+  if (!h || !t) return PBW_ERR_ARG;
+  if (t->band_lanes != 0 && t->band_lanes != 8 && t->band_lanes != 16) {
+    h->err = "pbw_set_tuning: band_lanes must be 0, 8 or 16";
+    return PBW_ERR_ARG;
+  }
+  auto& T = h->tune;
+  T.autotune = t->autotune != 0;
+  T.band_lanes = t->band_lanes;
+  T.length_bins = t->length_bins != 0;
+  T.pair_graphs = t->pair_graphs != 0;
+  for (int c = 0; c < 3; c++) {
+    T.chosen[c] = 0;
+    T.ms[c][0] = T.ms[c][1] = 0.f;
+  }
+  return PBW_OK;
+}
+
 int pbw_last_stats(const pbw_handle* h, pbw_stats* st) {
   if (!h || !st) return PBW_ERR_ARG;
   *st = h->stats;

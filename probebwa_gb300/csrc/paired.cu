@@ -156,8 +156,9 @@ __device__ __forceinline__ unsigned long long sat_u64(double x) {
 
 __global__ void k_pair_decide(PairArgs p) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.np) return;
-  const uint32_t pl = p.p0 + t;  // pair index within the super-chunk
+  const uint32_t np = p.batch ? p.batch[1] : p.np, p0 = p.batch ? p.batch[0] : p.p0;
+  if (t >= np) return;
+  const uint32_t pl = p0 + t;  // pair index within the super-chunk
   const ReadSum& S1 = p.sum[0][pl];
   const ReadSum& S2 = p.sum[1][pl];
   PairWork& W = p.work[pl];
@@ -320,8 +321,9 @@ __device__ __forceinline__ double insert_ll(const PairModel* M, double x) {
 
 __global__ void k_pair_resolve(PairArgs p) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.np) return;
-  const uint32_t pl = p.p0 + t;
+  const uint32_t np = p.batch ? p.batch[1] : p.np, p0 = p.batch ? p.batch[0] : p.p0;
+  if (t >= np) return;
+  const uint32_t pl = p0 + t;
   const ReadSum& S1 = p.sum[0][pl];
   const ReadSum& S2 = p.sum[1][pl];
   const PairWork& W = p.work[pl];
@@ -464,6 +466,7 @@ __global__ void k_pair_resolve(PairArgs p) {
     }
   }
   p.obs[pl] = obs;
+  if (p.obs_batch) p.obs_batch[t] = obs;
 }
 
 // InsertSizeDistribution::update (insert_size.rs:32-44) over one batch's

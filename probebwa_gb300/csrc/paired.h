@@ -76,6 +76,9 @@ struct PairArgs {
   const uint64_t* offs2;
   uint32_t read0;           // read index of super-chunk pair 0 in the offsets arrays
   uint32_t p0, np;          // the batch: super-chunk pairs [p0, p0 + np)
+  const uint32_t* batch;    // optional device {p0, np} in place of p0 / np (one graph replayed per batch;
+                            // np above is then only the grid bound)
+  double* obs_batch;        // optional: the batch's observations again at batch-relative indices
   const ReadSum* sum[2];
   const AlnOut* aln[2];
   const Cand* cand[2];

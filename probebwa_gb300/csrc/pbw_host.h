@@ -40,6 +40,12 @@ uint64_t scan_blocks(uint64_t n);
 void launch_scan_excl(unsigned int* a, uint64_t n, unsigned int* out, unsigned int* block_sums, unsigned int* total,
                       const unsigned int* base_in, cudaStream_t st);
 
+// Reorders the n_jobs (device count) alignment jobs into out by read-length
+// bins, longest first (batching.cu); bins holds job_bin_words() entries.
+size_t job_bin_words();
+void launch_job_bins(const AlnJob* jobs, const unsigned int* n_jobs, const uint64_t* offs, unsigned int* bins,
+                     AlnJob* out, int grid, cudaStream_t st);
+
 // Stable LSD radix sort of n (key, value) pairs by key bits
 // [8 * first_digit, 8 * (first_digit + passes)). Input in k[0] / v[0]; the
 // passes ping-pong with k[1] / v[1]; returns the index of the buffers that

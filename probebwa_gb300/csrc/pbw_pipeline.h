@@ -138,6 +138,20 @@ struct pbw_handle {
     pbw::DevBuf<uint8_t> c_label;
     uint64_t c_slots = 0;                             // slots per read set in the collection
   } rk;
+  // batching: seeded-DP form per read-length class, length bins, graphs
+  struct Tuning {
+    int autotune = 1;       // time the 8- and 16-lane band DP on a class's first chunk, keep the faster
+    int band_lanes = 0;     // 0: the tuned (or 8) form; 8 or 16: forced
+    int length_bins = 1;    // order the seeded DP queue by read length in mixed-length chunks
+    int pair_graphs = 1;    // one CUDA graph launch per batch of pairs
+    int chosen[3] = {0, 0, 0};  // lanes per read-length class (<= 128, <= 256, longer); 0: not tuned
+    float ms[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  } tune;
+  int call_lmin = 0;        // shortest read of the current call
+  pbw::DevBuf<pbw::AlnJob> d_jobs_b;
+  pbw::DevBuf<unsigned int> d_bins;
+  pbw::DevBuf<uint32_t> d_batch;
+  pbw::DevBuf<double> d_obs_batch;
   pbw::HostBuf h_stage;
   pbw::HostBuf h_fold;  // one batch's insert-size observations + the model
   std::vector<cudaEvent_t> events;

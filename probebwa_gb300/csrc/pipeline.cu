@@ -64,6 +64,7 @@ constexpr size_t OVF_POOL_HITS = 16ull << 20;
 struct ChunkCfg {
   uint32_t ch;      // reads per chunk
   int lmax;
+  int lmin;         // shortest read of the call (length bins when below lmax)
   uint32_t hcap;
   uint32_t wcap;
   int nmax;         // longest reference window
@@ -73,6 +74,7 @@ static ChunkCfg chunk_cfg(pbw_handle* h, uint64_t n, int lmax) {
   ChunkCfg c;
   c.ch = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(n, 1), h->opt.chunk_reads);
   c.lmax = std::max(lmax, 1);
+  c.lmin = std::min(std::max(h->call_lmin, 0), c.lmax);
   c.hcap = 4096;
   c.wcap = (uint32_t)std::max(c.lmax - KMER + 1, 1);
   const uint64_t rp = std::max<uint64_t>(h->opt.max_indel_len, 10);
@@ -96,6 +98,10 @@ static int ensure_chunk(pbw_handle* h, const ChunkCfg& c) {
   TRY(grow(h, h->d_n_cand, c.ch));
   TRY(grow(h, h->d_total_cand, c.ch));
   TRY(grow(h, h->d_jobs, (size_t)c.ch * MAX_CAND));
+  if (h->tune.length_bins && c.lmin < c.lmax) {
+    TRY(grow(h, h->d_jobs_b, (size_t)c.ch * MAX_CAND));
+    TRY(grow(h, h->d_bins, job_bin_words()));
+  }
   TRY(grow(h, h->d_aln, (size_t)c.ch * MAX_CAND));
   TRY(grow(h, h->d_cig_pool, (size_t)c.ch * MAX_CAND * 24 + 4096));
   TRY(grow(h, h->d_scan_sums, scan_blocks(c.ch) + 4));
@@ -311,6 +317,55 @@ static void rank_mate_features(pbw_handle* h, const MateBufs& m1, const MateBufs
   h->stats.kernel_launches += 2;
 }
 
+// Read-length class of a chunk for the tuned band-DP form.
+static int length_class(int lmax) { return lmax <= 128 ? 0 : (lmax <= 256 ? 1 : 2); }
+
+// The seeded band DP in the form chosen for this read-length class: forced
+// by pbw_set_tuning, or timed once per class on the class's first chunk --
+// the 8-lane form runs, the queue and the counters it moved are put back,
+// the 16-lane form runs on the same jobs (same results: the DP is exact),
+// and the faster one is kept for the class's later chunks.
+static int band_dp(pbw_handle* h, const AlignArgs& aa, const ChunkCfg& cfg) {
+  cudaStream_t st = h->st;
+  const int band = (int)h->opt.max_indel_len;
+  const int cls = length_class(cfg.lmax);
+  auto& T = h->tune;
+  if (!band_has_lanes16(band)) {
+    launch_align_band_lanes(aa, h->num_sms, band, 8, st);
+    return PBW_OK;
+  }
+  if (T.band_lanes == 8 || T.band_lanes == 16) {
+    launch_align_band_lanes(aa, h->num_sms, band, T.band_lanes, st);
+    return PBW_OK;
+  }
+  if (T.chosen[cls] || !T.autotune) {
+    launch_align_band_lanes(aa, h->num_sms, band, T.chosen[cls] ? T.chosen[cls] : 8, st);
+    return PBW_OK;
+  }
+  unsigned int* c32 = h->d_cnt32.p;
+  unsigned long long* c64 = h->d_cnt64.p;
+  cudaEvent_t* e = &h->events[24];
+  // snapshot: CIGAR pool cursor, DP job and cell counters
+  CK(cudaMemcpyAsync(c32 + 12, c32 + 2, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c64 + 12, c64 + 3, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+  CK(cudaEventRecord(e[0], st));
+  launch_align_band_lanes(aa, h->num_sms, band, 8, st);
+  CK(cudaEventRecord(e[1], st));
+  CK(cudaMemsetAsync(aa.next_job, 0, sizeof(unsigned int), st));
+  CK(cudaMemcpyAsync(c32 + 2, c32 + 12, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c64 + 3, c64 + 12, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+  CK(cudaEventRecord(e[2], st));
+  launch_align_band_lanes(aa, h->num_sms, band, 16, st);
+  CK(cudaEventRecord(e[3], st));
+  CK(cudaGetLastError());
+  CK(cudaEventSynchronize(e[3]));
+  T.ms[cls][0] = (float)ms_between(e[0], e[1]);
+  T.ms[cls][1] = (float)ms_between(e[2], e[3]);
+  T.chosen[cls] = T.ms[cls][1] < T.ms[cls][0] ? 16 : 8;
+  h->stats.kernel_launches += 1;
+  return PBW_OK;
+}
+
 // Candidates -> jobs -> K3 -> alignment statistics for one read set (with
 // the keep flags when prune), and the training labels when labels is set.
 // ev[3] marks the end. reset_pool clears the CIGAR pool (the first read set
@@ -364,8 +419,14 @@ static int align_candidates(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* b
   aa.tb_global_per_warp = 0;
   aa.counters = h->d_cnt64.p + 3;
   aa.err = h->d_err.p;
+  if (h->tune.length_bins && cfg.lmin < cfg.lmax) {
+    // mixed read lengths: the work queue in length bins, longest first
+    launch_job_bins(h->d_jobs.p, c32 + 0, offs, h->d_bins.p, h->d_jobs_b.p, h->num_sms * 4, st);
+    aa.jobs = h->d_jobs_b.p;
+    h->stats.kernel_launches += 3;
+  }
   if (h->opt.max_indel_len <= 31) {
-    launch_align_band(aa, h->num_sms, (int)h->opt.max_indel_len, st);
+    TRY(band_dp(h, aa, cfg));
   } else {
     aa.tb_global = h->d_tb_global.p;
     aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, cfg.nmax);
@@ -505,9 +566,10 @@ static int copy_records_out(pbw_handle* h, uint64_t n, pbw_records* out, bool pa
   return PBW_OK;
 }
 
-static int validate_reads(pbw_handle* h, const pbw_reads* r, uint64_t& total, int& lmax) {
+static int validate_reads(pbw_handle* h, const pbw_reads* r, uint64_t& total, int& lmax, int* lmin = nullptr) {
   if (!r || (r->n && (!r->offsets))) { h->err = "null reads"; return PBW_ERR_ARG; }
   lmax = 0;
+  int lo = PBW_MAX_READ_LEN;
   total = r->n ? r->offsets[r->n] - r->offsets[0] : 0;
   if (r->n && r->offsets[0] != 0) { h->err = "offsets[0] must be 0"; return PBW_ERR_ARG; }
   for (uint64_t i = 0; i < r->n; i++) {
@@ -518,7 +580,9 @@ static int validate_reads(pbw_handle* h, const pbw_reads* r, uint64_t& total, in
       return PBW_ERR_LIMIT;
     }
     lmax = std::max(lmax, (int)L);
+    lo = std::min(lo, (int)L);
   }
+  if (lmin) *lmin = r->n ? lo : 0;
   if (r->n >= (1ull << 31)) { h->err = "too many reads in one call"; return PBW_ERR_LIMIT; }
   return PBW_OK;
 }
@@ -637,7 +701,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   pm.sd = model->sd;
   pm.n = model->n_observed;
   pm.ln_2pi_sd2 = std::log(2.0 * 3.141592653589793 * pm.sd * pm.sd);
-  if (!h->h_fold.ensure(sizeof(PairModel) + 2000 * sizeof(double))) {
+  if (!h->h_fold.ensure(sizeof(PairModel) + 2000 * sizeof(double) + 16)) {
     h->err = "cudaMallocHost failed";
     return PBW_ERR_NOMEM;
   }
@@ -781,9 +845,51 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, wide_n);
     aa.counters = h->d_cnt64.p + 3;
     aa.err = h->d_err.p;
+    // One batch: decide -> cross-alignment DP -> statistics -> resolve, its
+    // observations to the host, the fold there (the model of the next batch).
+    // With pair_graphs the device side is captured once per super-chunk as a
+    // CUDA graph that reads the batch from device memory ({p0, np}, copied
+    // from pinned memory by the graph's first nodes with the model) and is
+    // replayed per batch; a capture the runtime refuses falls back to the
+    // launches below.
+    cudaGraphExec_t gexec = nullptr;
+    uint32_t* h_batch = (uint32_t*)((char*)h->h_fold.p + sizeof(PairModel) + 2000 * sizeof(double));
+    if (h->tune.pair_graphs) {
+      TRY(grow(h, h->d_batch, 2));
+      TRY(grow(h, h->d_obs_batch, 2000));
+      PairArgs pg = pa;
+      pg.batch = h->d_batch.p;
+      pg.obs_batch = h->d_obs_batch.p;
+      pg.np = 2000;
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(h->d_batch.p, h_batch, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st);
+        launch_pair_decide(pg, st);
+        launch_align_window(aa, grid_w, st);
+        launch_aln_stats(aa, (uint64_t)2000 * MAX_CROSS, st);
+        launch_pair_resolve(pg, st);
+        cudaMemcpyAsync(h_obs, h->d_obs_batch.p, 2000 * sizeof(double), cudaMemcpyDeviceToHost, st);
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (ec != cudaSuccess || !graph || cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
+        if (graph) cudaGraphDestroy(graph);
+      }
+      cudaGetLastError();  // a refused capture leaves no sticky error
+    }
     for (size_t k = bi; k < be; k++) {
       pa.p0 = (uint32_t)(batches[k].first - a);
       pa.np = (uint32_t)batches[k].second;
+      if (gexec) {
+        h_batch[0] = pa.p0;
+        h_batch[1] = pa.np;
+        CK(cudaGraphLaunch(gexec, st));
+        CK(cudaStreamSynchronize(st));
+        fold_insert_model(pm, h_obs, pa.np);
+        *h_pm = pm;
+        h->stats.kernel_launches += 4;
+        continue;
+      }
       CK(cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st));
       launch_pair_decide(pa, st);
       const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, (uint64_t)pa.np * MAX_CROSS);
@@ -797,6 +903,12 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       *h_pm = pm;
       CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st));
       h->stats.kernel_launches += 4;
+    }
+    if (gexec) {
+      // the model the graph path left on the host goes to the device for the
+      // next super-chunk's direct launches, if any
+      CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st));
+      cudaGraphExecDestroy(gexec);
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev[1], st));
@@ -885,8 +997,9 @@ int pbw_map_single(pbw_handle* h, const pbw_reads* reads, pbw_records* out) {
   cudaSetDevice(h->device);
   h->stats = pbw_stats{};
   uint64_t total;
-  int lmax;
-  TRY(validate_reads(h, reads, total, lmax));
+  int lmax, lmin;
+  TRY(validate_reads(h, reads, total, lmax, &lmin));
+  h->call_lmin = lmin;
   if (reads->n == 0) {
     if (out->cigar_off) out->cigar_off[0] = 0;
     return PBW_OK;
@@ -915,9 +1028,10 @@ int pbw_map_paired(pbw_handle* h, pbw_insert_model* model, const pbw_reads* r1, 
   }
   if (o1->n < r1->n || o2->n < r2->n) { h->err = "records array smaller than reads"; return PBW_ERR_CAPACITY; }
   uint64_t t1, t2;
-  int l1, l2;
-  TRY(validate_reads(h, r1, t1, l1));
-  TRY(validate_reads(h, r2, t2, l2));
+  int l1, l2, m1, m2;
+  TRY(validate_reads(h, r1, t1, l1, &m1));
+  TRY(validate_reads(h, r2, t2, l2, &m2));
+  h->call_lmin = std::min(m1, m2);
   const uint64_t n = r1->n;
   if (n == 0) {
     if (o1->cigar_off) o1->cigar_off[0] = 0;
@@ -949,8 +1063,9 @@ int pbw_map_single_device(pbw_handle* h, const pbw_reads* dev_reads, pbw_records
   CK(cudaMemcpy(offs.data(), dev_reads->offsets, (n + 1) * 8, cudaMemcpyDeviceToHost));
   pbw_reads hr{n, nullptr, nullptr, offs.data()};
   uint64_t total;
-  int lmax;
-  TRY(validate_reads(h, &hr, total, lmax));
+  int lmax, lmin;
+  TRY(validate_reads(h, &hr, total, lmax, &lmin));
+  h->call_lmin = lmin;
   TRY(map_single_dev(h, dev_reads->bases, dev_reads->quals, dev_reads->offsets, n, total, lmax, out));
   h->stats.ms_total = h->stats.ms_seed + h->stats.ms_cluster + h->stats.ms_align + h->stats.ms_finalize +
                       h->stats.ms_d2h;
