@@ -335,7 +335,7 @@ def run_ranked(args, m, opts, step, O1, O2, meta, n_reads, dev):
     t_gen = time.time() - t
     T1 = P.Reads(tr["b1"], tr["q1"], tr["o1"])
     T2 = P.Reads(tr["b2"], tr["q2"], tr["o2"])
-    rep = m.ranker_train(T1, T2)
+    rep = m.ranker_train(T1, T2, label_cut=args.label_cut)
     m.ranker_enable(True)
     for _ in range(args.warmup):
         step()
@@ -365,7 +365,7 @@ def run_ranked(args, m, opts, step, O1, O2, meta, n_reads, dev):
             "changed_primaries": ch_p, "changed_mapqs": ch_m,
             "candidates_pruned_frac": round(cnt["pruned"] / tot, 4) if tot else 0.0,
             "reads_kept_whole": cnt["reads_whole"],
-            "train": {"pairs": args.train_pairs, "samples": rep["samples"], "positives": rep["positives"],
+            "train": {"pairs": args.train_pairs, "label_cut": args.label_cut, "samples": rep["samples"], "positives": rep["positives"],
                       "loss_first": round(rep["loss_first"], 5), "loss_last": round(rep["loss_last"], 5),
                       "train_recall": round(rep["train_recall"], 6), "train_prune": round(rep["train_prune"], 4),
                       "ms_collect": round(rep["ms_collect"], 1), "ms_train": round(rep["ms_train"], 1),
@@ -627,6 +627,108 @@ def run_stage_cli(args, prefix, d, meta):
                                                    f"({'pairs' if paired else 'reads'}), index load included"}})
 
 
+def batch_workload(args):
+    """Mixed-length workload of the batching configuration, scaled to one
+    box's minutes: a 300 Mbp genome (12 contigs of U(50, 250) relative size,
+    GC 41%, 45% copies of 500 interspersed repeat families with 300 bp-6 kbp
+    consensus and 2-25% divergence, 3% tandem arrays); 1,000,000 single-end
+    reads and 500,000 pairs (insert N(300, 80)) trimmed to lengths U[60, 250],
+    0.5% substitutions and 0.05% indels; fresh reads of the same kind (200,000
+    single-end, 100,000 pairs) to train the ranker. The index is built with
+    pbw_build_hash."""
+    import probebwa_gb300 as P
+    from probebwa_gb300 import synth
+    seed = 0x5EED0002
+    os.makedirs(args.cache, exist_ok=True)
+    prefix = os.path.join(args.cache, "batch")
+    rp = prefix + ".reads.npz"
+    if not (os.path.exists(prefix + ".sthash") and os.path.exists(rp)):
+        t = time.time()
+        contigs = synth.genome_families(seed)
+        synth.write_stidx(prefix, contigs)
+        P.build_hash(prefix, prefix)
+        log(f"[bench] batch genome + index: {time.time() - t:.1f}s")
+        t = time.time()
+        d = {}
+        for tag, n_se, n_pe, s0 in (("ev", 1_000_000, 500_000, 11), ("tr", 200_000, 100_000, 23)):
+            b, q, o = synth.reads_single_fast(seed + s0, contigs, n_se, L=250, sub=0.005, indel=0.0005)
+            d[f"{tag}_s_b"], d[f"{tag}_s_q"], d[f"{tag}_s_o"] = synth.trim_lengths(seed + s0 + 1, b, q, o)
+            b1, q1, o1, b2, q2, o2 = synth.reads_paired_fast(seed + s0 + 2, contigs, n_pe, L=250, mean=300.0, sd=80.0,
+                                                             sub=0.005, indel=0.0005)
+            d[f"{tag}_1_b"], d[f"{tag}_1_q"], d[f"{tag}_1_o"] = synth.trim_lengths(seed + s0 + 3, b1, q1, o1)
+            d[f"{tag}_2_b"], d[f"{tag}_2_q"], d[f"{tag}_2_o"] = synth.trim_lengths(seed + s0 + 4, b2, q2, o2)
+        np.savez(rp, **d)
+        log(f"[bench] batch reads: {time.time() - t:.1f}s")
+    d = dict(np.load(rp))
+    return prefix, d
+
+
+def run_stage_batch(args):
+    """Plain, batched (length bins + tuned band DP + pair graphs) and
+    ranked+batched mapping of the mixed-length workload, device time per
+    pass; changed primaries and MAPQs of the ranked records against the plain
+    ones on the same reads."""
+    import probebwa_gb300 as P
+    P.build()
+    prefix, d = batch_workload(args)
+    R = lambda tag, k: P.Reads(d[f"{tag}_{k}_b"], d[f"{tag}_{k}_q"], d[f"{tag}_{k}_o"])
+    se, p1, p2 = R("ev", "s"), R("ev", "1"), R("ev", "2")
+    n_reads = se.n + p1.n + p2.n
+
+    def dev_ms(st):
+        return st["ms_seed"] + st["ms_cluster"] + st["ms_align"] + st["ms_pair"] + st["ms_finalize"] + st["ms_d2h"]
+
+    def timed(m, fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        ts, out = [], None
+        for _ in range(args.steps):
+            out = fn()
+            ts.append(dev_ms(m.stats()))
+        return statistics.mean(ts), out
+
+    res = {}
+    with P.Mapper(prefix) as ms, P.Mapper(prefix) as mp:
+        modes = {"plain": dict(length_bins=0, autotune=0, band_lanes=8, pair_graphs=0),
+                 "batched": dict(length_bins=1, autotune=1, band_lanes=0, pair_graphs=1)}
+        recs = {}
+        for name, kw in modes.items():
+            ms.set_tuning(**kw)
+            mp.set_tuning(**kw)
+            t_se, o_se = timed(ms, lambda: ms.map_single(se))
+            t_pe, o_pe = timed(mp, lambda: mp.map_paired(p1, p2))
+            recs[name] = (o_se, o_pe[0], o_pe[1])
+            res[name] = {"ms_single": round(t_se, 2), "ms_pairs": round(t_pe, 2),
+                         "reads_per_s": round(n_reads / ((t_se + t_pe) / 1e3), 1)}
+        res["batched"]["tuning_single"] = ms.tuning()
+        res["batched"]["tuning_pairs"] = mp.tuning()
+        rep_s = ms.ranker_train(R("tr", "s"), label_cut=args.label_cut)
+        rep_p = mp.ranker_train(R("tr", "1"), R("tr", "2"), label_cut=args.label_cut)
+        ms.ranker_enable(True)
+        mp.ranker_enable(True)
+        t_se, o_se = timed(ms, lambda: ms.map_single(se))
+        t_pe, o_pe = timed(mp, lambda: mp.map_paired(p1, p2))
+        cs, cp = ms.ranker_counters(), mp.ranker_counters()
+    ch_p = ch_m = 0
+    for a, b in zip((o_se, o_pe[0], o_pe[1]), recs["plain"]):
+        x, y = _primary_changes(a, b)
+        ch_p += x
+        ch_m += y
+    same_batched = sum(sum(_primary_changes(a, b)) for a, b in zip(recs["batched"], recs["plain"]))
+    res["ranked_batched"] = {"ms_single": round(t_se, 2), "ms_pairs": round(t_pe, 2),
+                             "reads_per_s": round(n_reads / ((t_se + t_pe) / 1e3), 1),
+                             "changed_primary_frac": ch_p / n_reads, "changed_mapq_frac": ch_m / n_reads,
+                             "candidates_pruned_frac_single": round(cs["pruned"] / max(1, cs["kept"] + cs["pruned"]), 4),
+                             "candidates_pruned_frac_pairs": round(cp["pruned"] / max(1, cp["kept"] + cp["pruned"]), 4),
+                             "train_single": {k: rep_s[k] for k in ("samples", "positives", "train_recall", "train_prune")},
+                             "train_pairs": {k: rep_p[k] for k in ("samples", "positives", "train_recall", "train_prune")}}
+    res["batched"]["records_differing_from_plain"] = int(same_batched)
+    v = res["ranked_batched"]["reads_per_s"]
+    meta = {"workload": "mixed-length 60-250 bp: 300 Mbp genome (45% repeat families, 3% tandem), "
+                        "1,000,000 single-end reads + 500,000 pairs", "reads": n_reads}
+    return _stage_line("batch", meta, v, "reads/s", dict(res, speedup_vs_plain=round(v / res["plain"]["reads_per_s"], 3)))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -639,10 +741,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ranked", type=int, default=1, help="also time the ranked path (pairs, 1 GPU)")
     ap.add_argument("--train-pairs", type=int, default=250_000, help="fresh pairs the ranker is trained on")
-    ap.add_argument("--stage", default="map", choices=["map", "index", "sam", "cli"],
+    ap.add_argument("--label-cut", type=float, default=None,
+                    help="ranker training label: lk - lk_max >= cut (default: -60 ln 2 for the paired "
+                         "workload, where pruning then cannot move sum_exp; ln 1e-12 for --stage batch)")
+    ap.add_argument("--stage", default="map", choices=["map", "index", "sam", "cli", "batch"],
                     help="map: the mapping path (default); index / sam / cli: build-hash, SAM output and the "
                          "command line, each against the oracle")
     args = ap.parse_args()
+    if args.label_cut is None:
+        args.label_cut = -27.631021115928547 if args.stage == "batch" else -41.58883083359672
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -651,6 +758,10 @@ def main():
             return
         prefix, d, meta = workload(args.config, args.cache, args.n)
         print(json.dumps(run_reference(args, prefix, d, meta)), flush=True)
+        return
+    if args.stage == "batch":
+        if rank == 0:
+            print(json.dumps(run_stage_batch(args)), flush=True)
         return
     if args.stage != "map":
         if rank != 0:

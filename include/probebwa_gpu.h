@@ -325,7 +325,7 @@ int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t);
  *
  * pbw_ranker_train maps r1 (and r2 as mates, or NULL) once with the plain
  * path, labels every aligned candidate (the read's select_best winner, or
- * exp(lk - lk_max) >= 2^-60), trains the model on the GPU and sets the keep
+ * lk - lk_max >= label_cut), trains the model on the GPU and sets the keep
  * threshold so that `recall` of the positive training candidates is kept.
  * pbw_ranker_enable switches pruning on or off for later map calls on the
  * handle (and clears the counters); pbw_ranker_counters returns candidates
@@ -339,6 +339,8 @@ typedef struct {
   double recall;            /* fraction of positive training candidates kept (0.9995) */
   double positive_weight;   /* extra loss weight of positives over class balance (4) */
   uint64_t seed;            /* weight initialisation */
+  double label_cut;         /* a candidate is positive when lk - lk_max >= label_cut (-60 ln 2: pruning
+                               cannot change sum_exp; looser, e.g. ln 1e-12, prunes more) */
 } pbw_ranker_train_options;
 
 typedef struct {

@@ -72,7 +72,7 @@ class SamSourceC(C.Structure):
 
 class RankerOptionsC(C.Structure):
     _fields_ = [("epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_double), ("recall", C.c_double),
-                ("positive_weight", C.c_double), ("seed", C.c_uint64)]
+                ("positive_weight", C.c_double), ("seed", C.c_uint64), ("label_cut", C.c_double)]
 
 
 class RankerReportC(C.Structure):

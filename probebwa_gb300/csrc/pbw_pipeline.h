@@ -128,6 +128,7 @@ struct pbw_handle {
     bool enabled = false;     // prune candidates in map calls
     bool collect = false;     // write features and labels of every slot (plain path)
     float tau = 0.f;          // keep a candidate whose logit >= tau
+    double label_cut = 0.0;   // training label: lk - lk_max >= label_cut
     pbw::DevBuf<float> d_norm, d_w, d_m, d_v, d_g, d_loss;
     pbw::DevBuf<uint32_t> d_wb;
     pbw::DevBuf<uint16_t> d_hit_info, d_hit_src;

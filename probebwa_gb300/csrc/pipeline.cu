@@ -434,7 +434,7 @@ static int align_candidates(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* b
   }
   launch_aln_stats(aa, (uint64_t)nr * MAX_CAND, st);
   if (labels) {
-    RankLabelArgs la{mb.aln, mb.n_cand, nr, labels};
+    RankLabelArgs la{mb.aln, mb.n_cand, nr, labels, h->rk.label_cut};
     launch_rank_label(la, st);
     h->stats.kernel_launches += 1;
   }

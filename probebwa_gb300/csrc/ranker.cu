@@ -18,10 +18,12 @@
 //
 // Label (plain path): the candidate was aligned and either is the read's
 // select_best winner (the last maximum, bayesian.rs:193-201) or has
-// exp(lk - lk_max) >= 2^-60, i.e. lk - lk_max >= -60 ln 2. Terms below that
-// cannot change the FP64 sum_exp (at most 19 of them add less than half an
-// ulp of the winner's 1.0), so pruning only such candidates leaves
-// select_best, sum_exp and finalize_mapq unchanged.
+// lk - lk_max >= cut. With the default cut, -60 ln 2 (exp >= 2^-60), terms
+// below it cannot change the FP64 sum_exp (at most 19 of them add less than
+// half an ulp of the winner's 1.0), so pruning only such candidates leaves
+// select_best, sum_exp and finalize_mapq unchanged; a looser cut (e.g.
+// ln 1e-12) labels fewer candidates positive, and pruned terms can then move
+// the posterior's last bits and, rarely, a MAPQ.
 //
 // Inference: one warp per tile of 16 candidate slots. Layer 1 is one
 // m16n8k16 per 8 hidden units (features padded to k = 16), layer 2 four
@@ -264,7 +266,7 @@ __global__ void k_rank_label(RankLabelArgs a) {
       best = (int)i;
     }
   }
-  const double cut = -60.0 * 0.69314718055994530942;
+  const double cut = a.cut;
   for (uint32_t i = 0; i < (uint32_t)MAX_CAND; i++) {
     uint8_t lab = RK_IGNORE;
     if (i < nc && A[i].n_ops != 0) lab = ((int)i == best || A[i].log_lk - mx >= cut) ? 1 : 0;

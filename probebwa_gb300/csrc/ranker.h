@@ -74,6 +74,7 @@ struct RankLabelArgs {
   const uint32_t* n_cand;
   uint32_t nr;
   uint8_t* label;                  // nr * MAX_CAND
+  double cut;                      // positive when lk - lk_max >= cut (log units)
 };
 
 void launch_rank_features(const RankFeatArgs& a, int grid, cudaStream_t st);

@@ -120,6 +120,7 @@ void pbw_ranker_default_options(pbw_ranker_train_options* o) {
   o->recall = 0.9995;
   o->positive_weight = 4.0;
   o->seed = 0x5EED;
+  o->label_cut = -60.0 * 0.69314718055994530942;
 }
 
 int pbw_ranker_train(pbw_handle* h, const pbw_reads* r1, const pbw_reads* r2, const pbw_ranker_train_options* opt,
@@ -151,6 +152,7 @@ int pbw_ranker_train(pbw_handle* h, const pbw_reads* r1, const pbw_reads* r2, co
   RK_CK(cudaMemsetAsync(R.c_label.p, RK_IGNORE, (size_t)sets * slots, st));
   R.c_slots = slots;
   const bool was_enabled = R.enabled;
+  R.label_cut = o.label_cut;
   R.collect = true;
   R.enabled = false;
   int rc = map_for_collection(h, r1, r2);

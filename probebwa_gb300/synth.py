@@ -81,6 +81,63 @@ def genome_paired(seed: int, n_contigs=25, contig_len=4_000_000, dup_frac=0.05, 
 # ---------------------------------------------------------------------------
 # reads
 # ---------------------------------------------------------------------------
+def genome_families(seed: int, total=300_000_000, n_contigs=12, family_frac=0.45, n_families=500,
+                    cons_len=(300, 6000), divergence=(0.02, 0.25), tandem_frac=0.03):
+    """Contig lengths U(50, 250) scaled to `total`, GC 41%; `family_frac` of the
+    bases are copies of `n_families` interspersed repeat families (consensus
+    300 bp-6 kbp, each copy diverged by U(2, 25)% substitutions), and
+    `tandem_frac` are tandem arrays of short units (2-50 bp)."""
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(50, 250, n_contigs)
+    lens = np.maximum((w / w.sum() * total).astype(np.int64), 10_000)
+    g = rand_codes(rng, int(lens.sum()))
+    cons = [rand_codes(rng, int(rng.integers(cons_len[0], cons_len[1] + 1))) for _ in range(n_families)]
+    # copies: families drawn in proportion, placed at random non-overlapping slots
+    target = int(family_frac * len(g))
+    placed = 0
+    starts = np.sort(rng.choice(len(g) - cons_len[1] - 1, size=int(target / np.mean(cons_len) * 1.2), replace=False))
+    last_end = 0
+    for st in starts:
+        if placed >= target:
+            break
+        if st < last_end:
+            continue
+        fam = cons[int(rng.integers(0, n_families))]
+        cp = mutate_subs(rng, fam, rng.uniform(*divergence))
+        g[st:st + len(cp)] = cp
+        last_end = st + len(cp)
+        placed += len(cp)
+    # tandem arrays
+    t_target = int(tandem_frac * len(g))
+    t_placed = 0
+    while t_placed < t_target:
+        unit = rand_codes(rng, int(rng.integers(2, 51)))
+        reps = int(rng.integers(10, 200))
+        arr = np.tile(unit, reps)
+        st = int(rng.integers(0, len(g) - len(arr)))
+        g[st:st + len(arr)] = mutate_subs(rng, arr, 0.02)
+        t_placed += len(arr)
+    out, o = [], 0
+    for i, L in enumerate(lens):
+        out.append((f"chr{i + 1}", g[o:o + L].copy()))
+        o += L
+    return out
+
+
+def trim_lengths(seed: int, bases: np.ndarray, quals: np.ndarray, offs: np.ndarray, lo=60, hi=250):
+    """Each read cut to a length drawn from U[lo, hi] (its 3' end dropped), as
+    after adapter trimming; reads shorter than the draw are kept whole."""
+    rng = np.random.default_rng(seed)
+    n = len(offs) - 1
+    L = np.diff(offs).astype(np.int64)
+    keep = np.minimum(rng.integers(lo, hi + 1, n), L)
+    starts = offs[:-1].astype(np.int64)
+    idx = np.repeat(starts, keep) + (np.arange(keep.sum()) - np.repeat(np.cumsum(keep) - keep, keep))
+    no = np.zeros(n + 1, np.uint64)
+    no[1:] = np.cumsum(keep)
+    return bases[idx], quals[idx], no
+
+
 def _quals(rng, n, mu=35.0, sd=4.0):
     return np.clip(np.rint(rng.normal(mu, sd, size=n)), 2, 41).astype(np.uint8)
 
