@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
       }
       qs[i] = b;
       qq[i] = q;
-      pen[i] = __ldg(&p.tab->mmpen[q]);
+      pen[i] = __ldg(&p.tab->mmpen[q]) * 256 | (int32_t)b;  // mismatch penalty << 8 | read symbol
     }
     if (p.ref_bytes) {
       for (int j = tid; j < n; j += WIN_THREADS) rs[j] = p.ref_bytes[J.ref_start + j];
@@ -219,12 +219,16 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
         int32_t rM = col_on ? 0 : NEG, rI = NEG, rD = NEG;  // received from lane - 1
         int32_t qM = lane == 0 ? 0 : NEG, qI = NEG, qD = NEG;  // diagonal (left of the previous step)
         uint32_t acc = 0;
-        int acc_word = -1;
         uint32_t* tbcol = tb + (size_t)j * TBS;
+        // cells of this lane's column: rows [ilo, ihi]
+        if (col_on && ihi >= ilo) cells_acc += (unsigned long long)(ihi - ilo + 1);
         const int T = nrows + 31;
-        for (int t = 0; t < T; t++) {
-          const int i = R0 + t - lane;
-          const int i0 = R0 + t;  // lane 0's row
+        // Steps where every lane's row is inside [R0, R1 - 1] and inside the
+        // band take the branch-free form below; the ramps at both ends (and
+        // tiles with a partial or banded column) take the general form.
+        const bool full_tile = __all_sync(0xffffffffu, col_on && ilo == R0 && ihi == R1);
+        const int f0 = full_tile ? 31 : T, f1 = full_tile ? max(31, nrows - 1) : T;
+        auto poll = [&](int t) {
           if (k > 0 && (t & 7) == 0 && t < nrows) {
             const int target = tag_in + min(t + 8, nrows);
             unsigned int spins = 0;
@@ -240,6 +244,25 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
             }
             __threadfence_block();
           }
+        };
+        auto publish = [&](int t, int i, int32_t oM, int32_t oI, int32_t oD) {
+          if (has_next) {
+            if (lane == 31 && i >= R0 && i <= R1) {
+              outM[i] = oM;
+              outI[i] = oI;
+              outD[i] = oD;
+            }
+            const int done = t - 30;  // rows R0 .. R0 + done - 1 written by lane 31
+            if (done > 0 && ((done & 7) == 0 || done == nrows) && lane == 31) {
+              __threadfence_block();
+              s_pub[bout] = k * WIN_TAG + done;
+            }
+          }
+        };
+        auto general = [&](int t) {
+          const int i = R0 + t - lane;
+          const int i0 = R0 + t;  // lane 0's row
+          poll(t);
           int32_t bM = NEG, bI = NEG, bD = NEG;
           if (k > 0 && i0 <= R1) {
             bM = inM[i0];
@@ -252,7 +275,8 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
           const int32_t dM = qM, dI = qI, dD = qD;
           int32_t oM, oI, oD;
           if (i >= ilo && i <= ihi) {
-            const int32_t sc = qs[i - 1] == rs_j ? 20 : pen[i - 1];
+            const int32_t pv = pen[i - 1];
+            const int32_t sc = (uint8_t)pv == rs_j ? 20 : (pv >> 8);
             const int32_t fm = dM + sc, fi = dI + sc, fd = dD + sc;
             const int32_t Mv = max(max(fm, fi), fd);
             const uint32_t tm = Mv == fm ? 0u : (Mv == fi ? 1u : 2u);
@@ -266,14 +290,11 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
             oI = Iv;
             oD = Dv;
             const int rr = i - R0;
-            const int w = rr >> 3;
-            if (w != acc_word) {
-              if (acc_word >= 0) tbcol[acc_word] = acc;
-              acc_word = w;
+            acc |= (tm | (ti << 2) | (td << 3)) << ((rr & 7) * 4);
+            if ((rr & 7) == 7 || i == ihi) {
+              tbcol[rr >> 3] = acc;
               acc = 0;
             }
-            acc |= (tm | (ti << 2) | (td << 3)) << ((rr & 7) * 4);
-            cells_acc++;
             if (i == R1) {
               const unsigned long long kM = ((unsigned long long)((long long)Mv + 2147483648LL) << 32) |
                                             ((unsigned long long)j << 1);
@@ -290,18 +311,7 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
             oI = NEG;
             oD = NEG;
           }
-          if (has_next) {
-            if (lane == 31 && i >= R0 && i <= R1) {
-              outM[i] = oM;
-              outI[i] = oI;
-              outD[i] = oD;
-            }
-            const int done = t - 30;  // rows R0 .. R0 + done - 1 written by lane 31
-            if (done > 0 && ((done & 7) == 0 || done == nrows) && lane == 31) {
-              __threadfence_block();
-              s_pub[bout] = k * WIN_TAG + done;
-            }
-          }
+          publish(t, i, oM, oI, oD);
           uM = oM;
           uI = oI;
           qM = lM;
@@ -310,8 +320,52 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
           rM = __shfl_up_sync(0xffffffffu, oM, 1);
           rI = __shfl_up_sync(0xffffffffu, oI, 1);
           rD = __shfl_up_sync(0xffffffffu, oD, 1);
+        };
+        int t = 0;
+        for (; t < f0; t++) general(t);
+        for (; t < f1; t++) {
+          // every lane in rows [R0, R1 - 1] of its in-band column
+          const int i = R0 + t - lane;
+          poll(t);
+          int32_t lM = rM, lI = rI, lD = rD;
+          if (k > 0) {
+            const int32_t bM = inM[R0 + t], bI = inI[R0 + t], bD = inD[R0 + t];
+            if (lane == 0) {
+              lM = bM;
+              lI = bI;
+              lD = bD;
+            }
+          } else if (lane == 0) {
+            lM = NEG;
+            lI = NEG;
+            lD = NEG;
+          }
+          const int32_t pv = pen[i - 1];
+          const int32_t sc = (uint8_t)pv == rs_j ? 20 : (pv >> 8);
+          const int32_t fm = qM + sc, fi = qI + sc, fd = qD + sc;
+          const int32_t Mv = max(max(fm, fi), fd);
+          const uint32_t tm = Mv == fm ? 0u : (Mv == fi ? 1u : 2u);
+          const int32_t io = uM + go_j, ie = uI + ge;
+          const int32_t Iv = max(io, ie);
+          const int32_t dop = lM + go_j, dex = lD + ge;
+          const int32_t Dv = max(dop, dex);
+          rM = __shfl_up_sync(0xffffffffu, Mv, 1);
+          rI = __shfl_up_sync(0xffffffffu, Iv, 1);
+          rD = __shfl_up_sync(0xffffffffu, Dv, 1);
+          const int rr = i - R0;
+          acc |= (tm | (Iv == io ? 0u : 4u) | (Dv == dop ? 0u : 8u)) << ((rr & 7) * 4);
+          if ((rr & 7) == 7) {
+            tbcol[rr >> 3] = acc;
+            acc = 0;
+          }
+          publish(t, i, Mv, Iv, Dv);
+          uM = Mv;
+          uI = Iv;
+          qM = lM;
+          qI = lI;
+          qD = lD;
         }
-        if (acc_word >= 0) tbcol[acc_word] = acc;
+        for (; t < T; t++) general(t);
       }
     }
     for (int d = 16; d >= 1; d >>= 1) bestKey = max(bestKey, __shfl_xor_sync(0xffffffffu, bestKey, d));
