@@ -244,6 +244,18 @@ int pbw_sam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, con
 int pbw_sam_format(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
                    const uint64_t* sel, uint64_t n_sel, char* out, uint64_t cap, uint64_t* len);
 
+/* The same stream as BAM (write_bam / write_bam_indexed, src/io/bam.rs:19-57):
+ * the SAM text formatted on the device is parsed back record by record (QUAL
+ * characters read as Phred+33, so raw score bytes outside '!'..'~' are an
+ * error, as for a strict SAM parser), encoded as BAM records and written as
+ * BGZF blocks compressed on the host threads (zlib, opened at run time as
+ * libz.so.1). With write_index (which needs opt->coordinate_sorted and
+ * records in coordinate order, see pbw_sort_coordinate) a BAI goes to
+ * path + ".bai". Errors as pbw_sam_write, and PBW_ERR_FORMAT for a record
+ * that does not parse. */
+int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
+                  const uint64_t* sel, uint64_t n_sel, const char* path, int32_t write_index);
+
 /* Coordinate order of the selected records (sort_for_coordinate_order,
  * sam.rs:114-124): stable sort by (index of the contig's name, the last
  * index when names repeat; position), unmapped records (pos 0) last, on the

@@ -150,6 +150,7 @@ def lib():
         L.pbw_sam_write.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, cp]
         L.pbw_sam_format.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, vp, u64, vp]
         L.pbw_sort_coordinate.argtypes = [vp, u32, C.POINTER(SamSourceC), vp, u64, vp]
+        L.pbw_bam_write.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, cp, C.c_int32]
         L.pbw_build_genome.argtypes = [cp, cp, cp, u32, C.POINTER(cp)]
         L.pbw_get_tuning.argtypes = [vp, C.POINTER(TuningC)]
         L.pbw_set_tuning.argtypes = [vp, C.POINTER(TuningC)]
@@ -485,6 +486,21 @@ class Mapper:
         buf = C.create_string_buffer(max(n.value, 1))
         self._check(lib().pbw_sam_format(self.h, C.byref(o), len(sources), arr, sp, ns, buf, n.value, C.byref(n)))
         return buf.raw[:n.value]
+
+    def write_bam(self, path: str, sources, sel=None, command_line: str = "probebwa map",
+                  read_group: str | None = None, coordinate_sorted: bool = False, index: bool = False):
+        """The SAM stream of sam_text as BGZF BAM (write_bam, src/io/bam.rs:19-57),
+        with a BAI at path + '.bai' when index is set (coordinate-sorted records)."""
+        arr, keep = self._sam_sources(sources)
+        o = SamOptionsC(command_line.encode(), read_group.encode() if read_group is not None else None,
+                        1 if coordinate_sorted else 0)
+        sp, ns = (None, 0)
+        if sel is not None:
+            sel = np.ascontiguousarray(sel, dtype=np.uint64)
+            keep.append(sel if sel.size else np.zeros(1, np.uint64))
+            sp, ns = (_ptr(keep[-1]), int(sel.size))
+        self._check(lib().pbw_bam_write(self.h, C.byref(o), len(sources), arr, sp, ns, path.encode(),
+                                        1 if index else 0))
 
     def sort_coordinate(self, sources, sel=None) -> np.ndarray:
         """sort_for_coordinate_order (sam.rs:114-124) of the selected record

@@ -12,9 +12,10 @@
 // Two read files map as pairs (records interleaved mate 1, mate 2, lib.rs:
 // 171-181); one (or three and more) as single-end reads. --threads is accepted
 // and has no effect (the mapping runs on the GPU); --casava8 changes nothing
-// in the reference either (fastx.rs:29-41). BAM output (-f bam, and --index,
-// which needs it) is not built: the command stops with an error after the
-// same argument checks as the reference. Errors: usage errors exit 2, others
+// in the reference either (fastx.rs:29-41). -f bam writes BGZF BAM to the
+// --output file (required, as in the reference) and --index (which needs it)
+// coordinate-sorts the records on the GPU and writes FILE.bai beside it
+// (main.rs:162-186, pbw_bam_write). Errors: usage errors exit 2, others
 // print "Error: ..." and exit 1. build-genome / build-hash write the same
 // index files as the reference's subcommands (the hash table is built on the
 // GPU).
@@ -373,9 +374,16 @@ int run_map(int argc, char** argv) {
     sorted.resize(sel.size());
     sel.swap(sorted);
   }
-  if (outformat == "bam") throw Fail("BAM output is not built (SAM only)");
   pbw_sam_options so{cl.c_str(), have_rg ? rg.c_str() : nullptr, index ? 1 : 0};
   const uint64_t none = 0;  // an empty selection still passes a list (NULL means every record)
+  if (outformat == "bam") {
+    if (!a.has("output"))
+      throw Fail("--outputformat=bam requires --output FILE (binary output shouldn't go to a terminal)");
+    Timer tm("BAM (SAM formatted on the GPU, BGZF on the host threads)");
+    H.check(pbw_bam_write(H.h, &so, n_src, src, sel.empty() ? &none : sel.data(), sel.size(),
+                          a.get("output", "").c_str(), index ? 1 : 0));
+    return 0;
+  }
   Timer tm("SAM (format on the GPU + write)");
   H.check(pbw_sam_write(H.h, &so, n_src, src, sel.empty() ? &none : sel.data(), sel.size(),
                         a.get("output", "-").c_str()));
