@@ -7,15 +7,20 @@
 // The recurrences, tie rules and traceback are those of
 // SmithWatermanAligner::align (src/align/smith_waterman.rs:113-255).
 //
-// A window of n columns is cut into tiles of 32 columns; tile k belongs to
-// warp k mod 8. Inside a tile lane l owns column j = 32k + 1 + l and lags lane
-// l-1 by one row: at step t it computes cell (i = R0 + t - l, j). The left and
-// diagonal cells come from lane l-1 by __shfl_up_sync, the cell above is the
-// lane's own previous output. Lane 0 reads the left column from the boundary
-// buffer that tile k-1's lane 31 writes row by row into shared memory, so the
-// eight warps run as a wavefront over the tiles: warp w follows warp w-1 at a
-// distance of about 40 rows. The producer publishes its progress every 8 rows
-// (fence, then a volatile store); the consumer polls it with a bounded spin.
+// A window of n columns is cut into tiles of 128 columns; tile k belongs to
+// warp k mod 8. Inside a tile lane l owns the four columns
+// j = 128k + 4l + 1 .. 128k + 4l + 4 and lags lane l-1 by one row: at step t
+// it computes row i = R0 + t - l of its columns from left to right. The left
+// and diagonal cells of its first column come from lane l-1's last column by
+// __shfl_up_sync; every other input is in the lane's registers (its previous
+// row). Lane 0 reads the left column from the boundary buffer that tile
+// k-1's lane 31 writes row by row into shared memory, so the eight warps run
+// as a wavefront over the tiles: warp w follows warp w-1 at a distance of
+// about 40 rows, and a window of n columns takes about n/128 * 40 + m steps
+// (four columns per lane put four cells of work behind each step's shuffles,
+// boundary loads and progress checks). The producer publishes its progress
+// every 8 rows (fence, then a volatile store); the consumer polls it with a
+// bounded spin.
 //
 // Per job the window symbols, gap-open costs, traceback ops and the 4-bit
 // traceback nibbles live in shared memory when they fit the block's budget,
@@ -31,6 +36,8 @@ namespace pbw {
 
 constexpr int WIN_WARPS = 8;  // power of two
 constexpr int WIN_THREADS = WIN_WARPS * 32;
+constexpr int WIN_C = 4;                      // window columns per lane
+constexpr int WIN_TILE = 32 * WIN_C;          // columns per tile (one warp)
 constexpr int WIN_TAG = 4096;                 // > rows of any job
 constexpr unsigned WIN_SPIN_LIMIT = 1u << 22;  // polls before a wait gives up
 constexpr size_t WIN_SMEM_CAP = 110 * 1024;    // two blocks per SM
@@ -192,19 +199,30 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
     const int32_t ge = J.gap_extend;
     unsigned long long bestKey = 0;  // (value + 2^31) << 32 | j << 1 | state; 0 = none
     if (nrows > 0) {
-      const int NT = (n + 31) >> 5;
+      const int NT = (n + WIN_TILE - 1) / WIN_TILE;
       for (int k = wid; k < NT; k += WIN_WARPS) {
-        const int j = 1 + 32 * k + lane;
-        const bool col_on = j <= n;
-        const uint8_t rs_j = col_on ? rs[j - 1] : 0;
-        const int32_t go_j = col_on ? go[j - 1] : 0;
-        // rows of this column inside the band: js(i) <= j <= je(i)
-        int ilo = 1, ihi = 0;
-        if (col_on) {
-          const long long lo = (long long)j - J.hint - (long long)J.band;
-          const long long hi = (long long)j - J.hint + (long long)J.band;
-          ilo = (int)max((long long)R0, lo);
-          ihi = (int)min((long long)R1, hi);
+        const int j0 = 1 + WIN_TILE * k + WIN_C * lane;  // the lane's first column
+        uint32_t rs4 = 0;      // window symbols of the lane's columns, a byte each
+        int32_t goc[WIN_C];    // gap open of each column
+        int ilo[WIN_C], ihi[WIN_C];  // rows of each column inside the band: js(i) <= j <= je(i)
+        bool con[WIN_C];
+        bool all_full = true;
+#pragma unroll
+        for (int c = 0; c < WIN_C; c++) {
+          const int j = j0 + c;
+          con[c] = j <= n;
+          rs4 |= (uint32_t)(con[c] ? rs[j - 1] : 0) << (8 * c);
+          goc[c] = con[c] ? go[j - 1] : 0;
+          ilo[c] = 1;
+          ihi[c] = 0;
+          if (con[c]) {
+            const long long lo = (long long)j - J.hint - (long long)J.band;
+            const long long hi = (long long)j - J.hint + (long long)J.band;
+            ilo[c] = (int)min(max((long long)R0, lo), (long long)R1 + 1);
+            ihi[c] = (int)max(min((long long)R1, hi), (long long)R0 - 1);
+            if (ihi[c] >= ilo[c]) cells_acc += (unsigned long long)(ihi[c] - ilo[c] + 1);
+          }
+          all_full = all_full && con[c] && ilo[c] == R0 && ihi[c] == R1;
         }
         const int bin = (k - 1) & (WIN_WARPS - 1), bout = k & (WIN_WARPS - 1);
         const int32_t* inM = bufs + (size_t)(3 * bin) * bstride;
@@ -215,18 +233,26 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
         int32_t* outD = outI + bstride;
         const bool has_next = k + 1 < NT;
         const int tag_in = (k - 1) * WIN_TAG;
-        int32_t uM = col_on ? 0 : NEG, uI = NEG;   // cell above (own previous output)
-        int32_t rM = col_on ? 0 : NEG, rI = NEG, rD = NEG;  // received from lane - 1
-        int32_t qM = lane == 0 ? 0 : NEG, qI = NEG, qD = NEG;  // diagonal (left of the previous step)
-        uint32_t acc = 0;
-        uint32_t* tbcol = tb + (size_t)j * TBS;
-        // cells of this lane's column: rows [ilo, ihi]
-        if (col_on && ihi >= ilo) cells_acc += (unsigned long long)(ihi - ilo + 1);
+        // the lane's previous row per column (up and, one column right, diagonal);
+        // before row R0 it is the initial row (smith_waterman.rs:174-176)
+        int32_t PM[WIN_C], PI[WIN_C], PD[WIN_C];
+        uint32_t acc[WIN_C];
+#pragma unroll
+        for (int c = 0; c < WIN_C; c++) {
+          PM[c] = con[c] ? 0 : NEG;
+          PI[c] = NEG;
+          PD[c] = NEG;
+          acc[c] = 0;
+        }
+        int32_t rM = con[0] ? 0 : NEG, rI = NEG, rD = NEG;     // received from lane - 1
+        int32_t qM = lane == 0 ? 0 : NEG, qI = NEG, qD = NEG;  // diagonal of the first column
+        uint32_t* tbc = tb + (size_t)j0 * TBS;                 // column j0 + c at tbc + c * TBS
         const int T = nrows + 31;
-        // Steps where every lane's row is inside [R0, R1 - 1] and inside the
-        // band take the branch-free form below; the ramps at both ends (and
-        // tiles with a partial or banded column) take the general form.
-        const bool full_tile = __all_sync(0xffffffffu, col_on && ilo == R0 && ihi == R1);
+        // Steps where every lane's row is inside [R0, R1 - 1] and all of the
+        // tile's columns are in the window and the band take the branch-free
+        // form below; the ramps at both ends (and tiles with a partial or
+        // banded column) take the general form.
+        const bool full_tile = __all_sync(0xffffffffu, all_full);
         const int f0 = full_tile ? 31 : T, f1 = full_tile ? max(31, nrows - 1) : T;
         auto poll = [&](int t) {
           if (k > 0 && (t & 7) == 0 && t < nrows) {
@@ -245,12 +271,12 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
             __threadfence_block();
           }
         };
-        auto publish = [&](int t, int i, int32_t oM, int32_t oI, int32_t oD) {
+        auto publish = [&](int t, int i) {
           if (has_next) {
             if (lane == 31 && i >= R0 && i <= R1) {
-              outM[i] = oM;
-              outI[i] = oI;
-              outD[i] = oD;
+              outM[i] = PM[WIN_C - 1];
+              outI[i] = PI[WIN_C - 1];
+              outD[i] = PD[WIN_C - 1];
             }
             const int done = t - 30;  // rows R0 .. R0 + done - 1 written by lane 31
             if (done > 0 && ((done & 7) == 0 || done == nrows) && lane == 31) {
@@ -269,62 +295,70 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
             bI = inI[i0];
             bD = inD[i0];
           }
-          const int32_t lM = lane == 0 ? bM : rM;
-          const int32_t lI = lane == 0 ? bI : rI;
-          const int32_t lD = lane == 0 ? bD : rD;
-          const int32_t dM = qM, dI = qI, dD = qD;
-          int32_t oM, oI, oD;
-          if (i >= ilo && i <= ihi) {
-            const int32_t pv = pen[i - 1];
-            const int32_t sc = (uint8_t)pv == rs_j ? 20 : (pv >> 8);
-            const int32_t fm = dM + sc, fi = dI + sc, fd = dD + sc;
-            const int32_t Mv = max(max(fm, fi), fd);
-            const uint32_t tm = Mv == fm ? 0u : (Mv == fi ? 1u : 2u);
-            const int32_t io = uM + go_j, ie = uI + ge;
-            const int32_t Iv = max(io, ie);
-            const uint32_t ti = Iv == io ? 0u : 1u;
-            const int32_t dop = lM + go_j, dex = lD + ge;
-            const int32_t Dv = max(dop, dex);
-            const uint32_t td = Dv == dop ? 0u : 1u;
-            oM = Mv;
-            oI = Iv;
-            oD = Dv;
-            const int rr = i - R0;
-            acc |= (tm | (ti << 2) | (td << 3)) << ((rr & 7) * 4);
-            if ((rr & 7) == 7 || i == ihi) {
-              tbcol[rr >> 3] = acc;
-              acc = 0;
+          int32_t lM = lane == 0 ? bM : rM;  // (i, j0 - 1)
+          int32_t lD = lane == 0 ? bD : rD;
+          const int32_t nqM = lM, nqI = lane == 0 ? bI : rI, nqD = lD;
+          int32_t dgM = qM, dgI = qI, dgD = qD;  // (i - 1, j0 - 1)
+          const bool row_in = i >= R0 && i <= R1;
+          const int32_t pv = row_in ? pen[i - 1] : 0;
+          const uint32_t qsym = (uint32_t)pv & 0xFFu;
+          const int32_t mp = pv >> 8;
+          const int rr = i - R0;
+#pragma unroll
+          for (int c = 0; c < WIN_C; c++) {
+            const int32_t uM = PM[c], uI = PI[c], uD = PD[c];
+            int32_t oM, oI, oD;
+            if (i >= ilo[c] && i <= ihi[c]) {
+              const int32_t sc = ((rs4 >> (8 * c)) & 0xFFu) == qsym ? 20 : mp;
+              const int32_t m2 = max(max(dgM, dgI), dgD);
+              oM = m2 + sc;
+              const uint32_t tm = dgM == m2 ? 0u : (dgI == m2 ? 1u : 2u);
+              const int32_t io = uM + goc[c], ie = uI + ge;
+              oI = max(io, ie);
+              const int32_t dop = lM + goc[c], dex = lD + ge;
+              oD = max(dop, dex);
+              acc[c] |= (tm | (io >= ie ? 0u : 4u) | (dop >= dex ? 0u : 8u)) << ((rr & 7) * 4);
+              if ((rr & 7) == 7 || i == ihi[c]) {
+                tbc[(size_t)c * TBS + (rr >> 3)] = acc[c];
+                acc[c] = 0;
+              }
+              if (i == R1) {
+                const unsigned long long jj = (unsigned long long)(j0 + c);
+                const unsigned long long kM = ((unsigned long long)((long long)oM + 2147483648LL) << 32) | (jj << 1);
+                const unsigned long long kI =
+                    ((unsigned long long)((long long)oI + 2147483648LL) << 32) | (jj << 1) | 1ull;
+                bestKey = max(bestKey, max(kM, kI));
+              }
+            } else if (i == R0 - 1 && con[c]) {
+              oM = 0;  // initial row
+              oI = NEG;
+              oD = NEG;
+            } else {
+              oM = NEG;
+              oI = NEG;
+              oD = NEG;
             }
-            if (i == R1) {
-              const unsigned long long kM = ((unsigned long long)((long long)Mv + 2147483648LL) << 32) |
-                                            ((unsigned long long)j << 1);
-              const unsigned long long kI = ((unsigned long long)((long long)Iv + 2147483648LL) << 32) |
-                                            ((unsigned long long)j << 1) | 1ull;
-              bestKey = max(bestKey, max(kM, kI));
-            }
-          } else if (i == R0 - 1 && col_on) {
-            oM = 0;  // initial row (smith_waterman.rs:174-176)
-            oI = NEG;
-            oD = NEG;
-          } else {
-            oM = NEG;
-            oI = NEG;
-            oD = NEG;
+            PM[c] = oM;
+            PI[c] = oI;
+            PD[c] = oD;
+            dgM = uM;
+            dgI = uI;
+            dgD = uD;
+            lM = oM;
+            lD = oD;
           }
-          publish(t, i, oM, oI, oD);
-          uM = oM;
-          uI = oI;
-          qM = lM;
-          qI = lI;
-          qD = lD;
-          rM = __shfl_up_sync(0xffffffffu, oM, 1);
-          rI = __shfl_up_sync(0xffffffffu, oI, 1);
-          rD = __shfl_up_sync(0xffffffffu, oD, 1);
+          publish(t, i);
+          qM = nqM;
+          qI = nqI;
+          qD = nqD;
+          rM = __shfl_up_sync(0xffffffffu, PM[WIN_C - 1], 1);
+          rI = __shfl_up_sync(0xffffffffu, PI[WIN_C - 1], 1);
+          rD = __shfl_up_sync(0xffffffffu, PD[WIN_C - 1], 1);
         };
         int t = 0;
         for (; t < f0; t++) general(t);
         for (; t < f1; t++) {
-          // every lane in rows [R0, R1 - 1] of its in-band column
+          // every lane in rows [R0, R1 - 1], every column in the window and the band
           const int i = R0 + t - lane;
           poll(t);
           int32_t lM = rM, lI = rI, lD = rD;
@@ -340,30 +374,48 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
             lI = NEG;
             lD = NEG;
           }
+          const int32_t nqM = lM, nqI = lI, nqD = lD;
+          int32_t dgM = qM, dgI = qI, dgD = qD;
           const int32_t pv = pen[i - 1];
-          const int32_t sc = (uint8_t)pv == rs_j ? 20 : (pv >> 8);
-          const int32_t fm = qM + sc, fi = qI + sc, fd = qD + sc;
-          const int32_t Mv = max(max(fm, fi), fd);
-          const uint32_t tm = Mv == fm ? 0u : (Mv == fi ? 1u : 2u);
-          const int32_t io = uM + go_j, ie = uI + ge;
-          const int32_t Iv = max(io, ie);
-          const int32_t dop = lM + go_j, dex = lD + ge;
-          const int32_t Dv = max(dop, dex);
-          rM = __shfl_up_sync(0xffffffffu, Mv, 1);
-          rI = __shfl_up_sync(0xffffffffu, Iv, 1);
-          rD = __shfl_up_sync(0xffffffffu, Dv, 1);
+          const uint32_t qsym = (uint32_t)pv & 0xFFu;
+          const int32_t mp = pv >> 8;
           const int rr = i - R0;
-          acc |= (tm | (Iv == io ? 0u : 4u) | (Dv == dop ? 0u : 8u)) << ((rr & 7) * 4);
-          if ((rr & 7) == 7) {
-            tbcol[rr >> 3] = acc;
-            acc = 0;
+          const int sh = (rr & 7) * 4;
+#pragma unroll
+          for (int c = 0; c < WIN_C; c++) {
+            const int32_t uM = PM[c], uI = PI[c], uD = PD[c];
+            const int32_t sc = ((rs4 >> (8 * c)) & 0xFFu) == qsym ? 20 : mp;
+            const int32_t m2 = max(max(dgM, dgI), dgD);
+            const int32_t Mv = m2 + sc;
+            const uint32_t tm = dgM == m2 ? 0u : (dgI == m2 ? 1u : 2u);
+            const int32_t io = uM + goc[c], ie = uI + ge;
+            const int32_t Iv = max(io, ie);
+            const int32_t dop = lM + goc[c], dex = lD + ge;
+            const int32_t Dv = max(dop, dex);
+            acc[c] |= (tm | (io >= ie ? 0u : 4u) | (dop >= dex ? 0u : 8u)) << sh;
+            PM[c] = Mv;
+            PI[c] = Iv;
+            PD[c] = Dv;
+            dgM = uM;
+            dgI = uI;
+            dgD = uD;
+            lM = Mv;
+            lD = Dv;
           }
-          publish(t, i, Mv, Iv, Dv);
-          uM = Mv;
-          uI = Iv;
-          qM = lM;
-          qI = lI;
-          qD = lD;
+          rM = __shfl_up_sync(0xffffffffu, PM[WIN_C - 1], 1);
+          rI = __shfl_up_sync(0xffffffffu, PI[WIN_C - 1], 1);
+          rD = __shfl_up_sync(0xffffffffu, PD[WIN_C - 1], 1);
+          if ((rr & 7) == 7) {
+#pragma unroll
+            for (int c = 0; c < WIN_C; c++) {
+              tbc[(size_t)c * TBS + (rr >> 3)] = acc[c];
+              acc[c] = 0;
+            }
+          }
+          publish(t, i);
+          qM = nqM;
+          qI = nqI;
+          qD = nqD;
         }
         for (; t < T; t++) general(t);
       }

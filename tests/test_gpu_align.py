@@ -59,6 +59,21 @@ def _problems(seed, n, kind):
             exp = int(rng.integers(0, rad + 1))
             read = _mutate(rng, ref[exp:exp + L], 0.05, 0.02)
             probs.append((read, bytes(rng.integers(2, 42, size=len(read)).astype(np.uint8)), ref, exp, len(ref)))
+        elif kind == "wide":
+            # windows of up to 40 column tiles: every warp of the window DP
+            # takes several tiles and reuses its boundary buffer; half of
+            # them banded, with hints that start or end the band off the window
+            L = int(rng.integers(30, 320))
+            n = int(rng.integers(500, 5000))
+            ref = _b(rng.choice(list(b"ACGT"), size=n))
+            exp = int(rng.integers(0, n - L))
+            read = _mutate(rng, ref[exp:exp + L], 0.05, 0.03)
+            if rng.random() < 0.5:
+                probs.append((read, bytes(rng.integers(2, 42, size=len(read)).astype(np.uint8)), ref, exp, n))
+            else:
+                hint = int(rng.integers(-300, n + 300))
+                band = int(rng.integers(32, 700))
+                probs.append((read, bytes(rng.integers(2, 42, size=len(read)).astype(np.uint8)), ref, hint, band))
         else:  # arbitrary bands and hints, homopolymers and N
             L = int(rng.integers(1, 120))
             n = int(rng.integers(1, 220))
@@ -71,7 +86,7 @@ def _problems(seed, n, kind):
     return probs
 
 
-@pytest.mark.parametrize("kind,seed,n", [("seeded", 1, 3000), ("window", 2, 400), ("odd", 3, 3000)])
+@pytest.mark.parametrize("kind,seed,n", [("seeded", 1, 3000), ("window", 2, 400), ("odd", 3, 3000), ("wide", 4, 120)])
 def test_align_batch_matches_oracle(M, oracle, kind, seed, n):
     probs = _problems(seed, n, kind)
     got = M.align_batch(probs)
