@@ -118,6 +118,8 @@ typedef struct {
   uint64_t dp_jobs;           /* alignments */
   uint64_t dp_cells;          /* DP cells (smith_waterman.rs:191-203 bands) */
   uint64_t kernel_launches;   /* kernels launched by the call */
+  uint64_t window_jobs;       /* paired path: mate rescue / shortlist cross-alignments (also in dp_jobs) */
+  uint64_t window_cells;      /* their DP cells (also in dp_cells) */
 } pbw_stats;
 
 void pbw_default_options(pbw_options* opt);

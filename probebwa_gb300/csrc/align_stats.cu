@@ -27,6 +27,10 @@ template <bool EXPLICIT>
 __global__ void __launch_bounds__(128) k_aln_stats(AlignArgs p) {
   __shared__ double s_llk[2][256];
   __shared__ uint8_t s_code[256];
+  // launched for the largest job count of a batch: blocks past the real
+  // count leave before staging the tables (the whole block, so no barrier
+  // is left waiting)
+  if (blockIdx.x * blockDim.x >= *p.n_jobs) return;
   for (int k = threadIdx.x; k < 256; k += blockDim.x) {
     s_llk[0][k] = p.tab->llk_match[k];
     s_llk[1][k] = p.tab->llk_mismatch[k];

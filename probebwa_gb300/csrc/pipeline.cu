@@ -843,7 +843,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     aa.tb_smem = 0;
     aa.tb_global = h->d_tb_global.p;
     aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, wide_n);
-    aa.counters = h->d_cnt64.p + 3;
+    aa.counters = h->d_cnt64.p + 5;  // cross-alignment jobs and cells, apart from the seeded DP's
     aa.err = h->d_err.p;
     // One batch: decide -> cross-alignment DP -> statistics -> resolve, its
     // observations to the host, the fold there (the model of the next batch).
@@ -944,8 +944,10 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   h->stats.seed_probes = c64[0];
   h->stats.seed_entries = c64[1];
   h->stats.seed_hits = c64[2];
-  h->stats.dp_jobs = c64[3];
-  h->stats.dp_cells = c64[4];
+  h->stats.dp_jobs = c64[3] + c64[5];
+  h->stats.dp_cells = c64[4] + c64[6];
+  h->stats.window_jobs = c64[5];
+  h->stats.window_cells = c64[6];
   // outputs
   unsigned int tot[2];
   CK(cudaMemcpy(tot, h->d_cnt32.p + 4, 8, cudaMemcpyDeviceToHost));
