@@ -7,18 +7,20 @@
 // The recurrences, tie rules and traceback are those of
 // SmithWatermanAligner::align (src/align/smith_waterman.rs:113-255).
 //
-// A window of n columns is cut into tiles of 128 columns; tile k belongs to
-// warp k mod 8. Inside a tile lane l owns the four columns
-// j = 128k + 4l + 1 .. 128k + 4l + 4 and lags lane l-1 by one row: at step t
-// it computes row i = R0 + t - l of its columns from left to right. The left
+// A window of n columns is cut into tiles of 32C columns (C = 4 or 8 columns
+// per lane); tile k belongs to warp k mod 8. Inside a tile lane l owns the C
+// columns j = 32Ck + Cl + 1 .. 32Ck + Cl + C and lags lane l-1 by one row: at
+// step t it computes row i = R0 + t - l of its columns from left to right. The left
 // and diagonal cells of its first column come from lane l-1's last column by
 // __shfl_up_sync; every other input is in the lane's registers (its previous
 // row). Lane 0 reads the left column from the boundary buffer that tile
 // k-1's lane 31 writes row by row into shared memory, so the eight warps run
 // as a wavefront over the tiles: warp w follows warp w-1 at a distance of
-// about 40 rows, and a window of n columns takes about n/128 * 40 + m steps
-// (four columns per lane put four cells of work behind each step's shuffles,
-// boundary loads and progress checks). The producer publishes its progress
+// about 40 rows, and a window of n columns takes about n/(32C) * 40 + m steps
+// (C columns per lane put C cells of work behind each step's shuffles,
+// boundary loads and progress checks). Every step is free of divergent
+// branches: the ramps at both ends of a tile, partial and banded tiles
+// compute each cell and select its output by predicates. The producer publishes its progress
 // every 8 rows (fence, then a volatile store); the consumer polls it with a
 // bounded spin.
 //
@@ -36,8 +38,6 @@ namespace pbw {
 
 constexpr int WIN_WARPS = 8;  // power of two
 constexpr int WIN_THREADS = WIN_WARPS * 32;
-constexpr int WIN_C = 4;                      // window columns per lane
-constexpr int WIN_TILE = 32 * WIN_C;          // columns per tile (one warp)
 constexpr int WIN_TAG = 4096;                 // > rows of any job
 constexpr unsigned WIN_SPIN_LIMIT = 1u << 22;  // polls before a wait gives up
 constexpr size_t WIN_SMEM_CAP = 110 * 1024;    // two blocks per SM
@@ -74,7 +74,10 @@ struct XBand {
   }
 };
 
-__global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsigned int smem_total) {
+// WIN_C window columns per lane; MINB resident blocks per SM the registers allow.
+template <int WIN_C, int MINB>
+__global__ void __launch_bounds__(WIN_THREADS, MINB) k_align_window(AlignArgs p, unsigned int smem_total) {
+  constexpr int WIN_TILE = 32 * WIN_C;  // columns per tile (one warp)
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ unsigned int s_jid;
   __shared__ unsigned long long s_best;
@@ -202,27 +205,31 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
       const int NT = (n + WIN_TILE - 1) / WIN_TILE;
       for (int k = wid; k < NT; k += WIN_WARPS) {
         const int j0 = 1 + WIN_TILE * k + WIN_C * lane;  // the lane's first column
-        uint32_t rs4 = 0;      // window symbols of the lane's columns, a byte each
+        uint32_t rsc[WIN_C];   // window symbols of the lane's columns
         int32_t goc[WIN_C];    // gap open of each column
-        int ilo[WIN_C], ihi[WIN_C];  // rows of each column inside the band: js(i) <= j <= je(i)
+        int ilo[WIN_C], sp[WIN_C];   // rows ilo .. ilo + sp of each column inside the band: js(i) <= j <= je(i)
         bool con[WIN_C];
         bool all_full = true;
 #pragma unroll
         for (int c = 0; c < WIN_C; c++) {
           const int j = j0 + c;
           con[c] = j <= n;
-          rs4 |= (uint32_t)(con[c] ? rs[j - 1] : 0) << (8 * c);
+          rsc[c] = con[c] ? rs[j - 1] : 0u;
           goc[c] = con[c] ? go[j - 1] : 0;
-          ilo[c] = 1;
-          ihi[c] = 0;
+          ilo[c] = 1 << 30;  // empty: (unsigned)(i - ilo) is never <= sp
+          sp[c] = 0;
           if (con[c]) {
             const long long lo = (long long)j - J.hint - (long long)J.band;
             const long long hi = (long long)j - J.hint + (long long)J.band;
-            ilo[c] = (int)min(max((long long)R0, lo), (long long)R1 + 1);
-            ihi[c] = (int)max(min((long long)R1, hi), (long long)R0 - 1);
-            if (ihi[c] >= ilo[c]) cells_acc += (unsigned long long)(ihi[c] - ilo[c] + 1);
+            const int a = (int)min(max((long long)R0, lo), (long long)R1 + 1);
+            const int b = (int)max(min((long long)R1, hi), (long long)R0 - 1);
+            if (b >= a) {
+              ilo[c] = a;
+              sp[c] = b - a;
+              cells_acc += (unsigned long long)(b - a + 1);
+            }
           }
-          all_full = all_full && con[c] && ilo[c] == R0 && ihi[c] == R1;
+          all_full = all_full && con[c] && ilo[c] == R0 && ilo[c] + sp[c] == R1;
         }
         const int bin = (k - 1) & (WIN_WARPS - 1), bout = k & (WIN_WARPS - 1);
         const int32_t* inM = bufs + (size_t)(3 * bin) * bstride;
@@ -285,6 +292,10 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
             }
           }
         };
+        // Ramps, partial and banded tiles: every cell is computed and the
+        // output is selected (in the band: the cell; row R0 - 1 of a window
+        // column: the initial row; else NEG_INF), so that lanes at different
+        // rows take no divergent branches.
         auto general = [&](int t) {
           const int i = R0 + t - lane;
           const int i0 = R0 + t;  // lane 0's row
@@ -299,45 +310,41 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
           int32_t lD = lane == 0 ? bD : rD;
           const int32_t nqM = lM, nqI = lane == 0 ? bI : rI, nqD = lD;
           int32_t dgM = qM, dgI = qI, dgD = qD;  // (i - 1, j0 - 1)
-          const bool row_in = i >= R0 && i <= R1;
-          const int32_t pv = row_in ? pen[i - 1] : 0;
+          const int32_t pv = pen[min(max(i - 1, 0), m - 1)];
           const uint32_t qsym = (uint32_t)pv & 0xFFu;
           const int32_t mp = pv >> 8;
           const int rr = i - R0;
+          const int sh = (rr & 7) * 4;
+          const bool init_row = i == R0 - 1;
+          const bool last_row = i == R1;
 #pragma unroll
           for (int c = 0; c < WIN_C; c++) {
             const int32_t uM = PM[c], uI = PI[c], uD = PD[c];
-            int32_t oM, oI, oD;
-            if (i >= ilo[c] && i <= ihi[c]) {
-              const int32_t sc = ((rs4 >> (8 * c)) & 0xFFu) == qsym ? 20 : mp;
-              const int32_t m2 = max(max(dgM, dgI), dgD);
-              oM = m2 + sc;
-              const uint32_t tm = dgM == m2 ? 0u : (dgI == m2 ? 1u : 2u);
-              const int32_t io = uM + goc[c], ie = uI + ge;
-              oI = max(io, ie);
-              const int32_t dop = lM + goc[c], dex = lD + ge;
-              oD = max(dop, dex);
-              acc[c] |= (tm | (io >= ie ? 0u : 4u) | (dop >= dex ? 0u : 8u)) << ((rr & 7) * 4);
-              if ((rr & 7) == 7 || i == ihi[c]) {
-                tbc[(size_t)c * TBS + (rr >> 3)] = acc[c];
-                acc[c] = 0;
-              }
-              if (i == R1) {
-                const unsigned long long jj = (unsigned long long)(j0 + c);
-                const unsigned long long kM = ((unsigned long long)((long long)oM + 2147483648LL) << 32) | (jj << 1);
-                const unsigned long long kI =
-                    ((unsigned long long)((long long)oI + 2147483648LL) << 32) | (jj << 1) | 1ull;
-                bestKey = max(bestKey, max(kM, kI));
-              }
-            } else if (i == R0 - 1 && con[c]) {
-              oM = 0;  // initial row
-              oI = NEG;
-              oD = NEG;
-            } else {
-              oM = NEG;
-              oI = NEG;
-              oD = NEG;
+            const bool on = (unsigned)(i - ilo[c]) <= (unsigned)sp[c];
+            const int32_t sc = rsc[c] == qsym ? 20 : mp;
+            const int32_t m2 = max(max(dgM, dgI), dgD);
+            const int32_t Mv = m2 + sc;
+            const uint32_t tm = dgM == m2 ? 0u : (dgI == m2 ? 1u : 2u);
+            const int32_t io = uM + goc[c], ie = uI + ge;
+            const int32_t Iv = max(io, ie);
+            const int32_t dop = lM + goc[c], dex = lD + ge;
+            const int32_t Dv = max(dop, dex);
+            const uint32_t nib = tm | (io >= ie ? 0u : 4u) | (dop >= dex ? 0u : 8u);
+            acc[c] |= on ? nib << sh : 0u;
+            if (on && ((rr & 7) == 7 || i == ilo[c] + sp[c])) {
+              tbc[(size_t)c * TBS + (rr >> 3)] = acc[c];
+              acc[c] = 0;
             }
+            if (on && last_row) {
+              const unsigned long long jj = (unsigned long long)(j0 + c);
+              const unsigned long long kM = ((unsigned long long)((long long)Mv + 2147483648LL) << 32) | (jj << 1);
+              const unsigned long long kI =
+                  ((unsigned long long)((long long)Iv + 2147483648LL) << 32) | (jj << 1) | 1ull;
+              bestKey = max(bestKey, max(kM, kI));
+            }
+            const int32_t oM = on ? Mv : ((init_row && con[c]) ? 0 : NEG);
+            const int32_t oI = on ? Iv : NEG;
+            const int32_t oD = on ? Dv : NEG;
             PM[c] = oM;
             PI[c] = oI;
             PD[c] = oD;
@@ -384,7 +391,7 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
 #pragma unroll
           for (int c = 0; c < WIN_C; c++) {
             const int32_t uM = PM[c], uI = PI[c], uD = PD[c];
-            const int32_t sc = ((rs4 >> (8 * c)) & 0xFFu) == qsym ? 20 : mp;
+            const int32_t sc = rsc[c] == qsym ? 20 : mp;
             const int32_t m2 = max(max(dgM, dgI), dgD);
             const int32_t Mv = m2 + sc;
             const uint32_t tm = dgM == m2 ? 0u : (dgI == m2 ? 1u : 2u);
@@ -460,10 +467,19 @@ __global__ void __launch_bounds__(WIN_THREADS) k_align_window(AlignArgs p, unsig
   }
 }
 
-void launch_align_window(const AlignArgs& a, int grid, cudaStream_t st) {
+// wide: 8 columns per lane, one block per SM (the paired path's ~1,000
+// column windows, fewer jobs per batch than SMs: the job's latency is the
+// batch's); else 4 columns per lane and two blocks per SM (many narrower
+// windows: throughput).
+void launch_align_window(const AlignArgs& a, int grid, cudaStream_t st, bool wide) {
   const size_t sm = window_smem_bytes(a.lmax, a.nmax);
-  cudaFuncSetAttribute(k_align_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_align_window<<<grid, WIN_THREADS, sm, st>>>(a, (unsigned int)sm);
+  if (wide) {
+    cudaFuncSetAttribute(k_align_window<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_align_window<8, 1><<<std::max(1, grid / 2), WIN_THREADS, sm, st>>>(a, (unsigned int)sm);
+  } else {
+    cudaFuncSetAttribute(k_align_window<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_align_window<4, 2><<<grid, WIN_THREADS, sm, st>>>(a, (unsigned int)sm);
+  }
 }
 
 }  // namespace pbw

@@ -155,8 +155,10 @@ bool band_has_lanes16(int band_max);
 size_t band_tb_slab_bytes(int lmax, int nmax, int num_sms, int band_max);
 // K3w, one job per block of 8 warps; tb_global_per_warp is the global slab of
 // one block (window_slab_bytes), used by windows that do not fit the block's
-// shared memory.
-void launch_align_window(const AlignArgs& a, int grid, cudaStream_t st);
+// shared memory. wide: 8 window columns per lane and one block per SM, for
+// batches of fewer ~1,000-column windows than SMs (the paired path's
+// cross-alignments); else 4 columns per lane and two blocks per SM.
+void launch_align_window(const AlignArgs& a, int grid, cudaStream_t st, bool wide = false);
 size_t window_smem_bytes(int lmax, int nmax);
 // Likelihood, log_entropy counts and edit distance of every aligned job from
 // its CIGAR (after K3b / K3w); max_jobs bounds the device job count.

@@ -867,7 +867,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
         cudaMemcpyAsync(h->d_batch.p, h_batch, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st);
         launch_pair_decide(pg, st);
-        launch_align_window(aa, grid_w, st);
+        launch_align_window(aa, grid_w, st, true);
         launch_aln_stats(aa, (uint64_t)2000 * MAX_CROSS, st);
         launch_pair_resolve(pg, st);
         cudaMemcpyAsync(h_obs, h->d_obs_batch.p, 2000 * sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -893,7 +893,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       CK(cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st));
       launch_pair_decide(pa, st);
       const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, (uint64_t)pa.np * MAX_CROSS);
-      launch_align_window(aa, std::max(gw, 1), st);
+      launch_align_window(aa, std::max(gw, 1), st, true);
       launch_aln_stats(aa, (uint64_t)pa.np * MAX_CROSS, st);
       launch_pair_resolve(pa, st);
       // the next batch sees the model updated by this batch's observations
