@@ -258,6 +258,16 @@ int pbw_sam_format(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, co
 int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
                   const uint64_t* sel, uint64_t n_sel, const char* path, int32_t write_index);
 
+/* write_bam / write_bam_indexed (src/io/bam.rs:19-57) on SAM text as the
+ * reference calls them: the len bytes of sam (a header, then one record per
+ * line) are encoded as by pbw_bam_write, with the reference dictionary taken
+ * from the header's @SQ lines (SN, LN) as a SAM parser builds it. Host code;
+ * no handle or device. write_index needs @HD SO:coordinate and records in
+ * that order. Errors (pbw_last_error(NULL)): PBW_ERR_FORMAT (an @SQ line
+ * without SN or LN, a record that does not parse, an RNAME not in the
+ * dictionary), PBW_ERR_ARG, PBW_ERR_IO. */
+int pbw_bam_write_text(const char* sam, uint64_t len, const char* path, int32_t write_index);
+
 /* Coordinate order of the selected records (sort_for_coordinate_order,
  * sam.rs:114-124): stable sort by (index of the contig's name, the last
  * index when names repeat; position), unmapped records (pos 0) last, on the

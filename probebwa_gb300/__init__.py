@@ -151,6 +151,7 @@ def lib():
         L.pbw_sam_format.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, vp, u64, vp]
         L.pbw_sort_coordinate.argtypes = [vp, u32, C.POINTER(SamSourceC), vp, u64, vp]
         L.pbw_bam_write.argtypes = [vp, C.POINTER(SamOptionsC), u32, C.POINTER(SamSourceC), vp, u64, cp, C.c_int32]
+        L.pbw_bam_write_text.argtypes = [C.c_char_p, u64, cp, C.c_int32]
         L.pbw_build_genome.argtypes = [cp, cp, cp, u32, C.POINTER(cp)]
         L.pbw_get_tuning.argtypes = [vp, C.POINTER(TuningC)]
         L.pbw_set_tuning.argtypes = [vp, C.POINTER(TuningC)]
@@ -306,6 +307,18 @@ def load_reads(path: str, fasta: bool = False, quality_offset: int = 33, adapter
     finally:
         L.pbw_reads_free(h)
     return Reads(bases, quals, offs, ids)
+
+
+def bam_from_sam(sam: bytes, path: str, index: bool = False) -> None:
+    """write_bam / write_bam_indexed (src/io/bam.rs:19-57) on SAM text through
+    pbw_bam_write_text: the stream as BGZF BAM at path, the reference
+    dictionary from its @SQ lines, and a BAI at path + '.bai' when index is
+    set (an @HD SO:coordinate stream). Host code: no device is needed."""
+    L = lib()
+    sam = bytes(sam)
+    rc = L.pbw_bam_write_text(sam, len(sam), path.encode(), 1 if index else 0)
+    if rc != 0:
+        raise PbwError(rc, L.pbw_last_error(None).decode())
 
 
 def build_genome(out_prefix: str, fasta_paths, species: str = "species", assembly: str = "assembly") -> None:

@@ -32,6 +32,10 @@
 #include "../../include/probebwa_gpu.h"
 #include "pbw_pipeline.h"
 
+namespace pbw {
+void set_handleless_error(const std::string& s);
+}
+
 namespace {
 
 // ---- zlib, opened at run time (the z_stream of its public API, LP64) ----
@@ -409,52 +413,41 @@ bool write_all(const std::string& path, const std::vector<std::vector<unsigned c
 
 }  // namespace
 
-extern "C" int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
-                             const uint64_t* sel, uint64_t n_sel, const char* path, int32_t write_index) {
-  if (!h || !opt || !path) return PBW_ERR_ARG;
-  if (!zlib().ok) {
-    h->err = "BAM output needs libz.so.1";
-    return PBW_ERR_IO;
-  }
-  if (write_index && !opt->coordinate_sorted) {
-    h->err = "pbw_bam_write: an index needs coordinate-sorted records (coordinate_sorted = 1)";
-    return PBW_ERR_ARG;
-  }
-  // the SAM stream, formatted on the device
-  uint64_t len = 0;
-  int rc = pbw_sam_format(h, opt, n_src, src, sel, n_sel, nullptr, 0, &len);
-  if (rc != PBW_OK) return rc;
-  std::vector<char> text(len + 1);
-  rc = pbw_sam_format(h, opt, n_src, src, sel, n_sel, text.data(), len, &len);
-  if (rc != PBW_OK) return rc;
+namespace {
+
+// The BAM stream of a SAM text whose reference dictionary is names / lens:
+// the header lines verbatim, the references, every record line encoded,
+// BGZF blocks deflated on all host threads; with write_index the BAI of the
+// (coordinate-sorted) records next to it. Returns a PBW status and sets err.
+int bam_from_text(const char* text, size_t len, const std::vector<std::string>& names,
+                  const std::vector<uint64_t>& lens, const char* path, bool write_index, std::string& err) {
   // header lines, then records
   size_t hdr_end = 0;
   while (hdr_end < len && text[hdr_end] == '@') {
-    const char* nl = (const char*)memchr(text.data() + hdr_end, '\n', len - hdr_end);
-    hdr_end = nl ? (size_t)(nl - text.data()) + 1 : len;
+    const char* nl = (const char*)memchr(text + hdr_end, '\n', len - hdr_end);
+    hdr_end = nl ? (size_t)(nl - text) + 1 : len;
   }
   std::map<std::string, int32_t> refs;
-  for (size_t c = 0; c < h->names.size(); c++) refs.emplace(h->names[c], (int32_t)c);
+  for (size_t c = 0; c < names.size(); c++) refs.emplace(names[c], (int32_t)c);
   std::vector<unsigned char> u = {'B', 'A', 'M', 1};
   put32(u, (uint32_t)hdr_end);
-  u.insert(u.end(), text.data(), text.data() + hdr_end);
-  put32(u, (uint32_t)h->names.size());
-  for (size_t c = 0; c < h->names.size(); c++) {
-    put32(u, (uint32_t)(h->names[c].size() + 1));
-    u.insert(u.end(), h->names[c].begin(), h->names[c].end());
+  u.insert(u.end(), text, text + hdr_end);
+  put32(u, (uint32_t)names.size());
+  for (size_t c = 0; c < names.size(); c++) {
+    put32(u, (uint32_t)(names[c].size() + 1));
+    u.insert(u.end(), names[c].begin(), names[c].end());
     u.push_back(0);
-    put32(u, (uint32_t)h->lens[c]);
+    put32(u, (uint32_t)lens[c]);
   }
   std::vector<RecIdx> recs;
-  recs.reserve(n_sel);
-  std::string err;
   for (size_t p = hdr_end; p < len;) {
-    const char* nl = (const char*)memchr(text.data() + p, '\n', len - p);
-    const size_t e = nl ? (size_t)(nl - text.data()) : len;
+    const char* nl = (const char*)memchr(text + p, '\n', len - p);
+    const size_t e = nl ? (size_t)(nl - text) : len;
     RecIdx ix;
     ix.u0 = u.size();
-    if (!encode_record(text.data() + p, e - p, refs, u, ix, err)) {
-      h->err = "BAM: record " + std::to_string(recs.size()) + ": " + err;
+    std::string rerr;
+    if (!encode_record(text + p, e - p, refs, u, ix, rerr)) {
+      err = "BAM: record " + std::to_string(recs.size()) + ": " + rerr;
       return PBW_ERR_FORMAT;
     }
     ix.u1 = u.size();
@@ -477,22 +470,111 @@ extern "C" int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t
     });
   for (auto& t : th) t.join();
   if (bad) {
-    h->err = "BAM: deflate failed";
+    err = "BAM: deflate failed";
     return PBW_ERR_IO;
   }
   blocks[nb].assign(BGZF_EOF, BGZF_EOF + sizeof(BGZF_EOF));
-  if (!write_all(path, blocks, err)) {
-    h->err = err;
-    return PBW_ERR_IO;
-  }
+  if (!write_all(path, blocks, err)) return PBW_ERR_IO;
   if (write_index) {
     std::vector<uint64_t> coff(nb + 1, 0);
     for (size_t b = 0; b < nb; b++) coff[b + 1] = coff[b] + blocks[b].size();
-    std::vector<std::vector<unsigned char>> bai(1, build_bai(recs, h->names.size(), coff));
-    if (!write_all(std::string(path) + ".bai", bai, err)) {
-      h->err = err;
-      return PBW_ERR_IO;
-    }
+    std::vector<std::vector<unsigned char>> bai(1, build_bai(recs, names.size(), coff));
+    if (!write_all(std::string(path) + ".bai", bai, err)) return PBW_ERR_IO;
   }
   return PBW_OK;
+}
+
+// The @HD line's SO value and the @SQ dictionary (SN, LN) of a SAM header,
+// as a SAM parser reads them. False for an @SQ line without SN or a valid LN.
+bool parse_sam_header(const char* text, size_t len, std::string& sort_order, std::vector<std::string>& names,
+                      std::vector<uint64_t>& lens, std::string& err) {
+  size_t p = 0;
+  while (p < len && text[p] == '@') {
+    const char* nl = (const char*)memchr(text + p, '\n', len - p);
+    const size_t e = nl ? (size_t)(nl - text) : len;
+    const std::string line(text + p, e - p);
+    std::vector<std::string> f;
+    for (size_t a = 0;;) {
+      const size_t b = line.find('\t', a);
+      f.push_back(line.substr(a, b == std::string::npos ? std::string::npos : b - a));
+      if (b == std::string::npos) break;
+      a = b + 1;
+    }
+    if (f[0] == "@HD") {
+      for (size_t k = 1; k < f.size(); k++)
+        if (f[k].compare(0, 3, "SO:") == 0) sort_order = f[k].substr(3);
+    } else if (f[0] == "@SQ") {
+      std::string sn;
+      bool have_ln = false;
+      uint64_t ln = 0;
+      for (size_t k = 1; k < f.size(); k++) {
+        if (f[k].compare(0, 3, "SN:") == 0) sn = f[k].substr(3);
+        if (f[k].compare(0, 3, "LN:") == 0) {
+          const std::string v = f[k].substr(3);
+          have_ln = !v.empty() && v.size() <= 10 && v.find_first_not_of("0123456789") == std::string::npos;
+          if (have_ln) ln = std::stoull(v);
+          have_ln = have_ln && ln >= 1 && ln <= 0x7FFFFFFFull;
+        }
+      }
+      if (sn.empty() || !have_ln) {
+        err = "BAM: @SQ line without SN or a valid LN: " + line;
+        return false;
+      }
+      names.push_back(sn);
+      lens.push_back(ln);
+    }
+    p = e + 1;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
+                             const uint64_t* sel, uint64_t n_sel, const char* path, int32_t write_index) {
+  if (!h || !opt || !path) return PBW_ERR_ARG;
+  if (!zlib().ok) {
+    h->err = "BAM output needs libz.so.1";
+    return PBW_ERR_IO;
+  }
+  if (write_index && !opt->coordinate_sorted) {
+    h->err = "pbw_bam_write: an index needs coordinate-sorted records (coordinate_sorted = 1)";
+    return PBW_ERR_ARG;
+  }
+  // the SAM stream, formatted on the device
+  uint64_t len = 0;
+  int rc = pbw_sam_format(h, opt, n_src, src, sel, n_sel, nullptr, 0, &len);
+  if (rc != PBW_OK) return rc;
+  std::vector<char> text(len + 1);
+  rc = pbw_sam_format(h, opt, n_src, src, sel, n_sel, text.data(), len, &len);
+  if (rc != PBW_OK) return rc;
+  std::string err;
+  rc = bam_from_text(text.data(), len, h->names, h->lens, path, write_index != 0, err);
+  if (rc != PBW_OK) h->err = err;
+  return rc;
+}
+
+extern "C" int pbw_bam_write_text(const char* sam, uint64_t len, const char* path, int32_t write_index) {
+  if (!sam || !path) {
+    pbw::set_handleless_error("pbw_bam_write_text: NULL text or path");
+    return PBW_ERR_ARG;
+  }
+  if (!zlib().ok) {
+    pbw::set_handleless_error("BAM output needs libz.so.1");
+    return PBW_ERR_IO;
+  }
+  std::string so, err;
+  std::vector<std::string> names;
+  std::vector<uint64_t> lens;
+  if (!parse_sam_header(sam, (size_t)len, so, names, lens, err)) {
+    pbw::set_handleless_error(err);
+    return PBW_ERR_FORMAT;
+  }
+  if (write_index && so != "coordinate") {
+    pbw::set_handleless_error("pbw_bam_write_text: an index needs a coordinate-sorted stream (@HD SO:coordinate)");
+    return PBW_ERR_ARG;
+  }
+  const int rc = bam_from_text(sam, (size_t)len, names, lens, path, write_index != 0, err);
+  if (rc != PBW_OK) pbw::set_handleless_error(err);
+  return rc;
 }
