@@ -156,9 +156,14 @@ struct pbw_handle {
   pbw::HostBuf h_stage;
   pbw::HostBuf h_fold;  // one batch's insert-size observations + the model
   std::vector<cudaEvent_t> events;
+  // paired calls: reads go up on a copy stream, one event per super-chunk
+  cudaStream_t st_up = nullptr;
+  std::vector<cudaEvent_t> up_ev;
   pbw_stats stats{};
   ~pbw_handle() {
     for (auto e : events) cudaEventDestroy(e);
+    for (auto e : up_ev) cudaEventDestroy(e);
+    if (st_up) cudaStreamDestroy(st_up);
     if (st) cudaStreamDestroy(st);
   }
 };

@@ -662,13 +662,46 @@ static std::vector<std::pair<uint64_t, uint64_t>> pair_batches(uint64_t n) {
   return b;
 }
 
+// Super-chunks of a paired call: whole batches, at most S pairs; pairs
+// [a, b) and batches [bi, be).
+struct SuperChunk {
+  uint64_t a, b;
+  size_t bi, be;
+};
+static std::vector<SuperChunk> pair_super_chunks(const std::vector<std::pair<uint64_t, uint64_t>>& batches,
+                                                 uint64_t S) {
+  std::vector<SuperChunk> out;
+  size_t bi = 0;
+  while (bi < batches.size()) {
+    const uint64_t a = batches[bi].first;
+    size_t be = bi;
+    uint64_t b = a;
+    while (be < batches.size() && batches[be].first + batches[be].second - a <= S) {
+      b = batches[be].first + batches[be].second;
+      be++;
+    }
+    out.push_back({a, b, bi, be});
+    bi = be;
+  }
+  return out;
+}
+static uint64_t pair_super_chunk_pairs(const pbw_handle* h) { return std::max<uint64_t>(h->opt.chunk_reads, 2000); }
+
+// up_ev: when the reads are still being copied up, event k marks the reads
+// of super-chunk k on the device (the compute stream waits for it).
 static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t* b1, const uint8_t* q1,
                           const uint64_t* of1, const uint8_t* b2, const uint8_t* q2, const uint64_t* of2, uint64_t n,
-                          uint64_t tot1, uint64_t tot2, int lmax, pbw_records* o1, pbw_records* o2) {
+                          uint64_t tot1, uint64_t tot2, int lmax, pbw_records* o1, pbw_records* o2,
+                          const std::vector<cudaEvent_t>* up_ev) {
   cudaStream_t st = h->st;
   const auto batches = pair_batches(n);
   // super-chunks: whole batches, at most chunk_reads pairs
-  const uint64_t S = std::max<uint64_t>(h->opt.chunk_reads, 2000);
+  const uint64_t S = pair_super_chunk_pairs(h);
+  const std::vector<SuperChunk> chunks = pair_super_chunks(batches, S);
+  if (up_ev && up_ev->size() < chunks.size()) {
+    h->err = "internal: fewer upload events than super-chunks";
+    return PBW_ERR_ARG;
+  }
   ChunkCfg cfg = chunk_cfg(h, std::min<uint64_t>(n, S), lmax);
   cfg.ch = (uint32_t)std::min<uint64_t>(n, S);
   TRY(ensure_chunk(h, cfg));
@@ -713,16 +746,12 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   CK(cudaMemsetAsync(h->d_cnt64.p, 0, 16 * sizeof(unsigned long long), st));
   cudaEvent_t* ev = &h->events[2];
   double t_seed = 0, t_cl = 0, t_al = 0, t_pair = 0, t_fin = 0;
-  size_t bi = 0;
-  while (bi < batches.size()) {
-    const uint64_t a = batches[bi].first;
-    size_t be = bi;
-    uint64_t b = a;
-    while (be < batches.size() && batches[be].first + batches[be].second - a <= S) {
-      b = batches[be].first + batches[be].second;
-      be++;
-    }
+  for (size_t sc = 0; sc < chunks.size(); sc++) {
+    const uint64_t a = chunks[sc].a, b = chunks[sc].b;
+    const size_t bi = chunks[sc].bi, be = chunks[sc].be;
     const uint32_t nr = (uint32_t)(b - a);
+    // this super-chunk's reads are on the device
+    if (up_ev) CK(cudaStreamWaitEvent(st, (*up_ev)[sc], 0));
     // phase A: both mates through K1-K3 and the per-read summaries
     MateBufs m1{h->d_cand.p, h->d_n_cand.p, h->d_aln.p, h->d_rep.p, 0};
     MateBufs m2{h->d_cand2.p, h->d_n_cand2.p, h->d_aln2.p, h->d_rep2.p, 0};
@@ -930,7 +959,6 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     CK(cudaEventSynchronize(ev[2]));
     t_pair += ms_between(ev[0], ev[1]);
     t_fin += ms_between(ev[1], ev[2]);
-    bi = be;
   }
   CK(cudaStreamSynchronize(st));
   TRY(check_device_errors(h));
@@ -1040,16 +1068,47 @@ int pbw_map_paired(pbw_handle* h, pbw_insert_model* model, const pbw_reads* r1, 
     if (o2->cigar_off) o2->cigar_off[0] = 0;
     return PBW_OK;
   }
-  cudaEvent_t a = h->events[30], b = h->events[31];
+  // The reads go up on a copy stream one super-chunk at a time (the offsets
+  // with the first), so that super-chunk k + 1 is copied while k is mapped;
+  // each super-chunk's seeding waits for its event.
+  TRY(grow(h, h->d_bases, t1 + 16));
+  TRY(grow(h, h->d_quals, t1 + 16));
+  TRY(grow(h, h->d_offs, n + 1));
+  TRY(grow(h, h->d_bases2, t2 + 16));
+  TRY(grow(h, h->d_quals2, t2 + 16));
+  TRY(grow(h, h->d_offs2, n + 1));
+  if (!h->st_up) CK(cudaStreamCreateWithFlags(&h->st_up, cudaStreamNonBlocking));
+  const std::vector<SuperChunk> chunks = pair_super_chunks(pair_batches(n), pair_super_chunk_pairs(h));
+  while (h->up_ev.size() < chunks.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    h->up_ev.push_back(e);
+  }
+  cudaEvent_t a = h->events[30];
   CK(cudaEventRecord(a, h->st));
-  TRY(upload_reads(h, r1, t1, h->d_bases, h->d_quals, h->d_offs));
-  TRY(upload_reads(h, r2, t2, h->d_bases2, h->d_quals2, h->d_offs2));
-  CK(cudaEventRecord(b, h->st));
+  CK(cudaStreamWaitEvent(h->st_up, a, 0));
+  cudaStream_t su = h->st_up;
+  CK(cudaMemcpyAsync(h->d_offs.p, r1->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, su));
+  CK(cudaMemcpyAsync(h->d_offs2.p, r2->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, su));
+  for (size_t k = 0; k < chunks.size(); k++) {
+    const pbw_reads* rr[2] = {r1, r2};
+    uint8_t* db[2] = {h->d_bases.p, h->d_bases2.p};
+    uint8_t* dq[2] = {h->d_quals.p, h->d_quals2.p};
+    for (int m = 0; m < 2; m++) {
+      const uint64_t x0 = rr[m]->offsets[chunks[k].a], x1 = rr[m]->offsets[chunks[k].b];
+      if (x1 > x0) {
+        CK(cudaMemcpyAsync(db[m] + x0, rr[m]->bases + x0, x1 - x0, cudaMemcpyHostToDevice, su));
+        CK(cudaMemcpyAsync(dq[m] + x0, rr[m]->quals + x0, x1 - x0, cudaMemcpyHostToDevice, su));
+      }
+    }
+    CK(cudaEventRecord(h->up_ev[k], su));
+  }
   TRY(map_paired_dev(h, model, h->d_bases.p, h->d_quals.p, h->d_offs.p, h->d_bases2.p, h->d_quals2.p,
-                     h->d_offs2.p, n, t1, t2, std::max(l1, l2), o1, o2));
-  h->stats.ms_h2d = ms_between(a, b);
-  h->stats.ms_total = h->stats.ms_h2d + h->stats.ms_seed + h->stats.ms_cluster + h->stats.ms_align +
-                      h->stats.ms_pair + h->stats.ms_finalize + h->stats.ms_d2h;
+                     h->d_offs2.p, n, t1, t2, std::max(l1, l2), o1, o2, &h->up_ev));
+  // copy time the mapping could not hide (until the first super-chunk was
+  // up), and the whole call from the first copy to the last record read back
+  h->stats.ms_h2d = ms_between(a, h->up_ev[0]);
+  h->stats.ms_total = ms_between(a, h->events[21]);
   return PBW_OK;
 }
 

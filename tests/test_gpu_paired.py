@@ -108,3 +108,41 @@ def test_super_chunks_are_invisible(P, oracle, tmp_path):
     R1 = P.Reads.from_lists(s1, q1)
     R2 = P.Reads.from_lists(s2, q2)
     _pair_parity(P, oracle, prefix, R1, R2, "chunk=2000", chunk_reads=2000)
+
+
+def test_pinned_inputs_upload_per_super_chunk(P, tmp_path):
+    """From pinned host memory the reads are copied up one super-chunk at a
+    time while earlier super-chunks are mapped: the records are those of the
+    same call from pageable memory (copied before mapping starts)."""
+    torch = pytest.importorskip("torch")
+    from probebwa_gb300 import synth
+    contigs = _paired_genome(33, n_contigs=2, contig_len=200_000)
+    prefix = str(tmp_path / "g")
+    synth.write_index(prefix, contigs)
+    s1, q1, s2, q2, _ = synth.reads_paired(34, contigs, 9000, L=150)
+    R1 = P.Reads.from_lists(s1, q1)
+    R2 = P.Reads.from_lists(s2, q2)
+    keep = []
+
+    def pinned(a):
+        t = torch.empty(max(a.nbytes, 1), dtype=torch.uint8, pin_memory=True)
+        keep.append(t)
+        v = t.numpy()[:a.nbytes].view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return v
+
+    P1 = P.Reads(pinned(R1.bases), pinned(R1.quals), pinned(R1.offsets))
+    P2 = P.Reads(pinned(R2.bases), pinned(R2.quals), pinned(R2.offsets))
+    assert P1.bases.ctypes.data == keep[0].data_ptr()  # no copy back to pageable memory
+    with P.Mapper(prefix, chunk_reads=2000) as m:
+        a1, a2, am = m.map_paired(R1, R2)
+        b1, b2, bm = m.map_paired(P1, P2)
+        st = m.stats()
+    assert am == bm
+    for x, y in ((a1, b1), (a2, b2)):
+        for k in ("contig", "pos", "mapq", "flag", "mate_contig", "mate_pos", "tlen", "as_score", "nm", "cigar_off"):
+            assert np.array_equal(x[k], y[k]), k
+        n = int(x["cigar_off"][-1])
+        assert np.array_equal(x["cigar"][:n], y["cigar"][:n])
+        assert np.array_equal(x["log_lk"].view(np.uint64), y["log_lk"].view(np.uint64))
+    assert st["ms_total"] > 0 and st["ms_h2d"] >= 0
