@@ -20,6 +20,7 @@
 // coordinate order with --index, a BAI with its magic.
 #include <algorithm>
 #include <atomic>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -154,6 +155,7 @@ struct Field {
   bool is(const char* s) const { return n == strlen(s) && memcmp(p, s, n) == 0; }
 };
 
+// A decimal integer of at most 18 digits (no overflow), optionally signed.
 bool parse_i64(const Field& f, int64_t& v) {
   if (f.n == 0) return false;
   size_t i = 0;
@@ -162,7 +164,7 @@ bool parse_i64(const Field& f, int64_t& v) {
     neg = f.p[0] == '-';
     i = 1;
   }
-  if (i == f.n) return false;
+  if (i == f.n || f.n - i > 18) return false;
   int64_t x = 0;
   for (; i < f.n; i++) {
     if (f.p[i] < '0' || f.p[i] > '9') return false;
@@ -195,9 +197,11 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
     return it == refs.end() ? -2 : it->second;
   };
   int64_t flag, pos, mapq, pnext, tlen;
+  constexpr int64_t POS_MAX = 0x7FFFFFFF;  // SAM POS / PNEXT / TLEN ranges (int32 in BAM)
   if (!parse_i64(f[1], flag) || !parse_i64(f[3], pos) || !parse_i64(f[4], mapq) || !parse_i64(f[7], pnext) ||
-      !parse_i64(f[8], tlen) || flag < 0 || flag > 0xFFFF || mapq < 0 || mapq > 255) {
-    err = "SAM record with a malformed number";
+      !parse_i64(f[8], tlen) || flag < 0 || flag > 0xFFFF || mapq < 0 || mapq > 255 || pos < 0 || pos > POS_MAX ||
+      pnext < 0 || pnext > POS_MAX || tlen < -POS_MAX || tlen > POS_MAX) {
+    err = "SAM record with a malformed or out-of-range number";
     return false;
   }
   const int32_t ref = ref_of(f[2], -1);
@@ -221,6 +225,10 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
       if (c >= '0' && c <= '9') {
         v = v * 10 + (c - '0');
         any = true;
+        if (v >= (1 << 28)) {  // BAM operation lengths have 28 bits
+          err = "CIGAR operation too long";
+          return false;
+        }
         continue;
       }
       const char* ops = "MIDNSHP=X";
@@ -237,6 +245,10 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
     }
     if (any) {
       err = "invalid CIGAR";
+      return false;
+    }
+    if (cig.size() > 0xFFFF) {  // the 16-bit operation count of a BAM record
+      err = "CIGAR with more than 65535 operations";
       return false;
     }
   }
@@ -286,7 +298,7 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
       aux.push_back(0);
     } else if (t.p[3] == 'i') {
       int64_t v;
-      if (!parse_i64(Field{t.p + 5, t.n - 5}, v)) {
+      if (!parse_i64(Field{t.p + 5, t.n - 5}, v) || v < INT32_MIN || v > INT32_MAX) {
         err = "invalid optional field";
         return false;
       }
@@ -301,6 +313,10 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
   const bool unmapped = (flag & 4) != 0;
   const int64_t beg = p0 < 0 ? -1 : p0;
   const int64_t end = beg < 0 ? 0 : beg + (span > 0 && !unmapped ? span : 1);
+  if (end > POS_MAX + 1) {
+    err = "alignment ends beyond 2^31";
+    return false;
+  }
   ix.ref = ref;
   ix.beg = beg;
   ix.end = end;

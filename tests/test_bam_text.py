@@ -101,3 +101,46 @@ def test_refusals(P, mapped, oracle):
     no_ln = sam.replace(sq[0], b"\t".join(f for f in sq[0].split(b"\t") if not f.startswith(b"LN:")))
     with pytest.raises(P.PbwError, match="SQ"):
         P.bam_from_sam(no_ln, str(d / "l.bam"))
+
+
+HDR = b"@HD\tVN:1.6\tSO:unsorted\n@SQ\tSN:c1\tLN:1000\n"
+
+
+@pytest.mark.parametrize("rec,why", [
+    (b"r1\t0\tc1\t10\t60\t4M\t*\t0\t0\tACGT", "fewer than 11 fields"),
+    (b"r1\t0\tc1\t10\t60\t4M\t*\t0\t0\tACGT\tIIII\tXX", "optional field"),
+    (b"r1\t0\tc1\t99999999999999999999999\t60\t4M\t*\t0\t0\tACGT\tIIII", "number"),
+    (b"r1\t0\tc1\t2147483648\t60\t4M\t*\t0\t0\tACGT\tIIII", "number"),
+    (b"r1\t0\tc1\t10\t256\t4M\t*\t0\t0\tACGT\tIIII", "number"),
+    (b"r1\t0\tc1\t10\t60\t4M\t*\t0\t-2147483648\tACGT\tIIII", "number"),
+    (b"r1\t0\tc1\t10\t60\t268435456M\t*\t0\t0\tACGT\tIIII", "CIGAR"),
+    (b"r1\t0\tc1\t10\t60\t99999999999999999999M\t*\t0\t0\tACGT\tIIII", "CIGAR"),
+    (b"r1\t0\tc1\t10\t60\t4Q\t*\t0\t0\tACGT\tIIII", "CIGAR"),
+    (b"r1\t0\tc1\t10\t60\tM\t*\t0\t0\tACGT\tIIII", "CIGAR"),
+    (b"r1\t0\tc1\t2147483000\t60\t100000M\t*\t0\t0\tACGT\tIIII", "2\\^31"),
+    (b"r1\t0\tc2\t10\t60\t4M\t*\t0\t0\tACGT\tIIII", "missing from the header"),
+    (b"r1\t0\tc1\t10\t60\t4M\t*\t0\t0\tAC!T\tIIII", "sequence base"),
+    (b"r1\t0\tc1\t10\t60\t4M\t*\t0\t0\tACGT\tIII", "differ in length"),
+    (b"r1\t0\tc1\t10\t60\t4M\t*\t0\t0\tACGT\tIIII\tNM:i:99999999999", "optional field"),
+    (b"r1\t0\tc1\t10\t60\t4M\t*\t0\t0\tACGT\tIIII\tXA:f:1.5", "optional field type"),
+    (b"\t0\tc1\t10\t60\t4M\t*\t0\t0\tACGT\tIIII", "read name"),
+])
+def test_malformed_records_are_errors(P, tmp_path, rec, why):
+    """Caller text is parsed defensively: every malformed or out-of-range
+    record is an error naming the record, never a crash or a silently
+    truncated field."""
+    with pytest.raises(P.PbwError, match=why):
+        P.bam_from_sam(HDR + rec + b"\n", str(tmp_path / "m.bam"))
+
+
+def test_well_formed_record_round_trip(P, tmp_path):
+    rec = b"r1\t16\tc1\t10\t60\t2M1I1M\t=\t100\t-5\tACGT\t!I~5\tRG:Z:g1\tNM:i:-3\n"
+    path = str(tmp_path / "ok.bam")
+    P.bam_from_sam(HDR + rec, path)
+    text, refs, recs = decode_bam(open(path, "rb").read())
+    assert refs == [("c1", 1000)] and len(recs) == 1
+    r = recs[0]
+    assert (r["name"], r["flag"], r["ref"], r["pos"], r["mapq"], r["cigar"]) == ("r1", 16, 0, 9, 60, "2M1I1M")
+    assert (r["nref"], r["npos"], r["tlen"], r["seq"]) == (0, 99, -5, "ACGT")
+    assert r["qual"] == bytes([0, 40, 93, 20])
+    assert r["aux"] == b"RGZg1\0" + b"NMi" + (-3).to_bytes(4, "little", signed=True)
