@@ -270,24 +270,41 @@ static int load_hash(pbw_handle* h, const std::string& prefix) {
   DevBuf<uint32_t> d_tab;
   DevBuf<unsigned long long> d_pos;
   TRY(dev_alloc(h, d_tab, std::max<uint64_t>(3 * n, 1)));
-  const size_t CH = 64ull << 20;
+  // (key, offset, count) entries as they stream past: the sum of the counts
+  // and the furthest bucket end
+  uint64_t sum_cnt = 0, max_end = 0;
+  auto tally = [&](const uint8_t* p, size_t c) {
+    for (size_t o = 0; o + 12 <= c; o += 12) {
+      uint32_t off, cnt;
+      memcpy(&off, p + o + 4, 4);
+      memcpy(&cnt, p + o + 8, 4);
+      sum_cnt += cnt;
+      max_end = std::max<uint64_t>(max_end, (uint64_t)off + cnt);
+    }
+  };
+  // chunks hold whole 12-byte table entries and whole 8-byte positions
+  const size_t CH = 48ull << 20;
   std::vector<uint8_t> buf(CH);
-  auto stream_to = [&](void* dst, uint64_t bytes) -> bool {
+  auto stream_to = [&](void* dst, uint64_t bytes, bool table) -> bool {
     uint64_t done = 0;
     while (done < bytes) {
       size_t c = (size_t)std::min<uint64_t>(CH, bytes - done);
       if (!fr.read(buf.data(), c)) return false;
+      if (table) tally(buf.data(), c);
       if (cudaMemcpy((char*)dst + done, buf.data(), c, cudaMemcpyHostToDevice) != cudaSuccess) return false;
       done += c;
     }
     return true;
   };
-  if (!stream_to(d_tab.p, 12 * n)) { h->err = "sthash: truncated table"; return PBW_ERR_FORMAT; }
+  if (!stream_to(d_tab.p, 12 * n, true)) { h->err = "sthash: truncated table"; return PBW_ERR_FORMAT; }
   uint64_t np;
   if (!fr.u64(np)) { h->err = "sthash: truncated positions"; return PBW_ERR_FORMAT; }
   if (np >= (1ull << 32)) { h->err = "sthash: more than 2^32 occurrences"; return PBW_ERR_LIMIT; }
+  // every bucket inside the positions and the buckets no larger than them
+  // together: the CSR fill below then reads and writes in bounds
+  if (max_end > np || sum_cnt > np) { h->err = "sthash: table entries point beyond the positions"; return PBW_ERR_FORMAT; }
   TRY(dev_alloc(h, d_pos, std::max<uint64_t>(np, 1)));
-  if (!stream_to(d_pos.p, 8 * np)) { h->err = "sthash: truncated positions"; return PBW_ERR_FORMAT; }
+  if (!stream_to(d_pos.p, 8 * np, false)) { h->err = "sthash: truncated positions"; return PBW_ERR_FORMAT; }
   uint64_t k, stride, total;
   if (!fr.u64(k) || !fr.u64(stride) || !fr.u64(total)) { h->err = "sthash: truncated trailer"; return PBW_ERR_FORMAT; }
   if (k != (uint64_t)KMER) { h->err = "sthash: k != 15 is not supported by the device path"; return PBW_ERR_LIMIT; }
@@ -296,9 +313,24 @@ static int load_hash(pbw_handle* h, const std::string& prefix) {
   TRY(dev_alloc(h, h->d_csr, NKMER + 1));
   TRY(dev_alloc(h, h->d_ent, std::max<uint64_t>(np, 1)));
   TRY(dev_alloc(h, h->d_err, 4));
-  CK(cudaMemset(h->d_err.p, 0, 16));
-  CK(cudaMemset(h->d_csr.p, 0, (NKMER + 1) * 4));
+  // the table and positions went up by cudaMemcpy on the legacy stream,
+  // which the handle's non-blocking stream does not wait for
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemsetAsync(h->d_err.p, 0, 16, h->st));
+  CK(cudaMemsetAsync(h->d_csr.p, 0, (NKMER + 1) * 4, h->st));
   launch_build_csr_counts(d_tab.p, n, np, h->d_csr.p, h->d_err.p, h->st);
+  // keys outside the 15-mers, buckets past the positions and repeated keys
+  // stop the load before the fill
+  {
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaGetLastError());
+    int err0 = 0;
+    CK(cudaMemcpy(&err0, h->d_err.p, 4, cudaMemcpyDeviceToHost));
+    if (err0) {
+      h->err = "sthash: invalid table entry (code " + std::to_string(err0) + ")";
+      return PBW_ERR_FORMAT;
+    }
+  }
   DevBuf<unsigned int> sums;
   TRY(dev_alloc(h, sums, scan_blocks(NKMER + 1) + 1));
   launch_scan_excl(h->d_csr.p, NKMER + 1, nullptr, sums.p, nullptr, nullptr, h->st);
@@ -362,6 +394,13 @@ int pbw_open(const char* genome_prefix, const char* hash_prefix, const pbw_optio
   if (rc == PBW_OK) rc = load_hash(h.get(), hash_prefix ? hash_prefix : genome_prefix);
   if (rc == PBW_OK) rc = build_tables(h.get());
   if (rc == PBW_OK) rc = pipeline_init(h.get());
+  // every upload above (legacy-stream copies from pageable memory may still
+  // be in flight when cudaMemcpy returns) is complete before the handle's
+  // stream runs a kernel on it
+  if (rc == PBW_OK && cudaDeviceSynchronize() != cudaSuccess) {
+    h->err = "cudaDeviceSynchronize failed after loading the index";
+    rc = PBW_ERR_CUDA;
+  }
   if (rc != PBW_OK) {
     g_open_err = h->err;
     return rc;
