@@ -31,11 +31,8 @@
 #include <dlfcn.h>
 
 #include "../../include/probebwa_gpu.h"
+#include "abi_guard.h"
 #include "pbw_pipeline.h"
-
-namespace pbw {
-void set_handleless_error(const std::string& s);
-}
 
 namespace {
 
@@ -546,9 +543,10 @@ bool parse_sam_header(const char* text, size_t len, std::string& sort_order, std
 
 }  // namespace
 
-extern "C" int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
-                             const uint64_t* sel, uint64_t n_sel, const char* path, int32_t write_index) {
-  if (!h || !opt || !path) return PBW_ERR_ARG;
+namespace {
+
+int bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
+              const uint64_t* sel, uint64_t n_sel, const char* path, int32_t write_index) {
   if (!zlib().ok) {
     h->err = "BAM output needs libz.so.1";
     return PBW_ERR_IO;
@@ -570,11 +568,7 @@ extern "C" int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t
   return rc;
 }
 
-extern "C" int pbw_bam_write_text(const char* sam, uint64_t len, const char* path, int32_t write_index) {
-  if (!sam || !path) {
-    pbw::set_handleless_error("pbw_bam_write_text: NULL text or path");
-    return PBW_ERR_ARG;
-  }
+int bam_write_text(const char* sam, uint64_t len, const char* path, int32_t write_index) {
   if (!zlib().ok) {
     pbw::set_handleless_error("BAM output needs libz.so.1");
     return PBW_ERR_IO;
@@ -593,4 +587,21 @@ extern "C" int pbw_bam_write_text(const char* sam, uint64_t len, const char* pat
   const int rc = bam_from_text(sam, (size_t)len, names, lens, path, write_index != 0, err);
   if (rc != PBW_OK) pbw::set_handleless_error(err);
   return rc;
+}
+
+}  // namespace
+
+extern "C" int pbw_bam_write(pbw_handle* h, const pbw_sam_options* opt, uint32_t n_src, const pbw_sam_source* src,
+                             const uint64_t* sel, uint64_t n_sel, const char* path, int32_t write_index) {
+  if (!h || !opt || !path) return PBW_ERR_ARG;
+  return pbw::guarded("pbw_bam_write", [h](const std::string& m) { h->err = m; },
+                      [&] { return bam_write(h, opt, n_src, src, sel, n_sel, path, write_index); });
+}
+
+extern "C" int pbw_bam_write_text(const char* sam, uint64_t len, const char* path, int32_t write_index) {
+  if (!sam || !path) {
+    pbw::set_handleless_error("pbw_bam_write_text: NULL text or path");
+    return PBW_ERR_ARG;
+  }
+  return pbw::guard_handleless("pbw_bam_write_text", [&] { return bam_write_text(sam, len, path, write_index); });
 }

@@ -31,10 +31,12 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "../../include/probebwa_gpu.h"
+#include "abi_guard.h"
 #include "fastx_text.h"
 #include "pbw_kernels.h"
 
@@ -92,15 +94,9 @@ void push_read(pbw_read_set* rs, const std::vector<uint8_t>& seq, const std::vec
 
 }  // namespace
 
-namespace pbw {
-void set_handleless_error(const std::string& s);
-}
+namespace {
 
-extern "C" {
-
-int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const char* adapter, pbw_read_set** out) {
-  if (!path || !out) return PBW_ERR_ARG;
-  *out = nullptr;
+int reads_load(const char* path, int fasta, uint8_t quality_offset, const char* adapter, pbw_read_set** out) {
   std::vector<char> buf;
   std::string err;
   const int lrc = pbw::text::load_text(path, buf, err);
@@ -108,7 +104,8 @@ int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const ch
     pbw::set_handleless_error(err);
     return lrc;
   }
-  pbw_read_set* rs = new pbw_read_set();
+  std::unique_ptr<pbw_read_set> owner(new pbw_read_set());
+  pbw_read_set* rs = owner.get();
   // sequence bytes are at most half of a FASTQ file, at most all of a FASTA one
   rs->bases.reserve(fasta ? buf.size() : buf.size() / 2 + 64);
   rs->quals.reserve(rs->bases.capacity());
@@ -169,8 +166,19 @@ int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const ch
       if (!have) break;
     }
   }
-  *out = rs;
+  *out = owner.release();
   return PBW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbw_reads_load(const char* path, int fasta, uint8_t quality_offset, const char* adapter, pbw_read_set** out) {
+  if (!path || !out) return PBW_ERR_ARG;
+  *out = nullptr;
+  return pbw::guard_handleless("pbw_reads_load",
+                               [&] { return reads_load(path, fasta, quality_offset, adapter, out); });
 }
 
 int pbw_reads_get(const pbw_read_set* rs, pbw_reads* view) {

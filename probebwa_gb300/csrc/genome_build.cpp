@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/probebwa_gpu.h"
+#include "abi_guard.h"
 #include "fastx_text.h"
 
 namespace pbw {
@@ -135,12 +136,10 @@ struct Writer {
 
 }  // namespace
 
-extern "C" int pbw_build_genome(const char* out_prefix, const char* species, const char* assembly, uint32_t n_files,
-                                const char* const* fasta_paths) {
-  if (!out_prefix || !species || !assembly || (n_files && !fasta_paths)) {
-    pbw::set_handleless_error("pbw_build_genome: null argument");
-    return PBW_ERR_ARG;
-  }
+namespace {
+
+int build_genome(const char* out_prefix, const char* species, const char* assembly, uint32_t n_files,
+                 const char* const* fasta_paths) {
   std::vector<Contig> contigs;
   for (uint32_t i = 0; i < n_files; i++) {
     const int rc = add_fasta(fasta_paths[i], contigs);
@@ -175,4 +174,16 @@ extern "C" int pbw_build_genome(const char* out_prefix, const char* species, con
     return PBW_ERR_IO;
   }
   return PBW_OK;
+}
+
+}  // namespace
+
+extern "C" int pbw_build_genome(const char* out_prefix, const char* species, const char* assembly, uint32_t n_files,
+                                const char* const* fasta_paths) {
+  if (!out_prefix || !species || !assembly || (n_files && !fasta_paths)) {
+    pbw::set_handleless_error("pbw_build_genome: null argument");
+    return PBW_ERR_ARG;
+  }
+  return pbw::guard_handleless("pbw_build_genome",
+                               [&] { return build_genome(out_prefix, species, assembly, n_files, fasta_paths); });
 }
