@@ -467,6 +467,20 @@ int bam_from_text(const char* text, size_t len, const std::vector<std::string>& 
     recs.push_back(ix);
     p = e + 1;
   }
+  // an index describes records in coordinate order: placed records by
+  // (reference, position), then the unplaced ones (bam.rs:38-43)
+  if (write_index) {
+    int64_t last = INT64_MIN;
+    for (size_t k = 0; k < recs.size(); k++) {
+      const RecIdx& r = recs[k];
+      const int64_t key = (r.ref < 0 || r.beg < 0) ? INT64_MAX : ((int64_t)r.ref << 32) | r.beg;
+      if (key < last) {
+        err = "BAM: record " + std::to_string(k) + " is out of coordinate order; an index needs sorted records";
+        return PBW_ERR_ARG;
+      }
+      last = key;
+    }
+  }
   // BGZF blocks on all host threads
   const size_t nb = (u.size() + BGZF_BLOCK - 1) / BGZF_BLOCK;
   std::vector<std::vector<unsigned char>> blocks(nb + 1);

@@ -79,9 +79,18 @@ def test_sorted_stream_and_index(P, mapped):
 def test_refusals(P, mapped, oracle):
     d, om, src, _ = mapped
     sam = om.sam_text(str(d / "u.sam"), src)
-    # an index needs a coordinate-sorted stream
-    with pytest.raises(P.PbwError):
+    # an index needs a coordinate-sorted stream, and records in that order
+    with pytest.raises(P.PbwError, match="coordinate"):
         P.bam_from_sam(sam, str(d / "u.bam"), index=True)
+    lines = sam.rstrip(b"\n").split(b"\n")
+    hdr = [x.replace(b"SO:unsorted", b"SO:coordinate") for x in lines if x.startswith(b"@")]
+    placed = [x for x in lines if not x.startswith(b"@") and x.split(b"\t")[2] != b"*"]
+    assert len(placed) > 2
+    order = sorted(range(len(placed)), key=lambda i: (placed[i].split(b"\t")[2], int(placed[i].split(b"\t")[3])))
+    swapped = [placed[i] for i in order]
+    swapped[0], swapped[-1] = swapped[-1], swapped[0]
+    with pytest.raises(P.PbwError, match="out of coordinate order"):
+        P.bam_from_sam(b"\n".join(hdr + swapped) + b"\n", str(d / "o.bam"), index=True)
     # raw scores below '!' are not QUAL characters
     R = src[0][0]
     seqs = [R.bases[R.offsets[i]:R.offsets[i + 1]].tobytes() for i in range(5)]
