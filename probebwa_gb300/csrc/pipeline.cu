@@ -1103,8 +1103,12 @@ int pbw_map_paired(pbw_handle* h, pbw_insert_model* model, const pbw_reads* r1, 
     }
     CK(cudaEventRecord(h->up_ev[k], su));
   }
-  TRY(map_paired_dev(h, model, h->d_bases.p, h->d_quals.p, h->d_offs.p, h->d_bases2.p, h->d_quals2.p,
-                     h->d_offs2.p, n, t1, t2, std::max(l1, l2), o1, o2, &h->up_ev));
+  const int rc = map_paired_dev(h, model, h->d_bases.p, h->d_quals.p, h->d_offs.p, h->d_bases2.p, h->d_quals2.p,
+                                h->d_offs2.p, n, t1, t2, std::max(l1, l2), o1, o2, &h->up_ev);
+  // no copy of the caller's reads is in flight when the call returns (after
+  // a success they have all landed already: every super-chunk waited for them)
+  cudaStreamSynchronize(su);
+  if (rc != PBW_OK) return rc;
   // copy time the mapping could not hide (until the first super-chunk was
   // up), and the whole call from the first copy to the last record read back
   h->stats.ms_h2d = ms_between(a, h->up_ev[0]);
