@@ -283,7 +283,8 @@ int pbw_sort_coordinate(pbw_handle* h, uint32_t n_src, const pbw_sam_source* src
  * adapter is not NULL, strip_adapter (:97-117). quality_offset is 33 or 64
  * (--phred64). pbw_reads_get gives the reads as pbw_reads (the quality track
  * has the sequence's length: missing scores are 30); pbw_reads_id the i-th
- * read ID (NUL-terminated, valid until pbw_reads_free). A path ending in
+ * read ID (NUL-terminated, valid until pbw_reads_free). The IDs are stored
+ * back to back: ID i + 1 starts right after the NUL that ends ID i. A path ending in
  * ".gz" is gunzipped first (open_maybe_gz, :120-129; zlib is opened at run
  * time as libz.so.1). Errors: PBW_ERR_IO (cannot open, corrupt gzip) and
  * PBW_ERR_FORMAT (text that is not UTF-8); pbw_last_error(NULL) names the

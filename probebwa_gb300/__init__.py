@@ -281,6 +281,21 @@ def cigar_strings(r: dict) -> list:
             for i in range(len(r["contig"]))]
 
 
+def _read_ids(L, h, n: int) -> list:
+    """The n read IDs of a read set: one read of the block they are stored
+    in back to back (NUL after each), or one call per ID when an ID holds a
+    NUL of its own."""
+    if n == 0:
+        return []
+    raw = C.cast(L.pbw_reads_id, C.CFUNCTYPE(C.c_void_p, C.c_void_p, C.c_uint64))
+    a0, an = raw(h, 0), raw(h, n - 1)
+    block = C.string_at(a0, an - a0 + len(C.string_at(an)))
+    ids = block.decode("utf-8", "replace").split("\0")
+    if len(ids) != n:
+        ids = [L.pbw_reads_id(h, i).decode("utf-8", "replace") for i in range(n)]
+    return ids
+
+
 def load_reads(path: str, fasta: bool = False, quality_offset: int = 33, adapter: str | bytes | None = None) -> "Reads":
     """read_reads_files_with_preprocessing for one file (src/io/fastx.rs:19-48)
     through pbw_reads_load: bases, Phred scores and IDs as a Reads object."""
@@ -303,7 +318,7 @@ def load_reads(path: str, fasta: bool = False, quality_offset: int = 33, adapter
         else:
             bases = np.zeros(0, np.uint8)
             quals = np.zeros(0, np.uint8)
-        ids = [L.pbw_reads_id(h, i).decode("utf-8", "replace") for i in range(n)]
+        ids = _read_ids(L, h, n)
     finally:
         L.pbw_reads_free(h)
     return Reads(bases, quals, offs, ids)
