@@ -67,6 +67,14 @@ inline Span first_token(Span s) {
 inline bool valid_utf8(const char* s, size_t n) {
   size_t i = 0;
   while (i < n) {
+    // runs of ASCII 8 bytes at a time (whole characters: i stays on a boundary)
+    while (i + 8 <= n) {
+      uint64_t w;
+      memcpy(&w, s + i, 8);
+      if (w & 0x8080808080808080ull) break;
+      i += 8;
+    }
+    if (i >= n) break;
     const uint8_t c = (uint8_t)s[i];
     if (c < 0x80) { i++; continue; }
     size_t need;

@@ -138,3 +138,37 @@ def test_loader_reads_gzip_members(oracle, tmp_path):
     corrupt.write_bytes(gzip.compress(text.encode())[:-20])
     with pytest.raises(P.PbwError):
         P.load_reads(str(corrupt))
+
+
+# multi-byte forms that std::str::from_utf8 accepts or rejects, for the word
+# boundaries of the validator's ASCII fast path
+UTF8_FORMS = [
+    (b"\xc3\xa9", True),          # U+00E9
+    (b"\xe2\x80\x83", True),      # U+2003
+    (b"\xf0\x9f\x98\x80", True),  # U+1F600
+    (b"\x80", False),             # lone continuation byte
+    (b"\xc0\xaf", False),         # overlong
+    (b"\xed\xa0\x80", False),     # surrogate
+    (b"\xe2\x80", False),         # truncated
+    (b"\xf4\x90\x80\x80", False),  # above U+10FFFF
+]
+
+
+@pytest.mark.parametrize("form,ok", UTF8_FORMS)
+def test_utf8_check_at_every_word_offset(oracle, tmp_path, form, ok):
+    """The validator skips ASCII 8 bytes at a time: a multi-byte form at each
+    offset of the first words (in the ID, after a padding of k bytes) is
+    accepted or refused exactly as the oracle's (from_utf8) check does."""
+    import probebwa_gb300 as P
+    P.build()
+    for k in range(17):
+        body = b"@" + b"x" * k + form + b"\nACGT\n+\nIIII\n@r2\nGG\n+\nII\n"
+        p = tmp_path / f"u{k}.fq"
+        p.write_bytes(body)
+        if ok:
+            _same(P.load_reads(str(p)), oracle.parse_reads(str(p)))
+        else:
+            with pytest.raises(RuntimeError):
+                oracle.parse_reads(str(p))
+            with pytest.raises(P.PbwError):
+                P.load_reads(str(p))
