@@ -1,10 +1,12 @@
 // fastx.cpp -- the input side of the mapping path: FASTQ / FASTA reads into
 // the structure-of-arrays layout the map calls take (src/io/fastx.rs).
 //
-// The file is read into memory once (gunzipped when its name ends in ".gz",
-// as open_maybe_gz, fastx.rs:120-129, with every gzip member decoded in turn
-// like flate2's MultiGzDecoder) and split into lines with memchr; each record
-// is decoded straight into the concatenated base, quality and offset arrays.
+// A regular file is mapped read-only (other inputs are read into memory; a
+// name ending in ".gz" is gunzipped, as open_maybe_gz, fastx.rs:120-129, with
+// every gzip member decoded in turn like flate2's MultiGzDecoder), checked
+// to be UTF-8 eight ASCII bytes at a time, and split into lines with memchr;
+// each record is decoded straight into the concatenated base, quality and
+// offset arrays.
 // Semantics follow the reference's parsers:
 //  * the text must be UTF-8 (each line goes through BufRead::read_line into
 //    a String); anything else is an error, as there;
@@ -97,7 +99,7 @@ void push_read(pbw_read_set* rs, const std::vector<uint8_t>& seq, const std::vec
 namespace {
 
 int reads_load(const char* path, int fasta, uint8_t quality_offset, const char* adapter, pbw_read_set** out) {
-  std::vector<char> buf;
+  pbw::text::Text buf;
   std::string err;
   const int lrc = pbw::text::load_text(path, buf, err);
   if (lrc != PBW_OK) {

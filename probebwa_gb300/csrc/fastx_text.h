@@ -11,6 +11,10 @@
 #include <vector>
 
 #include <dlfcn.h>
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "../../include/probebwa_gpu.h"
 
@@ -228,23 +232,78 @@ inline bool ends_with_gz(const char* path) {
   return strlen(base) > 3;
 }
 
+// The text of a file: a regular file is mapped read-only (no copy of its
+// bytes); anything else (a pipe, an empty file, a map that fails) and gzip
+// input is read or decoded into owned memory.
+class Text {
+ public:
+  Text() = default;
+  Text(const Text&) = delete;
+  Text& operator=(const Text&) = delete;
+  ~Text() { unmap(); }
+  const char* data() const { return p_; }
+  size_t size() const { return n_; }
+  bool map(const char* path) {
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) return false;
+    struct stat st;
+    void* m = MAP_FAILED;
+    if (fstat(fd, &st) == 0 && S_ISREG(st.st_mode) && st.st_size > 0)
+      m = mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_PRIVATE | MAP_POPULATE, fd, 0);
+    close(fd);
+    if (m == MAP_FAILED) return false;
+    map_ = m;
+    map_len_ = (size_t)st.st_size;
+    p_ = (const char*)m;
+    n_ = map_len_;
+    return true;
+  }
+  std::vector<char>& own() {
+    unmap();
+    p_ = own_.data();
+    n_ = own_.size();
+    return own_;
+  }
+  void adopt() {  // after filling own()
+    p_ = own_.data();
+    n_ = own_.size();
+  }
+
+ private:
+  void unmap() {
+    if (map_) munmap(map_, map_len_);
+    map_ = nullptr;
+  }
+  const char* p_ = nullptr;
+  size_t n_ = 0;
+  std::vector<char> own_;
+  void* map_ = nullptr;
+  size_t map_len_ = 0;
+};
+
 // The whole text of path, gunzipped when the name ends in ".gz", checked to
 // be UTF-8. PBW_OK, or PBW_ERR_IO / PBW_ERR_FORMAT with a message in err.
-inline int load_text(const char* path, std::vector<char>& buf, std::string& err) {
-  if (!read_file(path, buf)) {
-    err = std::string("cannot open ") + path;
-    return PBW_ERR_IO;
-  }
+inline int load_text(const char* path, Text& text, std::string& err) {
   if (ends_with_gz(path)) {
     std::vector<char> raw;
-    raw.swap(buf);
+    if (!read_file(path, raw)) {
+      err = std::string("cannot open ") + path;
+      return PBW_ERR_IO;
+    }
     std::string e;
-    if (!gunzip(raw, buf, e)) {
+    if (!gunzip(raw, text.own(), e)) {
       err = std::string(path) + ": " + e;
       return PBW_ERR_IO;
     }
+    text.adopt();
+  } else if (!text.map(path)) {
+    if (!read_file(path, text.own())) {
+      err = std::string("cannot open ") + path;
+      return PBW_ERR_IO;
+    }
+    text.adopt();
   }
-  if (!valid_utf8(buf.data(), buf.size())) {
+  if (!valid_utf8(text.data(), text.size())) {
     err = std::string(path) + ": stream did not contain valid UTF-8";
     return PBW_ERR_FORMAT;
   }

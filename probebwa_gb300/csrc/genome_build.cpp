@@ -70,7 +70,7 @@ void pack_contig(Contig& c, const std::vector<uint8_t>& seq) {
 }
 
 int add_fasta(const char* path, std::vector<Contig>& out) {
-  std::vector<char> buf;
+  Text buf;
   std::string err;
   const int rc = load_text(path, buf, err);
   if (rc != PBW_OK) {

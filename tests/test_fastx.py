@@ -172,3 +172,27 @@ def test_utf8_check_at_every_word_offset(oracle, tmp_path, form, ok):
                 oracle.parse_reads(str(p))
             with pytest.raises(P.PbwError):
                 P.load_reads(str(p))
+
+
+def test_loader_reads_from_a_pipe(oracle, tmp_path):
+    """A regular file is mapped; a pipe (no size, no mapping) is read as a
+    stream: the same reads either way."""
+    import os
+    import threading
+    import probebwa_gb300 as P
+    P.build()
+    text = FILES["multiline.fq"][1] + FILES["plain.fq"][1]
+    plain = tmp_path / "p.fq"
+    plain.write_text(text)
+    fifo = tmp_path / "pipe.fq"
+    os.mkfifo(fifo)
+
+    def writer():
+        with open(fifo, "w") as f:
+            f.write(text)
+    t = threading.Thread(target=writer)
+    t.start()
+    got = P.load_reads(str(fifo))
+    t.join(timeout=30)
+    _same(got, oracle.parse_reads(str(plain)))
+    _same(P.load_reads(str(plain)), oracle.parse_reads(str(plain)))
