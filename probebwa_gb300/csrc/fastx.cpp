@@ -76,21 +76,34 @@ size_t adapter_keep(const uint8_t* seq, size_t rl, const std::string& ad) {
   return rl;
 }
 
-// Appends one read: bases upper-cased, the quality track cut or padded to the
-// (possibly adapter-trimmed) sequence length.
-void push_read(pbw_read_set* rs, const std::vector<uint8_t>& seq, const std::vector<uint8_t>& qual,
-               const std::string* adapter) {
-  const size_t n = seq.size();
-  const size_t keep = adapter ? adapter_keep(seq.data(), n, *adapter) : n;
-  const size_t b0 = rs->bases.size();
+// Sequence text appended to the read set's bases, upper-cased.
+void append_bases(pbw_read_set* rs, Span t) {
+  const size_t o = rs->bases.size();
+  rs->bases.resize(o + t.n);
+  uint8_t* d = rs->bases.data() + o;
+  for (size_t k = 0; k < t.n; k++) d[k] = upper((uint8_t)t.p[k]);
+}
+
+// Quality text appended to the read set's quals: the byte minus the offset,
+// saturating at 0.
+void append_quals(pbw_read_set* rs, Span t, uint8_t offset) {
+  const size_t o = rs->quals.size();
+  rs->quals.resize(o + t.n);
+  uint8_t* d = rs->quals.data() + o;
+  for (size_t k = 0; k < t.n; k++) {
+    const uint8_t c = (uint8_t)t.p[k];
+    d[k] = c > offset ? (uint8_t)(c - offset) : (uint8_t)0;
+  }
+}
+
+// Ends the read whose bases start at b0 (its qualities, as many as were
+// given, start at b0 too): the adapter's 3' overlap is cut, and the quality
+// track is cut or padded with 30 to the kept length.
+void end_read(pbw_read_set* rs, size_t b0, const std::string* adapter) {
+  const size_t n = rs->bases.size() - b0;
+  const size_t keep = adapter ? adapter_keep(rs->bases.data() + b0, n, *adapter) : n;
   rs->bases.resize(b0 + keep);
-  rs->quals.resize(b0 + keep);
-  uint8_t* ob = rs->bases.data() + b0;
-  uint8_t* oq = rs->quals.data() + b0;
-  for (size_t t = 0; t < keep; t++) ob[t] = upper(seq[t]);
-  const size_t m = std::min(keep, qual.size());
-  if (m) memcpy(oq, qual.data(), m);
-  if (keep > m) memset(oq + m, 30, keep - m);
+  rs->quals.resize(b0 + keep, 30);
   rs->offsets.push_back(b0 + keep);
 }
 
@@ -116,29 +129,21 @@ int reads_load(const char* path, int fasta, uint8_t quality_offset, const char* 
   Builder bld{rs};
   Lines L{buf.data(), buf.data() + buf.size()};
   Span line;
-  std::vector<uint8_t> seq, qual;
   if (!fasta) {
     while (L.next(line)) {
       bld.add(first_token(strip_leading(line, '@')));
-      seq.clear();
-      qual.clear();
+      const size_t b0 = rs->bases.size();  // == rs->quals.size(): every read ends both at its length
       while (L.next(line)) {
         const Span t = trim(line);
         if (t.n && t.p[0] == '+') break;
-        seq.insert(seq.end(), (const uint8_t*)t.p, (const uint8_t*)t.p + t.n);
+        append_bases(rs, t);
       }
+      const size_t n = rs->bases.size() - b0;
       while (L.next(line)) {
-        const Span t = trim(line);
-        const size_t q0 = qual.size();
-        qual.resize(q0 + t.n);
-        uint8_t* o = qual.data() + q0;
-        for (size_t k = 0; k < t.n; k++) {
-          const uint8_t c = (uint8_t)t.p[k];
-          o[k] = c > quality_offset ? (uint8_t)(c - quality_offset) : (uint8_t)0;
-        }
-        if (qual.size() >= seq.size()) break;
+        append_quals(rs, trim(line), quality_offset);
+        if (rs->quals.size() - b0 >= n) break;
       }
-      push_read(rs, seq, qual, ad);
+      end_read(rs, b0, ad);
     }
   } else {
     bool have = false;
@@ -153,7 +158,7 @@ int reads_load(const char* path, int fasta, uint8_t quality_offset, const char* 
       }
       have = false;
       bld.add(first_token(strip_leading(header, '>')));
-      seq.clear();
+      const size_t b0 = rs->bases.size();
       while (L.next(line)) {
         const Span t = trim(line);
         if (t.n && t.p[0] == '>') {
@@ -161,10 +166,10 @@ int reads_load(const char* path, int fasta, uint8_t quality_offset, const char* 
           have = true;
           break;
         }
-        seq.insert(seq.end(), (const uint8_t*)t.p, (const uint8_t*)t.p + t.n);
+        append_bases(rs, t);
       }
-      qual.assign(seq.size(), 40);
-      push_read(rs, seq, qual, ad);
+      rs->quals.resize(rs->bases.size(), 40);  // FASTA reads: every quality 40
+      end_read(rs, b0, ad);
       if (!have) break;
     }
   }
