@@ -19,12 +19,14 @@
 // (tests/cli.rs:46-80, 148-195): BGZF with the BAM magic, records in
 // coordinate order with --index, a BAI with its magic.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
+#include <string_view>
 #include <thread>
 #include <vector>
 
@@ -173,10 +175,30 @@ bool parse_i64(const Field& f, int64_t& v) {
 
 const char* SEQ_CODES = "=ACMGRSVTWYHKDBN";
 
-// One SAM record line as a BAM record (block_size first) appended to out.
-bool encode_record(const char* line, size_t len, const std::map<std::string, int32_t>& refs,
-                   std::vector<unsigned char>& out, RecIdx& ix, std::string& err) {
-  std::vector<Field> f;
+// 4-bit SEQ code of a byte (lower case as upper case), 0xFF for a byte that
+// is not one of the 16 IUPAC symbols.
+const unsigned char* seq_code_table() {
+  static const auto table = [] {
+    std::array<unsigned char, 256> t;
+    t.fill(0xFF);
+    for (int k = 0; k < 16; k++) {
+      t[(unsigned char)SEQ_CODES[k]] = (unsigned char)k;
+      if (SEQ_CODES[k] >= 'A' && SEQ_CODES[k] <= 'Z') t[(unsigned char)(SEQ_CODES[k] + 32)] = (unsigned char)k;
+    }
+    return t;
+  }();
+  return table.data();
+}
+
+using RefMap = std::map<std::string, int32_t, std::less<>>;
+
+// One SAM record line as a BAM record (block_size first) appended to out;
+// on an error out is left as it was.
+bool encode_record(const char* line, size_t len, const RefMap& refs, std::vector<unsigned char>& out, RecIdx& ix,
+                   std::string& err) {
+  thread_local std::vector<Field> f;
+  thread_local std::vector<uint32_t> cig;
+  f.clear();
   size_t a = 0;
   for (size_t i = 0; i <= len; i++)
     if (i == len || line[i] == '\t') {
@@ -190,7 +212,7 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
   auto ref_of = [&](const Field& x, int32_t same) -> int32_t {
     if (x.is("*")) return -1;
     if (x.is("=")) return same;
-    auto it = refs.find(std::string(x.p, x.n));
+    auto it = refs.find(std::string_view(x.p, x.n));
     return it == refs.end() ? -2 : it->second;
   };
   int64_t flag, pos, mapq, pnext, tlen;
@@ -212,7 +234,7 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
     return false;
   }
   // CIGAR
-  std::vector<uint32_t> cig;
+  cig.clear();
   int64_t span = 0;
   if (!f[5].is("*")) {
     int64_t v = 0;
@@ -249,83 +271,28 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
       return false;
     }
   }
-  // SEQ and QUAL
   const Field& sq = f[9];
   const Field& ql = f[10];
   const size_t l_seq = (sq.is("*") || sq.n == 0) ? 0 : sq.n;
-  std::vector<unsigned char> seq((l_seq + 1) / 2, 0);
-  for (size_t i = 0; i < l_seq; i++) {
-    char c = sq.p[i];
-    if (c >= 'a' && c <= 'z') c -= 32;
-    const char* q = strchr(SEQ_CODES, c);
-    if (!q || c == 0) {
-      err = "invalid sequence base";
-      return false;
-    }
-    seq[i / 2] |= (unsigned char)((q - SEQ_CODES) << ((i & 1) ? 0 : 4));
-  }
-  std::vector<unsigned char> qual(l_seq, 0xFF);
-  if (!(ql.is("*") || ql.n == 0)) {
-    if (ql.n != l_seq) {
-      err = "quality scores and sequence differ in length";
-      return false;
-    }
-    for (size_t i = 0; i < l_seq; i++) {
-      const unsigned char c = (unsigned char)ql.p[i];
-      if (c < '!' || c > '~') {
-        err = "invalid quality score";
-        return false;
-      }
-      qual[i] = (unsigned char)(c - 33);
-    }
-  }
-  // optional fields: TAG:TYPE:VALUE, Z and i only (what this mapper writes)
-  std::vector<unsigned char> aux;
-  for (size_t k = 11; k < f.size(); k++) {
-    const Field& t = f[k];
-    if (t.n < 5 || t.p[2] != ':' || t.p[4] != ':') {
-      err = "invalid optional field";
-      return false;
-    }
-    aux.push_back((unsigned char)t.p[0]);
-    aux.push_back((unsigned char)t.p[1]);
-    if (t.p[3] == 'Z') {
-      aux.push_back('Z');
-      aux.insert(aux.end(), t.p + 5, t.p + t.n);
-      aux.push_back(0);
-    } else if (t.p[3] == 'i') {
-      int64_t v;
-      if (!parse_i64(Field{t.p + 5, t.n - 5}, v) || v < INT32_MIN || v > INT32_MAX) {
-        err = "invalid optional field";
-        return false;
-      }
-      aux.push_back('i');
-      put32(aux, (uint32_t)(int32_t)v);
-    } else {
-      err = "unsupported optional field type";
-      return false;
-    }
-  }
   const int32_t p0 = (int32_t)(pos - 1);
   const bool unmapped = (flag & 4) != 0;
   const int64_t beg = p0 < 0 ? -1 : p0;
   const int64_t end = beg < 0 ? 0 : beg + (span > 0 && !unmapped ? span : 1);
-  if (end > POS_MAX + 1) {
-    err = "alignment ends beyond 2^31";
-    return false;
-  }
-  ix.ref = ref;
-  ix.beg = beg;
-  ix.end = end;
-  ix.bin = reg2bin(beg, end);
-  ix.unmapped = unmapped;
+  const int bin = reg2bin(beg, end);
+  // fixed fields, name and CIGAR, then SEQ, QUAL and the optional fields as
+  // they are checked
   const size_t start = out.size();
+  auto fail = [&](const char* what) {
+    out.resize(start);
+    err = what;
+    return false;
+  };
   put32(out, 0);  // block_size, patched below
   put32(out, (uint32_t)ref);
   put32(out, (uint32_t)p0);
   out.push_back((unsigned char)(f[0].n + 1));
   out.push_back((unsigned char)mapq);
-  put16(out, (uint32_t)ix.bin);
+  put16(out, (uint32_t)bin);
   put16(out, (uint32_t)cig.size());
   put16(out, (uint32_t)flag);
   put32(out, (uint32_t)l_seq);
@@ -335,9 +302,53 @@ bool encode_record(const char* line, size_t len, const std::map<std::string, int
   out.insert(out.end(), f[0].p, f[0].p + f[0].n);
   out.push_back(0);
   for (uint32_t c : cig) put32(out, c);
-  out.insert(out.end(), seq.begin(), seq.end());
-  out.insert(out.end(), qual.begin(), qual.end());
-  out.insert(out.end(), aux.begin(), aux.end());
+  // SEQ: two 4-bit codes a byte, the first in the high nibble
+  const unsigned char* code = seq_code_table();
+  const size_t s0 = out.size();
+  out.resize(s0 + (l_seq + 1) / 2, 0);
+  for (size_t i = 0; i < l_seq; i++) {
+    const unsigned char k = code[(unsigned char)sq.p[i]];
+    if (k == 0xFF) return fail("invalid sequence base");
+    out[s0 + i / 2] |= (unsigned char)(k << ((i & 1) ? 0 : 4));
+  }
+  // QUAL: Phred+33 characters, or 0xFF for each base when absent
+  const size_t q0 = out.size();
+  out.resize(q0 + l_seq, 0xFF);
+  if (!(ql.is("*") || ql.n == 0)) {
+    if (ql.n != l_seq) return fail("quality scores and sequence differ in length");
+    for (size_t i = 0; i < l_seq; i++) {
+      const unsigned char c = (unsigned char)ql.p[i];
+      if (c < '!' || c > '~') return fail("invalid quality score");
+      out[q0 + i] = (unsigned char)(c - 33);
+    }
+  }
+  // optional fields: TAG:TYPE:VALUE, Z and i only (what this mapper writes)
+  for (size_t k = 11; k < f.size(); k++) {
+    const Field& t = f[k];
+    if (t.n < 5 || t.p[2] != ':' || t.p[4] != ':') return fail("invalid optional field");
+    if (t.p[3] == 'Z') {
+      out.push_back((unsigned char)t.p[0]);
+      out.push_back((unsigned char)t.p[1]);
+      out.push_back('Z');
+      out.insert(out.end(), t.p + 5, t.p + t.n);
+      out.push_back(0);
+    } else if (t.p[3] == 'i') {
+      int64_t v;
+      if (!parse_i64(Field{t.p + 5, t.n - 5}, v) || v < INT32_MIN || v > INT32_MAX) return fail("invalid optional field");
+      out.push_back((unsigned char)t.p[0]);
+      out.push_back((unsigned char)t.p[1]);
+      out.push_back('i');
+      put32(out, (uint32_t)(int32_t)v);
+    } else {
+      return fail("unsupported optional field type");
+    }
+  }
+  if (end > POS_MAX + 1) return fail("alignment ends beyond 2^31");
+  ix.ref = ref;
+  ix.beg = beg;
+  ix.end = end;
+  ix.bin = bin;
+  ix.unmapped = unmapped;
   const uint32_t bs = (uint32_t)(out.size() - start - 4);
   for (int i = 0; i < 4; i++) out[start + i] = (unsigned char)(bs >> (8 * i));
   return true;
@@ -440,9 +451,11 @@ int bam_from_text(const char* text, size_t len, const std::vector<std::string>& 
     const char* nl = (const char*)memchr(text + hdr_end, '\n', len - hdr_end);
     hdr_end = nl ? (size_t)(nl - text) + 1 : len;
   }
-  std::map<std::string, int32_t> refs;
+  RefMap refs;
   for (size_t c = 0; c < names.size(); c++) refs.emplace(names[c], (int32_t)c);
-  std::vector<unsigned char> u = {'B', 'A', 'M', 1};
+  std::vector<unsigned char> u;
+  u.reserve(len + 4096);  // a BAM stream is about the size of its SAM text or smaller
+  u.insert(u.end(), {'B', 'A', 'M', 1});
   put32(u, (uint32_t)hdr_end);
   u.insert(u.end(), text, text + hdr_end);
   put32(u, (uint32_t)names.size());
@@ -452,20 +465,67 @@ int bam_from_text(const char* text, size_t len, const std::vector<std::string>& 
     u.push_back(0);
     put32(u, (uint32_t)lens[c]);
   }
+  // records: contiguous slices of whole lines encoded on the host threads,
+  // then joined in order (the stream offsets of each slice's records shift
+  // by the bytes before it)
+  struct Slice {
+    size_t b = 0, e = 0;
+    std::vector<unsigned char> bytes;
+    std::vector<RecIdx> recs;
+    bool ok = true;
+    std::string err;
+  };
+  const size_t body = len - hdr_end;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t ns = body < (4u << 20) ? 1 : std::min<size_t>(hw, 16);
+  std::vector<Slice> sl(ns);
+  for (size_t k = 0; k < ns; k++) {
+    size_t b = k == 0 ? hdr_end : sl[k - 1].e;
+    size_t e = k + 1 == ns ? len : std::max(b, hdr_end + body / ns * (k + 1));
+    if (e < len) {  // to the start of the next line
+      const char* nl = (const char*)memchr(text + e, '\n', len - e);
+      e = nl ? (size_t)(nl - text) + 1 : len;
+    }
+    sl[k].b = b;
+    sl[k].e = e;
+  }
+  auto encode_slice = [&](Slice& x) {
+    x.bytes.reserve(x.e - x.b + 4096);
+    for (size_t p = x.b; p < x.e;) {
+      const char* nl = (const char*)memchr(text + p, '\n', x.e - p);
+      const size_t e = nl ? (size_t)(nl - text) : x.e;
+      RecIdx ix;
+      ix.u0 = x.bytes.size();
+      if (!encode_record(text + p, e - p, refs, x.bytes, ix, x.err)) {
+        x.ok = false;
+        return;
+      }
+      ix.u1 = x.bytes.size();
+      x.recs.push_back(ix);
+      p = e + 1;
+    }
+  };
+  if (ns == 1) {
+    encode_slice(sl[0]);
+  } else {
+    std::vector<std::thread> th;
+    for (size_t k = 0; k < ns; k++) th.emplace_back([&, k] { encode_slice(sl[k]); });
+    for (auto& t : th) t.join();
+  }
   std::vector<RecIdx> recs;
-  for (size_t p = hdr_end; p < len;) {
-    const char* nl = (const char*)memchr(text + p, '\n', len - p);
-    const size_t e = nl ? (size_t)(nl - text) : len;
-    RecIdx ix;
-    ix.u0 = u.size();
-    std::string rerr;
-    if (!encode_record(text + p, e - p, refs, u, ix, rerr)) {
-      err = "BAM: record " + std::to_string(recs.size()) + ": " + rerr;
+  for (Slice& x : sl) {
+    if (!x.ok) {  // the first record that failed, numbered over the whole stream
+      err = "BAM: record " + std::to_string(recs.size() + x.recs.size()) + ": " + x.err;
       return PBW_ERR_FORMAT;
     }
-    ix.u1 = u.size();
-    recs.push_back(ix);
-    p = e + 1;
+    const uint64_t base = u.size();
+    u.insert(u.end(), x.bytes.begin(), x.bytes.end());
+    for (RecIdx ix : x.recs) {
+      ix.u0 += base;
+      ix.u1 += base;
+      recs.push_back(ix);
+    }
+    std::vector<unsigned char>().swap(x.bytes);
   }
   // an index describes records in coordinate order: placed records by
   // (reference, position), then the unplaced ones (bam.rs:38-43)

@@ -153,3 +153,41 @@ def test_well_formed_record_round_trip(P, tmp_path):
     assert (r["nref"], r["npos"], r["tlen"], r["seq"]) == (0, 99, -5, "ACGT")
     assert r["qual"] == bytes([0, 40, 93, 20])
     assert r["aux"] == b"RGZg1\0" + b"NMi" + (-3).to_bytes(4, "little", signed=True)
+
+
+def _big_sam(n, bad=None):
+    """n records of 150 bases (about 9 MB for 25,000), the record numbered
+    bad with an invalid base."""
+    rng = np.random.default_rng(7)
+    hdr = b"@HD\tVN:1.6\tSO:coordinate\n" + b"".join(b"@SQ\tSN:c%d\tLN:5000000\n" % i for i in range(3))
+    seq = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, (n, 150))]
+    qual = (rng.integers(0, 41, (n, 150)) + 33).astype(np.uint8)
+    lines = []
+    for i in range(n):
+        s = seq[i].tobytes() if i != bad else b"AC!" + seq[i].tobytes()[3:]
+        c = i * 3 // n
+        lines.append(b"r%d\t99\tc%d\t%d\t60\t150M\tc%d\t%d\t300\t" % (i, c, 1 + i * 100, c, 151 + i * 100)
+                     + s + b"\t" + qual[i].tobytes() + b"\n")
+    return hdr + b"".join(lines)
+
+
+def test_large_stream_encoded_in_slices(P, tmp_path):
+    """Streams over 4 MB are encoded in slices on several threads: the
+    records, their order, the BAI and the number of a failing record are
+    those of the whole stream."""
+    sam = _big_sam(25_000)
+    path = str(tmp_path / "big.bam")
+    P.bam_from_sam(sam, path, index=True)
+    data = open(path, "rb").read()
+    recs = same_as_sam(sam, data)
+    assert [r["name"] for r in recs] == [f"r{i}" for i in range(25_000)]
+    index, no_coor = decode_bai(open(path + ".bai", "rb").read())
+    v = voffsets(data)
+    for r in recs[::97]:
+        bins, lin = index[r["ref"]]
+        vo = v(r["start"])
+        assert any(b <= vo < e for b, e in bins[r["bin"]])
+        assert lin[r["pos"] >> 14] <= vo
+    for bad in (3, 17_321, 24_999):
+        with pytest.raises(P.PbwError, match=f"record {bad}: invalid sequence base"):
+            P.bam_from_sam(_big_sam(25_000, bad=bad), str(tmp_path / "bad.bam"))
