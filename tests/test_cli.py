@@ -119,6 +119,26 @@ BAD_ARGS = [
 ]
 
 
+def test_cli_build_genome_like_oracle(clis, tmp_path):
+    """`probebwa build-genome -s -a -G out files...` (main.rs:33-41) writes
+    the .stidx the oracle's command line writes, byte for byte; a missing
+    input file fails on both."""
+    g = K.Xorshift64(55).gen_seq(3000)
+    f1 = tmp_path / "a.fa"
+    f1.write_text(f">c1 first\n{g[:1000]}\n{g[1000:1500].lower()}\n>c2\n{g[1500:2000]}NNNN{g[2000:2200]}\n")
+    f2 = tmp_path / "b.fa"
+    f2.write_text(f">c3\n{g[2200:]}\n")
+    outs = []
+    for exe, name in ((clis[0], "mine"), (clis[1], "ref")):
+        r = _run(exe, ["build-genome", "-s", "homo", "-a", "t2", "-G", str(tmp_path / name), str(f1), str(f2)])
+        assert r.returncode == 0, r.stderr
+        outs.append((tmp_path / f"{name}.stidx").read_bytes())
+    assert outs[0] == outs[1]
+    for exe in clis:
+        bad = _run(exe, ["build-genome", "-s", "x", "-a", "y", "-G", str(tmp_path / "z"), str(tmp_path / "absent.fa")])
+        assert bad.returncode != 0
+
+
 @pytest.mark.parametrize("args,code", BAD_ARGS)
 def test_cli_rejects_bad_arguments_like_oracle(clis, args, code):
     mine = _run(clis[0], args)
