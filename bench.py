@@ -1,24 +1,40 @@
 #!/usr/bin/env python3
 """Throughput of the probebwa mapping path on GB300.
 
-Workload (default): the paired-end configuration -- a synthetic 100 Mbp genome
-(25 x 4 Mbp, GC 41%, 5% segmental duplications of 1-10 kbp in 2-8 copies at
-95-99.5% identity, homopolymer runs of 6-15 bp at 1 per 2 kbp) and 1,000,000
-read pairs of 2 x 150 bp (insert N(350, 50), FR, 0.5% substitutions and
-0.05% indels enriched 5x in homopolymers, Phred N(35, 4) clipped to [2, 41]),
-mapped with the reference's default options. --config 0 selects the
-single-end configuration (1 Mbp genome with 20 planted 2 kbp repeat copies,
-10,000 x 120 bp reads). Data are generated from fixed seeds; no dataset is
-downloaded.
+Default workload (--config 2, the batching and ranker configurations on one
+genome): a synthetic 3.1 Gbp genome (24 contigs of U(50, 250) relative size,
+GC 41%, 45% copies of 500 interspersed repeat families with 300 bp-6 kbp
+consensus and 2-25% divergence, 3% tandem arrays), its full 15-mer index
+resident in HBM (built on the GPU with pbw_build_hash), and 10,000,000 reads
+trimmed to lengths U[60, 250], half single-end and half FR pairs (insert
+N(300, 80)), 0.5% substitutions and 0.05% indels (5x in homopolymers), Phred
+N(35, 4). One step maps one 1M-read chunk (500,000 single-end reads and
+250,000 pairs, each chunk an independent input mapped with the default
+options); the steps cycle through the 10 chunks. Three forms run on the same
+chunks: the plain method with batching off, the plain method with batching
+(length bins, autotuned band DP, pair graphs: `value`, bit-identical records)
+and ranked+batched (a candidate ranker trained on 2,000,000 fresh reads of the
+same genome). The line also carries parity against the oracle: a sample of the
+first chunk at this scale, the whole single-end configuration (1 Mbp, 10,000 x
+120 bp) and 40,000 pairs of the paired configuration (100 Mbp, 2 x 150 bp),
+plus the count of reads whose record depends on the SwissTable group width
+(8 vs 16) of the candidate tie order.
 
-One step maps the whole read set once. `value` is reads/s with the reads
-already in device memory (pbw_map_*_device-style timing from CUDA events on
-the pipeline's stream); `e2e` is the same metric through the public C ABI with
-pinned host buffers, host->device input copies and device->host record copies
-inside the timed region.
+--config 4: the repeat-stress workload (the 3.1 Gbp genome plus 200 families
+of 32-64 near-identical copies and homopolymer-rich regions; 2,000,000 pairs
+of 2 x 250 bp, insert N(500, 120), 3% substitutions, 0.3% indels, Phred
+N(28, 8), 30% of the pairs from the stress regions). --config 0 / 1: the
+single-end (1 Mbp) and paired-end (100 Mbp, 1,000,000 pairs) configurations,
+one step mapping the whole read set. Data are generated from fixed seeds; no
+dataset is downloaded.
+
+`value` is reads/s with the reads in pinned host memory and the device time
+of the pipeline's phases (CUDA events); `e2e` is the same metric through the
+public C ABI including every step's host->device input copies and
+device->host record copies (the calls' event spans).
 
 --impl reference times the CPU restatement of the reference path (oracle/)
-on the host cores instead.
+on the host cores on a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -36,13 +52,15 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SEED = {0: 0x5EED0000, 1: 0x5EED0001}
+SEED = {0: 0x5EED0000, 1: 0x5EED0001, 2: 0x5EED0002, 3: 0x5EED0002, 4: 0x5EED0004}
 CHUNK_READS = 131072  # the library's default chunk (pbw_options.chunk_reads = 0)
 # DRAM bytes (read + write) of K1 per read of the paired workload, from one
 # ncu capture of a 100,000-read launch (29.014 GB read + 0.161 GB written):
-# profiles/k_seed_paired_100k_pairs.md. Not measured for the single-end one.
+# profiles/k_seed_paired_100k_pairs.md. Not measured for the other workloads.
 SEED_DRAM_BYTES_PER_READ = {1: (29.014204e9 + 0.161155e9) / 100_000}
 METRIC = "reads/s @1 GB300: plain vs ranked+batched (≤0.05% primaries changed); DP GCUPS"
+LN_1E12 = -27.631021115928547     # ln(1e-12): ranker label cut of the repeat-family workloads
+STRICT_CUT = -41.58883083359672   # -60 ln 2: pruning cannot move sum_exp
 
 
 def log(*a):
@@ -72,7 +90,15 @@ def workload(cfg: int, cache: str, n_override: int | None = None):
             contigs = synth.genome_single(seed)
         else:
             contigs = synth.genome_paired(seed)
-        synth.write_index(prefix, contigs)
+        if cfg == 1 and _gpu_present():
+            # the 100 Mbp index: pbw_build_hash (byte-identical to the numpy
+            # and oracle builders, tests/test_index_build.py) in a second
+            synth.write_stidx(prefix, contigs)
+            import probebwa_gb300 as P
+            P.build()
+            P.build_hash(prefix, prefix)
+        else:
+            synth.write_index(prefix, contigs)
         log(f"[bench] index for config {cfg}: {time.time() - t:.1f}s")
         t = time.time()
         if cfg == 0:
@@ -85,6 +111,14 @@ def workload(cfg: int, cache: str, n_override: int | None = None):
         log(f"[bench] reads for config {cfg}: {time.time() - t:.1f}s")
     d = dict(np.load(rpath))
     return prefix, d, meta
+
+
+def _gpu_present() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
 
 
 # ---------------------------------------------------------------------------
@@ -213,6 +247,7 @@ def run_gpu(args, prefix, d, meta, rank, world):
     t_wall = time.time() - t_wall
     clocks = clk.stop()
     tuning = m.tuning()
+    plain_records = [_rec_copy(O1)] + ([_rec_copy(O2)] if paired else [])
     ranked = None
     if args.ranked and paired and world == 1:
         ranked = run_ranked(args, m, opts, step, O1, O2, meta, n_reads, dev)
@@ -283,12 +318,19 @@ def run_gpu(args, prefix, d, meta, rank, world):
         "dp_gcups": round(gcups, 2), "dp_cells_per_step": int(s0["dp_cells"]), "dp_jobs_per_step": int(s0["dp_jobs"]),
         "roofline": roofline, "roofline_dp": roofline_dp, "clocks": clocks, "wall_s_timed": round(t_wall, 3),
     }
+    out["_records"] = plain_records
     out["batching"] = {"band_dp_lanes_by_length_class": dict(zip(("<=128", "<=256", ">256"), tuning["chosen_lanes"])),
                        "band_dp_tuned_ms_8_16": dict(zip(("<=128", "<=256", ">256"), tuning["tuned_ms"])),
                        "length_bins": bool(tuning["length_bins"]), "pair_graphs": bool(tuning["pair_graphs"])}
     if ranked is not None:
         ranked["speedup_vs_plain"] = round(ranked["value"] / value, 3)
         out["ranked"] = ranked
+    if paired and world == 1:
+        # tie-order exposure: the same reads with the aarch64 SwissTable group width
+        with P.Mapper(prefix, options=P.MapperOptions(device=dev, group_width=8)) as m8:
+            g1, g2, _ = m8.map_paired(P.Reads(d["b1"], d["q1"], d["o1"]), P.Reads(d["b2"], d["q2"], d["o2"]))
+        out["tie_order_sensitive"] = int(_rec_diff(g1, out["_records"][0]) + _rec_diff(g2, out["_records"][1]))
+    m.close()
     return out
 
 
@@ -375,7 +417,7 @@ def run_ranked(args, m, opts, step, O1, O2, meta, n_reads, dev):
 # ---------------------------------------------------------------------------
 # CPU (reference path restatement)
 # ---------------------------------------------------------------------------
-def cpu_time(prefix, d, meta, n_sample: int, threads: int):
+def cpu_time(prefix, d, meta, n_sample: int, threads: int, records=False):
     from oracle import pyoracle as O
     O.build()
     m = O.Mapper(prefix, threads=threads)
@@ -386,22 +428,34 @@ def cpu_time(prefix, d, meta, n_sample: int, threads: int):
     if paired:
         o2 = d["o2"]
         R2 = O.Reads(d["b2"][:int(o2[k])], d["q2"][:int(o2[k])], o2[:k + 1])
-        t, _, _ = m.time_map_paired(R1, R2)
+        t, r1, r2 = m.time_map_paired(R1, R2)
+        recs = [r1, r2]
         reads = 2 * k
     else:
-        t, _ = m.time_map_single(R1)
+        t, r1 = m.time_map_single(R1)
+        recs = [r1]
         reads = k
     m.close()
-    return reads, t
+    return (reads, t, recs) if records else (reads, t)
 
 
-def cpu_baseline(prefix, d, meta):
+def cpu_baseline(prefix, d, meta, gpu_records=None):
+    """The oracle on the first reads (pairs) of the workload on every host
+    thread: its reads/s, and its records against the GPU's for the same reads
+    (the GPU mapped them as the first reads of the whole set, which the batch
+    schedule makes equivalent)."""
     threads = os.cpu_count() or 1
     n = 40_000 if meta["paired"] else 10_000
-    reads, t = cpu_time(prefix, d, meta, n, threads)
-    return {"value": round(reads / t, 1), "unit": "reads/s", "cores": threads, "kind": "port",
-            "sample": f"first {reads} reads ({'pairs' if meta['paired'] else 'reads'} incl. the serial warm-up) "
-                      f"of the same workload, oracle/ C++ restatement, {threads} threads"}
+    reads, t, recs = cpu_time(prefix, d, meta, n, threads, records=True)
+    cb = {"value": round(reads / t, 1), "unit": "reads/s", "cores": threads, "kind": "port",
+          "sample": f"first {reads} reads ({'pairs' if meta['paired'] else 'reads'} incl. the serial warm-up) "
+                    f"of the same workload, oracle/ C++ restatement, {threads} threads"}
+    if gpu_records is None:
+        return cb
+    par = [record_parity(g, e, len(e["contig"])) for g, e in zip(gpu_records, recs)]
+    parity = {"compared": sum(p["compared"] for p in par), "mismatched": sum(p["mismatched"] for p in par),
+              "by_read_set": par, "sample": cb["sample"]}
+    return cb, parity
 
 
 def run_reference(args, prefix, d, meta):
@@ -729,32 +783,613 @@ def run_stage_batch(args):
     return _stage_line("batch", meta, v, "reads/s", dict(res, speedup_vs_plain=round(v / res["plain"]["reads_per_s"], 3)))
 
 
+# ---------------------------------------------------------------------------
+# parity: records of the GPU path against the oracle's, field by field
+# ---------------------------------------------------------------------------
+PARITY_EXACT = ("contig", "pos", "mapq", "flag", "mate_contig", "mate_pos", "tlen", "as_score", "nm")
+
+
+def _cigar_rows(r, n):
+    """Per record the CIGAR words as bytes (for a row-by-row comparison)."""
+    co = r["cigar_off"].astype(np.int64)
+    cg = r["cigar"]
+    return [cg[co[i]:co[i + 1]].tobytes() for i in range(n)]
+
+
+def record_parity(got: dict, exp: dict, n: int | None = None, posterior_ulps: int = 4) -> dict:
+    """Reads whose records differ: bit-exact on every integer field, the
+    CIGAR and the log-likelihood bits; the posterior within a few ulps (its
+    last step is pow(10, -phred / 10) of a continuous phred). Returns the
+    count compared, the count mismatched and the mismatches per field."""
+    n = len(exp["contig"]) if n is None else n
+    bad = np.zeros(n, bool)
+    fields = {}
+    for k in PARITY_EXACT:
+        d = got[k][:n] != exp[k][:n]
+        if d.any():
+            fields[k] = int(d.sum())
+        bad |= d
+    d = got["log_lk"][:n].view(np.uint64) != exp["log_lk"][:n].view(np.uint64)
+    if d.any():
+        fields["log_lk"] = int(d.sum())
+    bad |= d
+    ep = exp["posterior"][:n]
+    d = np.abs(got["posterior"][:n] - ep) > posterior_ulps * np.spacing(np.maximum(np.abs(ep), 1e-300))
+    if d.any():
+        fields["posterior"] = int(d.sum())
+    bad |= d
+    gc, ec = _cigar_rows(got, n), _cigar_rows(exp, n)
+    d = np.array([a != b for a, b in zip(gc, ec)], bool) if n else np.zeros(0, bool)
+    if d.any():
+        fields["cigar"] = int(d.sum())
+    bad |= d
+    return {"compared": int(n), "mismatched": int(bad.sum()), "fields": fields}
+
+
+def _slice_reads(b, q, o, k):
+    o = o[:k + 1]
+    return b[:int(o[-1])], q[:int(o[-1])], o
+
+
+def _rec_copy(recs, n=None):
+    n = len(recs["contig"]) if n is None else n
+    out = {k: np.array(v[:n]) for k, v in recs.items() if not k.startswith("_") and k not in ("cigar_off", "cigar")}
+    co = recs["cigar_off"][:n + 1]
+    out["cigar_off"] = np.array(co)
+    out["cigar"] = np.array(recs["cigar"][:int(co[-1])])
+    return out
+
+
+def _rec_diff(a, b):
+    """Reads whose record differs in any field (tie-order exposure, batching
+    identity)."""
+    return record_parity(a, b)["mismatched"]
+
+
+# ---------------------------------------------------------------------------
+# hg38-scale workloads (configurations 2, 3 and 4)
+# ---------------------------------------------------------------------------
+class HgWorkload:
+    """Genome, index files and read chunks of the 3.1 Gbp configurations."""
+
+    def __init__(self, args, cfg: int):
+        import torch
+        import probebwa_gb300 as P
+        from probebwa_gb300 import synth_gpu as S
+        P.build()
+        self.cfg = 4 if cfg == 4 else 2
+        seed = SEED[self.cfg]
+        total = int(args.genome_bp)
+        cache = os.path.join(args.cache, f"hg{self.cfg}_{total}")
+        os.makedirs(cache, exist_ok=True)
+        self.prefix = os.path.join(cache, "genome")
+        t = time.time()
+        names, lens, codes = S.genome_hg(SEED[2], total=total)
+        self.regions = None
+        if self.cfg == 4:
+            codes, self.regions = S.add_stress(seed, codes, lens)
+        self.names, self.lens, self.codes = names, lens, codes
+        self.t_genome = time.time() - t
+        # the index files are cached per box; a checksum of the generated
+        # genome guards against a stale cache
+        g = torch.as_tensor(codes).cuda()
+        w = torch.arange(1, 8, device=g.device, dtype=torch.int64).repeat(len(codes) // 7 + 1)[:len(codes)]
+        csum = int((g.to(torch.int64) * w).sum().item())
+        meta_path = os.path.join(cache, "meta.json")
+        meta = json.load(open(meta_path)) if os.path.exists(meta_path) else {}
+        t = time.time()
+        if meta.get("checksum") != csum or not os.path.exists(self.prefix + ".sthash"):
+            S.write_stidx(self.prefix, names, lens, codes)
+            P.build_hash(self.prefix, self.prefix)
+            json.dump({"checksum": csum}, open(meta_path, "w"))
+            self.index_built = True
+        else:
+            self.index_built = False
+        self.t_index = time.time() - t
+        t = time.time()
+        self.chunks, self.train = [], None
+        if self.cfg == 2:
+            self.n_chunks = args.hg_chunks
+            for c in range(self.n_chunks):
+                se = S.reads(seed + 1000 + 2 * c, names, lens, codes, args.hg_se, 250, trim=(60, 250), g_dev=g)
+                pe = S.reads(seed + 1001 + 2 * c, names, lens, codes, args.hg_pairs, 250, paired=True, mean=300.0,
+                             sd=80.0, trim=(60, 250), g_dev=g)
+                self.chunks.append({"se": se, "pe": pe})
+            tr_se = S.reads(seed + 99, names, lens, codes, args.train_reads // 2, 250, trim=(60, 250), g_dev=g)
+            tr_pe = S.reads(seed + 98, names, lens, codes, args.train_reads // 4, 250, paired=True, mean=300.0,
+                            sd=80.0, trim=(60, 250), g_dev=g)
+            self.train = {"se": tr_se, "pe": tr_pe}
+            self.insert = (300.0, 80.0)
+        else:
+            self.n_chunks = args.hg_chunks
+            kw = dict(paired=True, mean=500.0, sd=120.0, sub=0.03, indel=0.003, qmu=28.0, qsd=8.0,
+                      regions=self.regions, region_frac=0.3, g_dev=g)
+            for c in range(self.n_chunks):
+                pe = S.reads(seed + 1001 + 2 * c, names, lens, codes, args.stress_pairs, 250, **kw)
+                self.chunks.append({"se": None, "pe": pe})
+            self.train = {"se": None, "pe": S.reads(seed + 98, names, lens, codes, args.train_reads // 2, 250, **kw)}
+            self.insert = (500.0, 120.0)
+        del g
+        torch.cuda.empty_cache()
+        self.t_reads = time.time() - t
+        self.reads_per_chunk = [(len(c["se"][2]) - 1 if c["se"] else 0) + 2 * (len(c["pe"][2]) - 1)
+                                for c in self.chunks]
+
+    def meta(self):
+        if self.cfg == 2:
+            w = ("batching + ranker: 3.1 Gbp hg38-scale genome (24 contigs, 45% from 500 repeat families, 3% tandem), "
+                 f"{sum(self.reads_per_chunk):,} reads of 60-250 bp in {self.n_chunks} chunks of "
+                 f"{self.reads_per_chunk[0]:,} (half single-end, half pairs, insert N(300,80))")
+        else:
+            w = ("repeat stress: 3.1 Gbp genome + 200 families x 32-64 near-identical copies + homopolymer-rich "
+                 f"regions, {sum(self.reads_per_chunk) // 2:,} pairs 2x250 in {self.n_chunks} chunks, insert "
+                 "N(500,120), 3% subs, 0.3% indels, Q N(28,8)")
+        return {"workload": w, "genome_bp": int(np.sum(self.lens)), "contigs": len(self.lens),
+                "reads": int(sum(self.reads_per_chunk)), "chunks": self.n_chunks,
+                "reads_per_step": int(self.reads_per_chunk[0]), "paired": True,
+                "seed": SEED[self.cfg], "generate_s": round(self.t_genome + self.t_reads, 1),
+                "index_s": round(self.t_index, 1), "index_built_here": self.index_built}
+
+
+def _hg_inputs(P, W):
+    """Pinned host copies of every chunk's reads (the C ABI's inputs)."""
+    out = []
+    for c in W.chunks:
+        d = {}
+        if c["se"] is not None:
+            d["se"] = P.Reads(*[pinned(x) for x in c["se"]])
+        b1, q1, o1, b2, q2, o2 = c["pe"]
+        d["p1"] = P.Reads(pinned(b1), pinned(q1), pinned(o1))
+        d["p2"] = P.Reads(pinned(b2), pinned(q2), pinned(o2))
+        out.append(d)
+    return out
+
+
+class HgRunner:
+    """Maps the chunks through the C ABI with pinned host buffers; one handle
+    for single-end reads and one for pairs (each has its own ranker)."""
+
+    def __init__(self, P, W, inputs, group_width=16):
+        import ctypes as C
+        self.P, self.W, self.C, self.L = P, W, C, P.lib()
+        self.inputs = inputs
+        opts = P.MapperOptions(group_width=group_width)
+        self.opts = opts
+        t = time.time()
+        self.ms = P.Mapper(W.prefix, options=opts) if W.cfg == 2 else None
+        self.mp = P.Mapper(W.prefix, options=opts)
+        self.t_open = time.time() - t
+        n_se = max([len(d["se"].offsets) - 1 for d in inputs if "se" in d] + [0])
+        b_se = max([len(d["se"].bases) for d in inputs if "se" in d] + [0])
+        n_pe = max(len(d["p1"].offsets) - 1 for d in inputs)
+        b_pe = max(max(len(d["p1"].bases), len(d["p2"].bases)) for d in inputs)
+        pin = lambda r: {k: pinned(v) for k, v in r.items()}
+        self.o_se = pin(P.alloc_records(n_se, b_se)) if n_se else None
+        self.o_p1 = pin(P.alloc_records(n_pe, b_pe))
+        self.o_p2 = pin(P.alloc_records(n_pe, b_pe))
+
+    def handles(self):
+        return [m for m in (self.ms, self.mp) if m is not None]
+
+    def set_tuning(self, **kw):
+        for m in self.handles():
+            m.set_tuning(**kw)
+
+    def _view(self, o, n):
+        r = {k: v[:n] for k, v in o.items() if k not in ("cigar_off", "cigar") and not k.startswith("_")}
+        r["cigar_off"] = o["cigar_off"][:n + 1]
+        r["cigar"] = o["cigar"]
+        return r
+
+    def step(self, c):
+        """Maps chunk c; returns (reads, device ms, end-to-end ms, stats list)."""
+        P, C, L = self.P, self.C, self.L
+        d = self.inputs[c]
+        stats, reads = [], 0
+        if "se" in d:
+            R = d["se"]
+            o = self._view(self.o_se, R.n)
+            self.ms._check(L.pbw_map_single(self.ms.h, C.byref(R.c()), C.byref(P.records_c(o))))
+            stats.append(self.ms.stats())
+            reads += R.n
+        R1, R2 = d["p1"], d["p2"]
+        o1, o2 = self._view(self.o_p1, R1.n), self._view(self.o_p2, R2.n)
+        mdl = P.InsertModelC(self.opts.insert_size_mean, self.opts.insert_size_sd, 0)
+        self.mp._check(L.pbw_map_paired(self.mp.h, C.byref(mdl), C.byref(R1.c()), C.byref(R2.c()),
+                                        C.byref(P.records_c(o1)), C.byref(P.records_c(o2))))
+        stats.append(self.mp.stats())
+        reads += R1.n + R2.n
+        dev = sum(s["ms_seed"] + s["ms_cluster"] + s["ms_align"] + s["ms_pair"] + s["ms_finalize"] + s["ms_d2h"]
+                  for s in stats)
+        e2e = sum(s["ms_total"] for s in stats)
+        return reads, dev, e2e, stats
+
+    def records(self, c):
+        """Copies of the records of the chunk mapped last (chunk c)."""
+        d = self.inputs[c]
+        out = {}
+        if "se" in d:
+            out["se"] = _rec_copy(self._view(self.o_se, d["se"].n))
+        out["p1"] = _rec_copy(self._view(self.o_p1, d["p1"].n))
+        out["p2"] = _rec_copy(self._view(self.o_p2, d["p2"].n))
+        return out
+
+    def close(self):
+        for m in self.handles():
+            m.close()
+
+
+def _sum_stats(stats):
+    keys = ("ms_seed", "ms_cluster", "ms_align", "ms_pair", "ms_finalize", "ms_d2h", "ms_total", "seed_probes",
+            "seed_entries", "seed_hits", "dp_jobs", "dp_cells", "kernel_launches", "window_jobs", "window_cells")
+    out = {k: 0 for k in keys}
+    for s in stats:
+        for k in keys:
+            out[k] += s[k]
+    return out
+
+
+def _timed_steps(R, W, warmup, steps, start, keep=None, clock=False):
+    """warmup + steps chunk maps from chunk `start` on; returns the timed
+    steps' totals and (with keep) the records of every chunk mapped."""
+    c = start
+    for _ in range(warmup):
+        R.step(c % W.n_chunks)
+        if keep is not None and c % W.n_chunks not in keep:
+            keep[c % W.n_chunks] = R.records(c % W.n_chunks)
+        c += 1
+    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if clock else None
+    if clk:
+        clk.start()
+    reads = dev = e2e = 0.0
+    all_stats = []
+    per_step = []
+    for _ in range(steps):
+        ci = c % W.n_chunks
+        n, d, e, st = R.step(ci)
+        if keep is not None and ci not in keep:
+            keep[ci] = R.records(ci)
+        reads += n
+        dev += d
+        e2e += e
+        all_stats += st
+        per_step.append(d)
+        c += 1
+    clocks = clk.stop() if clk else None
+    return {"reads": reads, "dev_ms": dev, "e2e_ms": e2e, "stats": _sum_stats(all_stats), "clocks": clocks,
+            "step_ms": per_step, "next": c}
+
+
+def _changes(recs, base):
+    """Reads whose primary (contig, POS, FLAG, CIGAR) or MAPQ changed."""
+    cp = cm = n = 0
+    for ci, r in recs.items():
+        for k in r:
+            a, b = _primary_changes(r[k], base[ci][k])
+            cp += a
+            cm += b
+            n += len(r[k]["contig"])
+    return cp, cm, n
+
+
+def _h2d_d2h(inputs, R, c):
+    d = inputs[c]
+    h2d = sum(int(x.bases.nbytes + x.quals.nbytes + x.offsets.nbytes) for k, x in d.items())
+    d2h = 0
+    for k, x in d.items():
+        o = R.records(c)[k]
+        d2h += sum(int(v.nbytes) for kk, v in o.items() if kk not in ("cigar",)) + 4 * len(o["cigar"])
+    return h2d, d2h
+
+
+def hg_oracle_sample(W, n_se, n_pairs, threads):
+    """The oracle on the first n_se single-end reads and n_pairs pairs of
+    chunk 0 (mapped from the default insert model, as the GPU maps the
+    chunk): records and the seconds each part took."""
+    from oracle import pyoracle as O
+    O.build()
+    t = time.time()
+    om = O.Mapper(W.prefix, threads=threads)
+    t_open = time.time() - t
+    c = W.chunks[0]
+    out, secs, reads = {}, 0.0, 0
+    if c["se"] is not None and n_se:
+        b, q, o = _slice_reads(*c["se"], n_se)
+        t, out["se"] = om.time_map_single(O.Reads(b, q, o))
+        secs += t
+        reads += n_se
+    b1, q1, o1, b2, q2, o2 = c["pe"]
+    R1 = O.Reads(*_slice_reads(b1, q1, o1, n_pairs))
+    R2 = O.Reads(*_slice_reads(b2, q2, o2, n_pairs))
+    t, out["p1"], out["p2"] = om.time_map_paired(R1, R2)
+    secs += t
+    reads += 2 * n_pairs
+    om.close()
+    return out, secs, reads, t_open
+
+
+def int32_peak():
+    """Measured INT32 add and max throughput of this GPU (independent chains,
+    CUDA events): G ops/s."""
+    import ctypes as C
+    import probebwa_gb300 as P
+    L = P.lib()
+    add, mx = C.c_double(0), C.c_double(0)
+    rc = L.pbw_int32_peak(0, C.byref(add), C.byref(mx))
+    return (add.value, mx.value) if rc == 0 else (None, None)
+
+
+def run_hg(args, rank, world):
+    import torch
+    import probebwa_gb300 as P
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    t_all = time.time()
+    W = HgWorkload(args, args.config)
+    log(f"[bench] hg workload ready: genome {W.t_genome:.1f}s index {W.t_index:.1f}s reads {W.t_reads:.1f}s")
+    inputs = _hg_inputs(P, W)
+    R = HgRunner(P, W, inputs)
+    log(f"[bench] handles open: {R.t_open:.1f}s")
+    plain = {}
+    # 1. the plain method with batching (the drop-in path; `value`)
+    main = _timed_steps(R, W, args.warmup, args.steps, 0, keep=plain, clock=True)
+    tuning = {k: (m.tuning() if m else None) for k, m in (("single", R.ms), ("pairs", R.mp))}
+    nxt = main["next"]
+    # every chunk's plain records (for the other forms' comparisons)
+    for ci in range(W.n_chunks):
+        if ci not in plain:
+            R.step(ci)
+            plain[ci] = R.records(ci)
+    h2d, d2h = _h2d_d2h(inputs, R, (nxt - 1) % W.n_chunks)
+    steps_other = min(args.steps, args.other_steps) if args.other_steps else args.steps
+    warm_other = max(3, min(args.warmup, 3))
+    # 2. batching off
+    R.set_tuning(length_bins=0, autotune=0, band_lanes=8, pair_graphs=0)
+    recs_u = {}
+    unb = _timed_steps(R, W, warm_other, steps_other, 0, keep=recs_u)
+    R.set_tuning(length_bins=1, autotune=1, band_lanes=0, pair_graphs=1)
+    differ_unbatched = sum(_rec_diff(recs_u[ci][k], plain[ci][k]) for ci in recs_u for k in recs_u[ci])
+    # 3. ranked + batched: rankers trained on fresh reads of the same genome
+    t = time.time()
+    cut = args.label_cut
+    train = {}
+    if R.ms is not None and W.train["se"] is not None:
+        train["single"] = R.ms.ranker_train(P.Reads(*W.train["se"]), label_cut=cut)
+        R.ms.ranker_enable(True)
+    b1, q1, o1, b2, q2, o2 = W.train["pe"]
+    train["pairs"] = R.mp.ranker_train(P.Reads(b1, q1, o1), P.Reads(b2, q2, o2), label_cut=cut)
+    R.mp.ranker_enable(True)
+    t_train = time.time() - t
+    for m in R.handles():
+        m.ranker_enable(True)  # counters from here
+    recs_r = {}
+    rk = _timed_steps(R, W, warm_other, steps_other, 0, keep=recs_r)
+    cnt = [m.ranker_counters() for m in R.handles()]
+    for m in R.handles():
+        m.ranker_enable(False)
+    ch_p, ch_m, n_cmp = _changes(recs_r, plain)
+    R.close()
+    # 4. tie-order exposure: chunk 0 with the aarch64 SwissTable group width
+    R8 = HgRunner(P, W, inputs[:1], group_width=8)
+    R8.step(0)
+    r8 = R8.records(0)
+    R8.close()
+    tie = sum(_rec_diff(r8[k], plain[0][k]) for k in r8)
+    n_tie = sum(len(r8[k]["contig"]) for k in r8)
+    # 5. parity against the oracle on a sample of chunk 0 (also the CPU baseline)
+    threads = os.cpu_count() or 1
+    orc, t_cpu, n_cpu, t_orc_open = hg_oracle_sample(W, args.parity_se if W.cfg == 2 else 0, args.parity_pairs,
+                                                     threads)
+    par = {}
+    for k, r in orc.items():
+        par[k] = record_parity(plain[0][k], r, len(r["contig"]))
+    # rooflines
+    s = main["stats"]
+    value = main["reads"] / (main["dev_ms"] / 1e3)
+    e2e = main["reads"] / (main["e2e_ms"] / 1e3)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    bases = sum(int(inputs[ci % W.n_chunks][k].offsets[-1]) for ci in range(args.steps)
+                for k in inputs[ci % W.n_chunks])
+    n_launch_seed = sum(-(-(len(inputs[ci % W.n_chunks][k].offsets) - 1) // CHUNK_READS)
+                        for ci in range(args.steps) for k in inputs[ci % W.n_chunks])
+    seed_bytes = (bases + (bases + 3) // 4) + 8 * (s["seed_probes"] + s["seed_entries"] + s["seed_hits"])
+    seed_gbs = seed_bytes / (s["ms_seed"] / 1e3) / 1e9 if s["ms_seed"] > 0 else 0.0
+    roofline = {"kernel": "k_seed (K1 seeding)", "bound": "hbm", "achieved": round(seed_gbs, 1), "peak": hbm_peak,
+                "unit": "GB/s", "frac": round(seed_gbs / hbm_peak, 4), "traffic": None,
+                "traffic_note": "no ncu capture of this workload's seeding yet",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst), of measured" if peaks else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": int(seed_bytes / max(n_launch_seed, 1)),
+                "launches_in_timed_region": int(n_launch_seed)}
+    add_g, max_g = int32_peak()
+    gcups = s["dp_cells"] / (s["ms_align"] / 1e3) / 1e9 if s["ms_align"] > 0 else 0.0
+    int_peak = max(x for x in (add_g, max_g) if x) if (add_g or max_g) else None
+    roofline_dp = {"kernel": "k_align_band (seeded banded DP, the seeded-alignment phase)", "bound": "int32 issue",
+                   "achieved_gcups": round(gcups, 1), "int_ops_per_cell": 10,
+                   "achieved_gops": round(gcups * 10, 1),
+                   "peak_gops": round(int_peak, 1) if int_peak else None,
+                   "frac": round(gcups * 10 / int_peak, 4) if int_peak else None,
+                   "peak_source": ("pbw_int32_peak: independent add.s32 / max.s32 chains, CUDA events, the larger "
+                                   f"of add {add_g:.0f} and max {max_g:.0f} G ops/s") if int_peak else None,
+                   "cells_in_timed_region": int(s["dp_cells"])}
+    phases = {k[3:]: round(s[k], 2) for k in ("ms_seed", "ms_cluster", "ms_align", "ms_pair", "ms_finalize",
+                                                "ms_d2h")}
+    tot_r = sum(c["kept"] + c["pruned"] for c in cnt)
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "reads/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(main["dev_ms"] / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded)",
+        "config": dict(W.meta(), l2="inputs larger than L2: 4 GiB k-mer CSR + ~10 GB positions + genome + reads",
+                       parallelism=f"replicas x{world}", handles_open_s=round(R.t_open, 1),
+                       step="one 1M-read chunk (single-end call + paired call), chunks cycled"),
+        "e2e": {"value": round(e2e, 1), "unit": "reads/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(main["e2e_ms"] / args.steps, 3)},
+        "gpu_launches": int(s["kernel_launches"]),
+        "dp_gcups": round(gcups, 2), "dp_cells_per_step": int(s["dp_cells"] / args.steps),
+        "phase_ms_per_step": {k: round(v / args.steps, 2) for k, v in phases.items()},
+        "roofline": roofline, "roofline_dp": roofline_dp, "clocks": main["clocks"],
+        "modes": {
+            "plain_unbatched": {"value": round(unb["reads"] / (unb["dev_ms"] / 1e3), 1), "steps": steps_other,
+                                "records_differing_from_batched": int(differ_unbatched)},
+            "plain_batched": {"value": round(value, 1), "steps": args.steps},
+            "ranked_batched": {"value": round(rk["reads"] / (rk["dev_ms"] / 1e3), 1), "steps": steps_other,
+                               "e2e": round(rk["reads"] / (rk["e2e_ms"] / 1e3), 1),
+                               "changed_primary_frac": ch_p / max(n_cmp, 1),
+                               "changed_mapq_frac": ch_m / max(n_cmp, 1), "reads_compared": int(n_cmp),
+                               "candidates_pruned_frac": round(sum(c["pruned"] for c in cnt) / tot_r, 4) if tot_r
+                               else 0.0,
+                               "label_cut": cut, "train_s": round(t_train, 1),
+                               "train": {k: {kk: v[kk] for kk in ("samples", "positives", "train_recall",
+                                                                  "train_prune")} for k, v in train.items()}},
+        },
+        "batching": {"tuning": tuning},
+        "parity": {"oracle_sample": par, "compared": sum(v["compared"] for v in par.values()),
+                   "mismatched": sum(v["mismatched"] for v in par.values()),
+                   "sample": f"chunk 0: first {args.parity_se if W.cfg == 2 else 0} single-end reads and "
+                             f"first {args.parity_pairs} pairs",
+                   "tie_order_sensitive": int(tie), "tie_order_compared": int(n_tie),
+                   "tie_order_note": "reads of chunk 0 whose record differs between SwissTable group widths 16 "
+                                     "(x86_64, the default) and 8 (aarch64)"},
+    }
+    r_u = out["modes"]["plain_unbatched"]["value"]
+    out["modes"]["speedup_ranked_batched_vs_plain_unbatched"] = round(out["modes"]["ranked_batched"]["value"] / r_u, 3)
+    out["modes"]["speedup_ranked_batched_vs_plain_batched"] = round(out["modes"]["ranked_batched"]["value"] / value, 3)
+    out["cpu_baseline"] = {"value": round(n_cpu / t_cpu, 1), "unit": "reads/s", "cores": threads, "kind": "port",
+                           "sample": f"the oracle parity sample ({n_cpu} reads of chunk 0), oracle/ C++ "
+                                     f"restatement on {threads} threads; oracle index load {t_orc_open:.1f}s "
+                                     "not timed"}
+    if args.small_parity and W.cfg == 2:
+        out["parity"]["single_end_config"] = small_parity(args, 0)
+        out["parity"]["paired_config"] = small_parity(args, 1)
+    out["wall_s"] = round(time.time() - t_all, 1)
+    return out
+
+
+def small_parity(args, cfg):
+    """The GPU path against the oracle on the whole single-end configuration
+    (cfg 0, 10,000 reads) or on 40,000 pairs of the paired one (cfg 1)."""
+    import probebwa_gb300 as P
+    from oracle import pyoracle as O
+    n = 10_000 if cfg == 0 else args.parity_cfg1_pairs
+    prefix, d, meta = workload(cfg, args.cache, n)
+    O.build()
+    om = O.Mapper(prefix, threads=os.cpu_count() or 1)
+    with P.Mapper(prefix) as m:
+        if cfg == 0:
+            R = P.Reads(d["b1"], d["q1"], d["o1"])
+            got = {"se": m.map_single(R)}
+            exp = {"se": om.map_single(O.Reads(R.bases, R.quals, R.offsets))}
+        else:
+            R1, R2 = P.Reads(d["b1"], d["q1"], d["o1"]), P.Reads(d["b2"], d["q2"], d["o2"])
+            g1, g2, _ = m.map_paired(R1, R2)
+            e1, e2, _ = om.map_paired(O.Reads(R1.bases, R1.quals, R1.offsets), O.Reads(R2.bases, R2.quals, R2.offsets))
+            got, exp = {"p1": g1, "p2": g2}, {"p1": e1, "p2": e2}
+    with P.Mapper(prefix, group_width=8) as m8:
+        if cfg == 0:
+            g8 = {"se": m8.map_single(R)}
+        else:
+            a, b, _ = m8.map_paired(R1, R2)
+            g8 = {"p1": a, "p2": b}
+    om.close()
+    par = {k: record_parity(got[k], exp[k]) for k in got}
+    return {"workload": meta["workload"] + (f" (first {n} pairs)" if cfg == 1 else ""),
+            "compared": sum(v["compared"] for v in par.values()),
+            "mismatched": sum(v["mismatched"] for v in par.values()), "by_read_set": par,
+            "tie_order_sensitive": int(sum(_rec_diff(g8[k], got[k]) for k in got))}
+
+
+def run_reference_hg(args):
+    """The oracle (C++ restatement of the reference's CPU path) on a bounded
+    sample of each step's chunk, all host threads."""
+    W = HgWorkload(args, args.config)
+    from oracle import pyoracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    t = time.time()
+    om = O.Mapper(W.prefix, threads=threads)
+    t_open = time.time() - t
+    n_se, n_pe = args.ref_se, args.ref_pairs
+
+    def one(c):
+        ch = W.chunks[c % W.n_chunks]
+        secs, reads = 0.0, 0
+        if ch["se"] is not None and n_se:
+            tt, _ = om.time_map_single(O.Reads(*_slice_reads(*ch["se"], n_se)))
+            secs += tt
+            reads += n_se
+        b1, q1, o1, b2, q2, o2 = ch["pe"]
+        tt, _, _ = om.time_map_paired(O.Reads(*_slice_reads(b1, q1, o1, n_pe)), O.Reads(*_slice_reads(b2, q2, o2, n_pe)))
+        return secs + tt, reads + 2 * n_pe
+
+    for c in range(args.warmup):
+        one(c)
+    times, reads = [], 0
+    for c in range(args.steps):
+        tt, n = one(args.warmup + c)
+        times.append(tt)
+        reads += n
+    om.close()
+    v = reads / sum(times)
+    sample = (f"per step the first {n_se if W.cfg == 2 else 0} single-end reads and {n_pe} pairs of that step's "
+              f"1M-read chunk ({'half single-end, half pairs' if W.cfg == 2 else 'pairs'}), oracle/ C++ restatement "
+              f"of the reference CPU path on {threads} threads; index load {t_open:.1f}s not timed")
+    cb = {"value": round(v, 1), "unit": "reads/s", "cores": threads, "kind": "port", "sample": sample}
+    return {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "reads/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(times) * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+            "data": "synthetic (seeded)", "config": W.meta(), "cpu_baseline": cb,
+            "e2e": {"value": round(v, 1), "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1])
-    ap.add_argument("--n", type=int, default=None, help="override read / pair count")
+    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4],
+                    help="2 (default) and 3: the 3.1 Gbp batching + ranker workload; 4: repeat stress; "
+                         "0 / 1: the single-end and paired configurations")
+    ap.add_argument("--n", type=int, default=None, help="override read / pair count (configs 0 and 1)")
     ap.add_argument("--cache", default=os.environ.get("PBW_BENCH_CACHE", "/tmp/pbw_bench_cache"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ranked", type=int, default=1, help="also time the ranked path (pairs, 1 GPU)")
-    ap.add_argument("--train-pairs", type=int, default=250_000, help="fresh pairs the ranker is trained on")
+    ap.add_argument("--ranked", type=int, default=1, help="also time the ranked path (configs 0 / 1, 1 GPU)")
+    ap.add_argument("--train-pairs", type=int, default=250_000, help="fresh pairs the ranker is trained on (config 1)")
     ap.add_argument("--label-cut", type=float, default=None,
-                    help="ranker training label: lk - lk_max >= cut (default: -60 ln 2 for the paired "
-                         "workload, where pruning then cannot move sum_exp; ln 1e-12 for --stage batch)")
+                    help="ranker training label: lk - lk_max >= cut (default: ln 1e-12 for the repeat-family "
+                         "workloads, -60 ln 2, where pruning cannot move sum_exp, for the paired one)")
+    # hg38-scale workloads
+    ap.add_argument("--genome-bp", type=float, default=3.1e9)
+    ap.add_argument("--hg-chunks", type=int, default=10)
+    ap.add_argument("--hg-se", type=int, default=500_000, help="single-end reads per chunk (config 2)")
+    ap.add_argument("--hg-pairs", type=int, default=250_000, help="pairs per chunk (config 2)")
+    ap.add_argument("--stress-pairs", type=int, default=250_000, help="pairs per chunk (config 4)")
+    ap.add_argument("--train-reads", type=int, default=2_000_000, help="fresh reads the rankers are trained on")
+    ap.add_argument("--other-steps", type=int, default=10, help="timed steps of the unbatched and ranked forms")
+    ap.add_argument("--parity-se", type=int, default=50_000)
+    ap.add_argument("--parity-pairs", type=int, default=25_000)
+    ap.add_argument("--parity-cfg1-pairs", type=int, default=40_000)
+    ap.add_argument("--small-parity", type=int, default=1, help="add configs 0 / 1 parity to the config 2 line")
+    ap.add_argument("--ref-se", type=int, default=8_000)
+    ap.add_argument("--ref-pairs", type=int, default=4_000)
     ap.add_argument("--stage", default="map", choices=["map", "index", "sam", "cli", "batch"],
                     help="map: the mapping path (default); index / sam / cli: build-hash, SAM output and the "
                          "command line, each against the oracle")
     args = ap.parse_args()
+    hg = args.config in (2, 3, 4)
     if args.label_cut is None:
-        args.label_cut = -27.631021115928547 if args.stage == "batch" else -41.58883083359672
+        args.label_cut = LN_1E12 if (args.stage == "batch" or hg) else STRICT_CUT
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         if rank != 0:
+            return
+        if hg:
+            print(json.dumps(run_reference_hg(args)), flush=True)
             return
         prefix, d, meta = workload(args.config, args.cache, args.n)
         print(json.dumps(run_reference(args, prefix, d, meta)), flush=True)
@@ -774,11 +1409,17 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    prefix, d, meta = workload(args.config, args.cache, args.n)
-    out = run_gpu(args, prefix, d, meta, rank, world)
+    if hg:
+        out = run_hg(args, rank, world)
+    else:
+        prefix, d, meta = workload(args.config, args.cache, args.n)
+        out = run_gpu(args, prefix, d, meta, rank, world)
+        recs = out.pop("_records")
+        if rank == 0 and not args.no_cpu_baseline:
+            out["cpu_baseline"], out["parity"] = cpu_baseline(prefix, d, meta, recs)
+            if "tie_order_sensitive" in out:
+                out["parity"]["tie_order_sensitive"] = out.pop("tie_order_sensitive")
     if rank == 0:
-        if not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(prefix, d, meta)
         print(json.dumps(out), flush=True)
     if world > 1:
         import torch

@@ -166,14 +166,19 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
  * the hit count and, in emission order, hits packed as
  * (strand << 63) | (contig << 40) | ref_pos with read_pos in hit_read_pos;
  * repeat_prob per 15-mer window (n_windows = len - 14). hit_off (n+1) and
- * win_off (n+1) are computed by the call. */
+ * win_off (n+1) are computed by the call. Reads with more hits than the
+ * per-read buffer (4096) are seeded again into the overflow pool as in a map
+ * call, so every read's list is complete; PBW_ERR_CAPACITY when hit_cap or
+ * win_cap is too small. */
 int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uint64_t* hits,
                    uint32_t* hit_read_pos, uint64_t hit_cap, uint64_t* win_off, double* repeat_prob,
                    uint64_t win_cap);
 
 /* cluster_hits (src/mapper/candidates.rs:30-78) after seeding: per read the
  * first max_per_read candidates in final order (contig, 0-based position,
- * strand, score) and the full candidate count. */
+ * strand, score) and the full candidate count. Row i of the candidate
+ * arrays starts at i * max_per_read; its first n_cand[i] entries are set.
+ * Over-capacity reads are clustered from the overflow pool as in a map call. */
 int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_read, uint32_t* n_cand,
                       uint32_t* total_cand, uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,
                       double* cand_score);
@@ -329,7 +334,15 @@ int pbw_build_hash(const char* genome_prefix, const char* out_prefix, uint64_t k
  * chosen_lanes / tuned_ms are outputs of pbw_get_tuning: the form chosen
  * per read-length class (0 = not tuned yet) and the two timings (8 lanes,
  * 16 lanes, ms) that chose it. All settings are on by default.
- * pbw_set_tuning reads the four inputs and clears the tuned choices. */
+ * wait_polls: the whole-window DP's warps wait for the warp to their left
+ *   with a bounded spin; after this many polls (0 = the default, 2^22) the
+ *   wait gives up, the call discards its results and returns PBW_ERR_DEVICE.
+ *   Lowering it only serves to exercise that path.
+ * ovf_slice_hits: reads with more than 4096 seed hits are seeded again into
+ *   an overflow pool one slice of this many hits at a time (0 = the default,
+ *   16 M; larger values are clamped to it). A chunk's over-capacity reads may
+ *   hold 16 default slices in all, and one read one slice.
+ * pbw_set_tuning reads the inputs and clears the tuned choices. */
 typedef struct {
   int32_t autotune;
   int32_t band_lanes;
@@ -337,6 +350,8 @@ typedef struct {
   int32_t pair_graphs;
   int32_t chosen_lanes[3];
   float tuned_ms[3][2];
+  uint32_t wait_polls;
+  uint32_t ovf_slice_hits;
 } pbw_tuning;
 int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t);
 int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t);
@@ -391,35 +406,45 @@ int pbw_ranker_score(pbw_handle* h, const float* feat, uint64_t n, float* logit)
 int pbw_ranker_import(pbw_handle* h, const float* in, uint64_t n);
 
 /* Allocation-free window alignment. No counterpart in the reference: it exists
- * for callers that cannot call cudaMalloc -- code running while a stream is
- * captured into a CUDA graph, applications whose allocator owns all device
- * memory, fixed-budget real-time loops. It performs the same alignment as
- * pbw_align_batch (SmithWatermanAligner::align) on the wide-band DP kernel and
- * needs no handle.
+ * for callers that must not call cudaMalloc -- a host application whose own
+ * allocator has reserved the GPU's memory (a framework's caching allocator, a
+ * pool sized at start-up) or a loop with a fixed device-memory budget. It
+ * performs the same alignment as pbw_align_batch
+ * (SmithWatermanAligner::align) on the wide-band DP kernel and needs no
+ * handle.
  *
  * Every pointer is DEVICE memory owned by the caller: n problems with reads /
  * quals concatenated at read_off (n+1), reference windows concatenated at
  * ref_off (n+1), hint[n], band[n]; outputs score[n], offset[n] (start of the
  * alignment in its window), n_ops[n] and cigar[n * cigar_stride] ((len << 4) |
  * op, op 0=M 1=I 2=D 4=S), the i-th CIGAR at cigar + i * cigar_stride.
- * stream is a cudaStream_t (NULL = legacy default stream); the call returns
- * after the stream has finished its work.
+ * stream is a cudaStream_t (NULL = legacy default stream); the call
+ * synchronises that stream: it returns after the stream has finished its work.
  *
  * Limits: n <= 4096 problems per call, reads <= 256 bases, windows <= 2048
- * bases; beyond them PBW_ERR_LIMIT, and a CIGAR longer than cigar_stride gives
- * PBW_ERR_CAPACITY; pbw_last_error(NULL) describes the failure.
+ * bases; beyond them PBW_ERR_LIMIT (a read or window over its limit is
+ * detected on the device, the others are still aligned), and a CIGAR longer
+ * than cigar_stride gives PBW_ERR_CAPACITY; pbw_last_error(NULL) describes
+ * the failure. CIGARs longer than 12 operations share a static pool sized for
+ * the worst case (2 x 256 + 1 operations for each of 4096 problems).
  *
- * Scratch: a file-scope device array of about 6 MB, held on every GPU that
+ * Scratch: a file-scope device array of about 14 MB, held on every GPU that
  * loads the library until the process exits. The first call on a device (with
  * that device current) looks up the array's device address and writes its
- * parameter table; make that first call before any stream capture. Every call
- * reuses the same array and clears its counters first, so calls that overlap
- * on the GPU (two streams, two host threads) race and must be serialised by
- * the caller. */
+ * parameter table with a synchronous copy; that first call should come before
+ * any stream capture. Every call reuses the same array and clears its
+ * counters first, so calls that overlap on the GPU (two streams, two host
+ * threads) race and must be serialised by the caller. */
 int pbw_align_noalloc(uint64_t n, const uint8_t* reads, const uint8_t* quals, const uint64_t* read_off,
                       const uint8_t* refs, const uint64_t* ref_off, const int64_t* hint, const uint64_t* band,
                       uint32_t gap_open_phred, uint32_t gap_extend_phred, int32_t* score, uint64_t* offset,
                       uint32_t* n_ops, uint32_t* cigar, uint32_t cigar_stride, void* stream);
+
+/* Measured integer throughput of a device (no counterpart in the reference):
+ * G operations/s of add.s32 and of max.s32 over independent dependency
+ * chains on every SM, timed with CUDA events. The banded DP is a max-plus
+ * recurrence on 32-bit integers; these are its roofline denominators. */
+int pbw_int32_peak(int32_t device, double* add_gops, double* max_gops);
 
 #ifdef __cplusplus
 }

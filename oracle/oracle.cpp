@@ -22,6 +22,11 @@
 #include <utility>
 #include <vector>
 
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 namespace orc {
 
 using u8 = uint8_t;
@@ -430,16 +435,74 @@ struct FlatTable {
   }
 };
 
+// A read-only view of a whole file (mmap).
+struct MappedFile {
+  const u8* p = nullptr;
+  size_t n = 0;
+  bool open(const std::string& path) {
+    int fd = ::open(path.c_str(), O_RDONLY);
+    if (fd < 0) return false;
+    struct stat st;
+    if (fstat(fd, &st) != 0) { ::close(fd); return false; }
+    n = (size_t)st.st_size;
+    void* m = n ? mmap(nullptr, n, PROT_READ, MAP_PRIVATE, fd, 0) : nullptr;
+    ::close(fd);
+    if (n && m == MAP_FAILED) { n = 0; return false; }
+    p = (const u8*)m;
+    return true;
+  }
+  ~MappedFile() { if (p) munmap((void*)p, n); }
+};
+
+// Direct-address table over the 32-bit hash: word = (count << 32) | offset,
+// count 0 = no bucket. Used for tables too large for FlatTable's single-thread
+// build (a 3.1 Gbp genome has ~7e8 buckets); an anonymous mapping, so only
+// the pages of present keys are ever touched.
+struct DenseMap {
+  static constexpr size_t BYTES = sizeof(u64) << 32;
+  u64* w = nullptr;
+  bool init() {
+    void* m = mmap(nullptr, BYTES, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS | MAP_NORESERVE, -1, 0);
+    if (m == MAP_FAILED) return false;
+    w = (u64*)m;
+    return true;
+  }
+  DenseMap() = default;
+  DenseMap(const DenseMap&) = delete;
+  DenseMap& operator=(const DenseMap&) = delete;
+  DenseMap(DenseMap&& o) noexcept : w(o.w) { o.w = nullptr; }
+  DenseMap& operator=(DenseMap&& o) noexcept { std::swap(w, o.w); return *this; }
+  ~DenseMap() { if (w) munmap(w, BYTES); }
+};
+
+template <class F>
+static void on_threads(size_t n, F f) {
+  unsigned t = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+  if (n < (1u << 20)) t = 1;
+  std::vector<std::thread> th;
+  for (unsigned k = 0; k < t; k++) th.emplace_back([&, k] { f(n * k / t, n * (k + 1) / t); });
+  for (auto& x : th) x.join();
+}
+
 struct HashTable {
   FlatTable table;
+  DenseMap dense;  // instead of table for large loaded files
   std::vector<u64> positions;
   u64 k = 15, seed_stride = 5, total_entries = 0;
-  // In-file entry order, kept for save().
+  // In-file entry order, kept for save() (tables built or loaded through
+  // FlatTable).
   std::vector<std::pair<u32, std::pair<u32, u32>>> entries;
 
   // HashTable::lookup / get (hashtable.rs:90-102).
   inline void lookup(const u8* kmer, size_t len, const u64*& ptr, u64& cnt) const {
-    const std::pair<u32, u32>* v = table.get(hash_kmer(kmer, len));
+    const u32 key = hash_kmer(kmer, len);
+    if (dense.w) {
+      const u64 v = dense.w[key];
+      cnt = v >> 32;
+      ptr = cnt ? positions.data() + (u32)v : nullptr;
+      return;
+    }
+    const std::pair<u32, u32>* v = table.get(key);
     if (!v) { ptr = nullptr; cnt = 0; return; }
     ptr = positions.data() + v->first;
     cnt = v->second;
@@ -449,6 +512,7 @@ struct HashTable {
   // seed_stride, total_entries}. The map is written in the builder's
   // ascending-hash order (a map's content, not its order, is the format).
   bool save(const std::string& prefix) const {
+    if (dense.w) { g_err = "save of a table loaded as a direct-address map"; return false; }
     BinWriter w;
     w.u64v(entries.size());
     for (auto& e : entries) { w.u32v(e.first); w.u32v(e.second.first); w.u32v(e.second.second); }
@@ -460,37 +524,60 @@ struct HashTable {
     return w.save(prefix + ".sthash");
   }
 
-  // HashTable::load (hashtable.rs:73-79).
-  bool load(const std::string& prefix) {
-    BinReader r;
-    if (!r.load(prefix + ".sthash")) { g_err = "cannot open " + prefix + ".sthash"; return false; }
+  // HashTable::load (hashtable.rs:73-79) over a mapping of the file.
+  bool load(const std::string& prefix, u64 dense_min = 1ull << 24) {
+    MappedFile f;
+    if (!f.open(prefix + ".sthash")) { g_err = "cannot open " + prefix + ".sthash"; return false; }
+    size_t p = 0;
+    auto need = [&](size_t n) {
+      if (p + n > f.n || p + n < p) throw std::runtime_error("bincode: unexpected end of file");
+    };
+    auto u64v = [&]() { need(8); u64 v; memcpy(&v, f.p + p, 8); p += 8; return v; };
     try {
-      u64 n = r.u64v();
-      entries.resize(n);
-      table.init(n);
-      for (auto& e : entries) {
-        e.first = r.u32v();
-        e.second.first = r.u32v();
-        e.second.second = r.u32v();
-        table.insert(e.first, e.second);
-      }
-      u64 np = r.u64v();
-      r.need(np * 8);
+      const u64 n = u64v();
+      if (n > (f.n - p) / 12) throw std::runtime_error("bincode: unexpected end of file");
+      const u8* tab = f.p + p;
+      p += n * 12;
+      const u64 np = u64v();
+      if (np > (f.n - p) / 8) throw std::runtime_error("bincode: unexpected end of file");
+      const u8* pos = f.p + p;
+      p += np * 8;
+      k = u64v();
+      seed_stride = u64v();
+      total_entries = u64v();
       positions.resize(np);
-      memcpy(positions.data(), &r.data[r.p], np * 8);
-      r.p += np * 8;
-      k = r.u64v();
-      seed_stride = r.u64v();
-      total_entries = r.u64v();
+      on_threads(np, [&](size_t a, size_t b) { memcpy(positions.data() + a, pos + a * 8, (b - a) * 8); });
+      auto entry = [&](size_t i, u32& key, u32& off, u32& cnt) {
+        memcpy(&key, tab + 12 * i, 4);
+        memcpy(&off, tab + 12 * i + 4, 4);
+        memcpy(&cnt, tab + 12 * i + 8, 4);
+      };
+      std::atomic<bool> bad{false};
+      if (n > dense_min) {
+        if (!dense.init()) { g_err = "cannot map the direct-address table"; return false; }
+        on_threads(n, [&](size_t a, size_t b) {
+          for (size_t i = a; i < b; i++) {
+            u32 key, off, cnt;
+            entry(i, key, off, cnt);
+            if ((u64)off + cnt > np || cnt == 0) bad = true;
+            dense.w[key] = ((u64)cnt << 32) | off;
+          }
+        });
+      } else {
+        entries.resize(n);
+        table.init(n);
+        for (size_t i = 0; i < n; i++) {
+          u32 key, off, cnt;
+          entry(i, key, off, cnt);
+          entries[i] = {key, {off, cnt}};
+          table.insert(key, {off, cnt});
+          if ((u64)off + cnt > np) bad = true;
+        }
+      }
+      if (bad) { g_err = "sthash: bucket out of range"; return false; }
     } catch (std::exception& e) {
       g_err = e.what();
       return false;
-    }
-    for (auto& e : entries) {
-      if ((u64)e.second.first + e.second.second > positions.size()) {
-        g_err = "sthash: bucket out of range";
-        return false;
-      }
     }
     return true;
   }
@@ -1269,7 +1356,7 @@ struct Mapper {
   bool open(const std::string& gp, const std::string& hp, const orc_options& o) {
     opt = o;
     if (!genome.load(gp)) return false;
-    if (!ht.load(hp)) return false;
+    if (!ht.load(hp, opt.dense_min_buckets)) return false;
     sw.reset(new Aligner(opt.max_indel_len, opt.gap_open_phred, opt.gap_extend_phred));
     mq.reset(new Mapq(opt.substitution_rate, ht.k, genome.total_length));
     sv_prior_log_prob = -opt.sv_prior_phred / 10.0 * LN_10;  // paired.rs:97
@@ -1785,6 +1872,7 @@ void orc_default_options(orc_options* o) {
   o->sv_prior_phred = 55.0;
   o->threads = 1;
   o->group_width = 16;
+  o->dense_min_buckets = 1ull << 24;
 }
 
 int orc_build_genome(const char* out_prefix, const char* species, const char* assembly, int nfiles,

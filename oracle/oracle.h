@@ -39,6 +39,7 @@ typedef struct {
   double sv_prior_phred;     // default 55
   int32_t threads;           // worker threads (0 = all cores)
   int32_t group_width;       // 16 or 8
+  uint64_t dense_min_buckets;  // .sthash tables with more buckets load as a direct-address map (default 2^24)
 } orc_options;
 
 // Reads as structure-of-arrays: concatenated sequence bytes and Phred

@@ -41,6 +41,7 @@ class Options(C.Structure):
         ("sv_prior_phred", C.c_double),
         ("threads", C.c_int32),
         ("group_width", C.c_int32),
+        ("dense_min_buckets", C.c_uint64),
     ]
 
 

@@ -83,7 +83,8 @@ class RankerReportC(C.Structure):
 
 class TuningC(C.Structure):
     _fields_ = [("autotune", C.c_int32), ("band_lanes", C.c_int32), ("length_bins", C.c_int32),
-                ("pair_graphs", C.c_int32), ("chosen_lanes", C.c_int32 * 3), ("tuned_ms", (C.c_float * 2) * 3)]
+                ("pair_graphs", C.c_int32), ("chosen_lanes", C.c_int32 * 3), ("tuned_ms", (C.c_float * 2) * 3),
+                ("wait_polls", C.c_uint32), ("ovf_slice_hits", C.c_uint32)]
 
 
 class InsertModelC(C.Structure):
@@ -164,6 +165,7 @@ def lib():
         L.pbw_ranker_import.argtypes = [vp, vp, u64]
         L.pbw_ranker_score.argtypes = [vp, vp, u64, vp]
         L.pbw_build_hash.argtypes = [cp, cp, u64, u64, u64, C.c_int32]
+        L.pbw_int32_peak.argtypes = [C.c_int32, vp, vp]
         if hasattr(L, "pbw_align_noalloc"):
             L.pbw_align_noalloc.argtypes = [u64, vp, vp, vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, u32, vp]
         _lib = L
@@ -419,7 +421,9 @@ class Mapper:
     def seed_batch(self, reads: Reads, hit_cap: int | None = None):
         """find_seed_hits per read: (hit_off, packed hits, read_pos, win_off, repeat_prob)."""
         n = reads.n
-        hit_cap = hit_cap or (4096 * max(n, 1))
+        # in-buffer reads hold at most 4096 hits each; over-capacity reads
+        # share the 16 M-hit overflow pool of a chunk
+        hit_cap = hit_cap or (4096 * max(n, 1) + (16 << 20) * (1 + n // 131072))
         hit_off = np.zeros(n + 1, np.uint64)
         hits = np.zeros(hit_cap, np.uint64)
         rpos = np.zeros(hit_cap, np.uint32)
@@ -457,9 +461,6 @@ class Mapper:
         rb = np.frombuffer(b"".join(reads) + b"\0", np.uint8)[:-1].copy()
         qb = np.frombuffer(b"".join(quals) + b"\0", np.uint8)[:-1].copy()
         fb = np.frombuffer(b"".join(refs) + b"\0", np.uint8)[:-1].copy()
-        for a in ("rb", "qb", "fb"):
-            if locals()[a].size == 0:
-                pass
         rb = rb if rb.size else np.zeros(1, np.uint8)
         qb = qb if qb.size else np.zeros(1, np.uint8)
         fb = fb if fb.size else np.zeros(1, np.uint8)
@@ -548,10 +549,12 @@ class Mapper:
         self._check(lib().pbw_get_tuning(self.h, C.byref(t)))
         return {"autotune": t.autotune, "band_lanes": t.band_lanes, "length_bins": t.length_bins,
                 "pair_graphs": t.pair_graphs, "chosen_lanes": list(t.chosen_lanes),
-                "tuned_ms": [list(r) for r in t.tuned_ms]}
+                "tuned_ms": [list(r) for r in t.tuned_ms], "wait_polls": t.wait_polls,
+                "ovf_slice_hits": t.ovf_slice_hits}
 
     def set_tuning(self, **kw):
-        """pbw_set_tuning: autotune, band_lanes (0, 8, 16), length_bins, pair_graphs."""
+        """pbw_set_tuning: autotune, band_lanes (0, 8, 16), length_bins, pair_graphs, wait_polls,
+        ovf_slice_hits."""
         t = TuningC()
         self._check(lib().pbw_get_tuning(self.h, C.byref(t)))
         for k, v in kw.items():

@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(WIN_THREADS, MINB) k_align_window(AlignArgs p,
   const size_t var_avail = (size_t)smem_total - win_fixed_bytes(p.lmax);
   unsigned char* slab = p.tb_global ? p.tb_global + p.tb_global_per_warp * blockIdx.x : nullptr;
   const unsigned int njobs = *p.n_jobs;
+  const unsigned int spin_limit = p.wait_polls ? p.wait_polls : WIN_SPIN_LIMIT;
   unsigned long long cells_acc = 0, jobs_acc = 0;
 
   while (true) {
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(WIN_THREADS, MINB) k_align_window(AlignArgs p,
             unsigned int spins = 0;
             while (s_pub[bin] < target) {
               if (s_abort) break;
-              if (++spins > WIN_SPIN_LIMIT) {
+              if (++spins > spin_limit) {
                 if (lane == 0) {
                   s_abort = 1;
                   atomicExch(p.err, 9);

@@ -432,6 +432,8 @@ int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t) {
   t->band_lanes = T.band_lanes;
   t->length_bins = T.length_bins;
   t->pair_graphs = T.pair_graphs;
+  t->wait_polls = T.wait_polls;
+  t->ovf_slice_hits = T.ovf_slice_hits;
   for (int c = 0; c < 3; c++) {
     t->chosen_lanes[c] = T.chosen[c];
     t->tuned_ms[c][0] = T.ms[c][0];
@@ -451,6 +453,8 @@ int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t) {
   T.band_lanes = t->band_lanes;
   T.length_bins = t->length_bins != 0;
   T.pair_graphs = t->pair_graphs != 0;
+  T.wait_polls = t->wait_polls;
+  T.ovf_slice_hits = t->ovf_slice_hits;
   for (int c = 0; c < 3; c++) {
     T.chosen[c] = 0;
     T.ms[c][0] = T.ms[c][1] = 0.f;

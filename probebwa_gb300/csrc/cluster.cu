@@ -334,16 +334,35 @@ __global__ void k_cluster(ClusterArgs p, uint32_t np_max) {
   }
 }
 
+// Reads with more hits than shared memory sorts (p.h_lo < H <= p.h_hi, both
+// above the shared-memory tier): hits in the per-read buffer, work arrays in
+// one global slab per block (p.scratch, slab_bytes each).
+__global__ void k_cluster_big(ClusterArgs p, uint32_t np_max, size_t slab_bytes) {
+  __shared__ unsigned long long wtmp64[32];
+  __shared__ uint32_t wtmp32[32];
+  __shared__ uint32_t sh_G, sh_C;
+  unsigned char* slab = p.scratch + (size_t)blockIdx.x * slab_bytes;
+  for (uint32_t r = blockIdx.x; r < p.nr; r += gridDim.x) {
+    const uint32_t H = p.hit_cnt[r];
+    if (p.overflow[r]) continue;
+    if (!(H > p.h_lo && H <= p.h_hi)) continue;
+    cluster_read(p, r, H, p.hits + (size_t)r * p.hcap, slab, np_max, wtmp32, wtmp64, sh_G, sh_C, false);
+  }
+}
+
 // Overflowed reads (list mode): hits in the pool, arrays in global scratch.
 __global__ void k_cluster_list(ClusterArgs p) {
   __shared__ unsigned long long wtmp64[32];
   __shared__ uint32_t wtmp32[32];
   __shared__ uint32_t sh_G, sh_C;
   const unsigned int n = *p.list_n;
+  const unsigned long long s_lo = (unsigned long long)p.slice * p.pool_slice;
+  if (s_lo >= *p.list_total) return;
   for (uint32_t w = blockIdx.x; w < n; w += gridDim.x) {
+    if (p.list_hoff[w] / p.pool_slice != p.slice) continue;
     const uint32_t r = p.list[w];
     const uint32_t H = p.need[r];
-    const unsigned long long off = p.list_hoff[w];
+    const unsigned long long off = p.list_hoff[w] - s_lo;
     uint32_t NP = next_pow2(H);
     cluster_read(p, r, H, p.hits_pool + off, p.scratch + 2 * off * 56, NP, wtmp32, wtmp64, sh_G, sh_C, true);
   }
@@ -357,6 +376,18 @@ void launch_cluster(const ClusterArgs& a, uint32_t hmax, int threads, cudaStream
   if (grid < 1) grid = 1;
   cudaFuncSetAttribute(k_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_cluster<<<grid, threads, sm, st>>>(a, np);
+}
+
+size_t cluster_big_slab_bytes(uint32_t hmax) {
+  uint32_t np = 1;
+  while (np < hmax) np <<= 1;
+  return ((size_t)np * 56 + 64 + 255) & ~(size_t)255;
+}
+
+void launch_cluster_big(const ClusterArgs& a, uint32_t hmax, int grid, cudaStream_t st) {
+  uint32_t np = 1;
+  while (np < hmax) np <<= 1;
+  k_cluster_big<<<grid, 1024, 0, st>>>(a, np, cluster_big_slab_bytes(hmax));
 }
 
 void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st) {

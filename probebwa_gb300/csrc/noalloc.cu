@@ -3,11 +3,13 @@
 // pbw_align_noalloc runs the window DP of align_window.cu with every piece of
 // scratch -- jobs, per-alignment outputs, queue counters, the CIGAR overflow
 // pool, the per-block slabs for windows too large for shared memory and the
-// parameter table -- inside one file-scope device array. Inputs and outputs are device memory owned by the caller.
-// Callers that are not allowed to call cudaMalloc (code running while a
-// stream is being captured into a CUDA graph, allocators that own all device
-// memory, real-time loops with a fixed memory budget) can call it; it calls no
-// cudaMalloc, cudaFree or allocating library routine.
+// parameter table -- inside one file-scope device array. Inputs and outputs
+// are device memory owned by the caller. It is for callers that must not call
+// cudaMalloc: a host application whose own allocator has reserved the GPU's
+// memory (a framework's caching allocator, a memory pool sized at start-up),
+// or a loop with a fixed device-memory budget that may not grow at run time.
+// It calls no cudaMalloc, cudaFree or allocating library routine, and it
+// synchronises the caller's stream before returning.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -23,7 +25,11 @@ constexpr uint64_t NA_MAX_PROBLEMS = 4096;
 constexpr int NA_MAX_READ = 256;
 constexpr int NA_MAX_REF = 2048;
 constexpr int NA_BLOCKS = 16;                 // window kernel blocks (8 warps each)
-constexpr uint64_t NA_POOL_OPS = NA_MAX_PROBLEMS * 64;
+// CIGARs longer than CIG_INLINE operations spill into the pool. Runs of M
+// and I consume at least one read base each and runs of D sit between them,
+// so a read of m bases has at most 2m + 1 operations: the pool holds that
+// for every problem of a full call.
+constexpr uint64_t NA_POOL_OPS = NA_MAX_PROBLEMS * (2 * NA_MAX_READ + 1);
 
 constexpr size_t na16(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t NA_SLAB = window_slab_bytes(NA_MAX_READ, NA_MAX_REF);
@@ -33,7 +39,7 @@ constexpr size_t NA_OFF_JOBS = na16(NA_OFF_CNT + 64);
 constexpr size_t NA_OFF_OUT = na16(NA_OFF_JOBS + NA_MAX_PROBLEMS * sizeof(AlnJob));
 constexpr size_t NA_OFF_POOL = na16(NA_OFF_OUT + NA_MAX_PROBLEMS * sizeof(AlnOut));
 constexpr size_t NA_OFF_SLAB = na16(NA_OFF_POOL + NA_POOL_OPS * 4);
-constexpr size_t NA_BYTES = na16(NA_OFF_SLAB + NA_SLAB * NA_BLOCKS);  // about 6 MB
+constexpr size_t NA_BYTES = na16(NA_OFF_SLAB + NA_SLAB * NA_BLOCKS);  // about 14 MB
 
 // The scratch. Every GPU that loads this library holds it until the process
 // exits. In host code the name is only a handle for cudaGetSymbolAddress.
@@ -128,8 +134,8 @@ extern "C" int pbw_align_noalloc(uint64_t n, const uint8_t* reads, const uint8_t
     return PBW_ERR_CUDA;
   }
   // First call on this device: find the scratch's device address and write
-  // its parameter table (mismatch penalties etc.). Must run outside stream
-  // capture.
+  // its parameter table (mismatch penalties etc.) with a synchronous copy.
+  // This first call should come before any stream capture.
   if (!g_scratch_ptr[dev]) {
     void* ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
@@ -203,6 +209,15 @@ extern "C" int pbw_align_noalloc(uint64_t n, const uint8_t* reads, const uint8_t
   if (err == 7) {
     g_noalloc_err = "pbw_align_noalloc: a CIGAR has more operations than cigar_stride";
     return PBW_ERR_CAPACITY;
+  }
+  if (err == 3) {
+    g_noalloc_err = "pbw_align_noalloc: the static CIGAR overflow pool (" + std::to_string(NA_POOL_OPS) +
+                    " operations) is full";
+    return PBW_ERR_CAPACITY;
+  }
+  if (err == 9) {
+    g_noalloc_err = "pbw_align_noalloc: a wavefront wait of the window DP gave up; results discarded";
+    return PBW_ERR_DEVICE;
   }
   if (err) {
     g_noalloc_err = "pbw_align_noalloc: device error " + std::to_string(err);

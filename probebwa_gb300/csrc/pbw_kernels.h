@@ -25,7 +25,8 @@ struct SeedArgs {
   unsigned int* n_overflow; // 1
   uint8_t* rep;             // nr * wcap: 0 none, 1 neighbour repetitive, 2 exact repetitive
   uint32_t wcap;
-  uint16_t* hit_rpos;       // optional nr * hcap read positions (parity tests)
+  uint16_t* hit_rpos;       // optional nr * hcap read positions (stage entry point)
+  uint16_t* hit_rpos_pool;  // optional, list mode: read positions beside hits_pool
   uint16_t* hit_info;       // optional nr * hcap: read position | log2 exact bucket << 10 | neighbour << 15
   unsigned long long* counters;  // probes, entries, hits
   // overflow handling: reads with more than hcap hits are queued with their
@@ -35,8 +36,13 @@ struct SeedArgs {
   unsigned int* n_ovf;      // queue length
   const uint32_t* list;     // list mode: work item w is read list[w]
   const unsigned int* list_n;
-  const unsigned long long* list_hoff;  // hits pool offset of item w
+  const unsigned long long* list_hoff;  // exclusive prefix of the listed reads' hit counts
   unsigned long long* hits_pool;
+  // the pool holds one slice at a time: item w belongs to slice
+  // list_hoff[w] / pool_slice and sits at list_hoff[w] - slice * pool_slice
+  unsigned long long pool_slice;
+  uint32_t slice;
+  const unsigned long long* list_total;  // all listed hits (slices past it exit at once)
 };
 __host__ __device__ inline size_t seed_smem_per_warp(int lmax) {
   int W = lmax - KMER + 1 > 0 ? lmax - KMER + 1 : 1;
@@ -74,6 +80,9 @@ struct ClusterArgs {
   const unsigned long long* hits_pool;
   const uint32_t* need;
   unsigned char* scratch;   // 2 * 56 bytes per pooled hit
+  unsigned long long pool_slice;  // as SeedArgs: the slice of the pool in use
+  uint32_t slice;
+  const unsigned long long* list_total;
   // optional, for the candidate ranker: sorted hits written back in place,
   // their emission slots, and each kept candidate's range in that order
   unsigned long long* sorted_hits;  // nr * hcap (the hits array itself)
@@ -83,10 +92,18 @@ struct ClusterArgs {
 size_t cluster_smem(uint32_t hmax, int threads);
 void launch_cluster(const ClusterArgs& a, uint32_t hmax, int threads, cudaStream_t st);
 void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st);
+// Reads of h_lo < H <= h_hi hits (beyond the shared-memory tiers) from the
+// per-read buffer; a.scratch holds grid slabs of cluster_big_slab_bytes(h_hi).
+size_t cluster_big_slab_bytes(uint32_t hmax);
+void launch_cluster_big(const ClusterArgs& a, uint32_t hmax, int grid, cudaStream_t st);
 void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st);
+// Exclusive offsets of the listed (over-capacity) reads' hit counts, their
+// total, and the list length for the list-mode passes; a read needing more
+// than one slice (pool_slice hits), or a total beyond max_slices slices, is
+// error 5 and empties the list.
 void launch_ovf_offsets(const uint32_t* list, const unsigned int* list_n, const uint32_t* need,
-                        unsigned long long* hoff, unsigned long long pool_cap, int* err, unsigned int* list_n_out,
-                        cudaStream_t st);
+                        unsigned long long* hoff, unsigned long long* total, unsigned long long pool_slice,
+                        uint32_t max_slices, int* err, unsigned int* list_n_out, cudaStream_t st);
 
 // ---- K3 alignment ----
 // One alignment problem: query = read (forward) or its reverse complement,
@@ -144,6 +161,7 @@ struct AlignArgs {
   size_t tb_global_per_warp;  // K3w: bytes of one block's slab
   unsigned long long* counters;  // jobs, cells
   int* err;
+  uint32_t wait_polls;      // K3w: polls before a wavefront wait gives up (error 9); 0 = WIN_SPIN_LIMIT
 };
 // K3b, band <= band_max <= 31; grid sized from the shared memory per warp.
 // AlignArgs::tb_global must hold band_tb_slab_bytes(lmax, nmax, num_sms,

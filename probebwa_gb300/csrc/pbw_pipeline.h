@@ -100,6 +100,7 @@ struct pbw_handle {
   pbw::DevBuf<uint32_t> d_need, d_ovf_list;
   pbw::DevBuf<unsigned long long> d_list_hoff, d_hits_pool;
   pbw::DevBuf<unsigned char> d_cl_scratch;
+  pbw::DevBuf<unsigned char> d_cl_big;  // K2 global slabs for reads of 4096-16384 hits
   // outputs of a call
   pbw::DevBuf<int32_t> o_contig, o_mate_contig, o_as, o_nm, o_best;
   pbw::DevBuf<unsigned long long> o_pos, o_mate_pos;
@@ -147,6 +148,8 @@ struct pbw_handle {
     int pair_graphs = 1;    // one CUDA graph launch per batch of pairs
     int chosen[3] = {0, 0, 0};  // lanes per read-length class (<= 128, <= 256, longer); 0: not tuned
     float ms[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    uint32_t wait_polls = 0;  // window-DP wavefront waits: polls before giving up (0 = the kernel's default)
+    uint32_t ovf_slice_hits = 0;  // over-capacity reads: hits per pool slice (0 = the default, 16 M)
   } tune;
   int call_lmin = 0;        // shortest read of the current call
   pbw::DevBuf<pbw::AlnJob> d_jobs_b;

@@ -56,9 +56,26 @@ int pipeline_init(pbw_handle* h) {
   return PBW_OK;
 }
 
-// Seed hits pooled for reads that overflow the per-read capacity (per
-// chunk); their clustering scratch takes 112 bytes per pooled hit.
-constexpr size_t OVF_POOL_HITS = 16ull << 20;
+// Seed hits of reads that overflow the per-read capacity go to a pool, one
+// slice of OVF_SLICE_HITS at a time: the reads whose exclusive offset falls
+// in slice s are seeded again and clustered in the s-th list-mode pass. A
+// read reaches at most one slice past its start, so the pool holds two
+// slices; their clustering scratch takes 112 bytes per pooled hit. A chunk's
+// over-capacity reads may hold up to OVF_MAX_SLICES slices of hits.
+constexpr size_t OVF_SLICE_HITS = 16ull << 20;
+constexpr size_t OVF_POOL_HITS = 2 * OVF_SLICE_HITS;
+constexpr uint32_t OVF_MAX_SLICES = 16;
+constexpr uint32_t CL_SMEM_HITS = 4096;  // the largest read K2 sorts in shared memory
+static int cl_big_grid(const pbw_handle* h) { return h->num_sms * 2; }
+// The slice in use: OVF_SLICE_HITS unless pbw_set_tuning lowered it (the
+// total the chunk may hold stays OVF_MAX_SLICES * OVF_SLICE_HITS).
+static uint64_t ovf_slice_hits(const pbw_handle* h) {
+  const uint64_t s = h->tune.ovf_slice_hits;
+  return s && s < OVF_SLICE_HITS ? s : OVF_SLICE_HITS;
+}
+static uint32_t ovf_max_slices(const pbw_handle* h) {
+  return (uint32_t)((OVF_MAX_SLICES * OVF_SLICE_HITS) / ovf_slice_hits(h));
+}
 
 // Scratch sizing for one chunk.
 struct ChunkCfg {
@@ -75,7 +92,11 @@ static ChunkCfg chunk_cfg(pbw_handle* h, uint64_t n, int lmax) {
   c.ch = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(n, 1), h->opt.chunk_reads);
   c.lmax = std::max(lmax, 1);
   c.lmin = std::min(std::max(h->call_lmin, 0), c.lmax);
-  c.hcap = 4096;
+  // per-read hit buffer: 4096 hits sort in shared memory; long reads on a
+  // repeat-rich genome have more (a 3.1 Gbp genome with 45% interspersed
+  // repeats gives 250-base reads ~4,100 hits on average, 11,600 at the 99th
+  // percentile), sorted in global slabs up to 16384, the rest in the pool
+  c.hcap = c.lmax > 160 ? 16384 : 4096;
   c.wcap = (uint32_t)std::max(c.lmax - KMER + 1, 1);
   const uint64_t rp = std::max<uint64_t>(h->opt.max_indel_len, 10);
   c.nmax = (int)(c.lmax + 10 + rp);
@@ -110,6 +131,7 @@ static int ensure_chunk(pbw_handle* h, const ChunkCfg& c) {
   TRY(grow(h, h->d_list_hoff, c.ch));
   TRY(grow(h, h->d_hits_pool, OVF_POOL_HITS));
   TRY(grow(h, h->d_cl_scratch, OVF_POOL_HITS * 112));
+  if (c.hcap > CL_SMEM_HITS) TRY(grow(h, h->d_cl_big, cluster_big_slab_bytes(c.hcap) * (size_t)cl_big_grid(h)));
   if (h->opt.max_indel_len > 31) TRY(ensure_window_slab(h, c.lmax, c.nmax, window_grid(h)));
   else TRY(grow(h, h->d_tb_global, band_tb_slab_bytes(c.lmax, c.nmax, h->num_sms, (int)h->opt.max_indel_len)));
   return PBW_OK;
@@ -183,16 +205,13 @@ static uint8_t* rank_label(pbw_handle* h, int mate, uint32_t r0) {
   return h->rk.collect ? h->rk.c_label.p + (size_t)mate * h->rk.c_slots + (size_t)r0 * MAX_CAND : nullptr;
 }
 
-// K1 -> K2 for reads [r0, r0+nr) of one read set; with feat, also the
-// ranker's hit-level candidate features. Events ev[0..2] mark the start and
-// the seed / cluster boundaries.
-static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
-                        const uint64_t* offs, uint32_t r0, uint32_t nr, const MateBufs& mb, cudaEvent_t* ev,
-                        float* feat) {
+// K1 for reads [r0, r0+nr): the per-read pass, then the pool offsets of the
+// reads over the per-read capacity (their list-mode passes run slice by
+// slice with the clustering, ovf_slice).
+static int seed_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint64_t* offs, uint32_t r0,
+                      uint32_t nr, uint8_t* rep, bool ranker_info, uint16_t* hit_rpos) {
   cudaStream_t st = h->st;
   unsigned int* c32 = h->d_cnt32.p;
-  CK(cudaMemsetAsync(mb.n_cand, 0, nr * sizeof(uint32_t), st));
-  CK(cudaEventRecord(ev[0], st));
   SeedArgs sa{};
   sa.G = h->G;
   sa.idx = h->I;
@@ -206,10 +225,10 @@ static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases
   sa.hit_cnt = h->d_hit_cnt.p;
   sa.overflow = h->d_overflow.p;
   sa.n_overflow = c32 + 3;
-  sa.rep = mb.rep;
+  sa.rep = rep;
   sa.wcap = cfg.wcap;
-  sa.hit_rpos = nullptr;
-  sa.hit_info = feat ? h->rk.d_hit_info.p : nullptr;
+  sa.hit_rpos = hit_rpos;  // optional: each hit's read position (stage entry point)
+  sa.hit_info = ranker_info ? h->rk.d_hit_info.p : nullptr;
   sa.counters = h->d_cnt64.p;
   sa.need = h->d_need.p;
   sa.ovf_list = h->d_ovf_list.p;
@@ -220,21 +239,69 @@ static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases
     int bps = (int)std::max<size_t>(1, std::min<size_t>(8, (228 * 1024) / std::max<size_t>(sm, 1)));
     launch_seed(sa, h->num_sms * bps, st);
   }
-  // reads over capacity: exact-size pool slots, seeded again in list mode
-  launch_ovf_offsets(h->d_ovf_list.p, c32 + 6, h->d_need.p, h->d_list_hoff.p, OVF_POOL_HITS, h->d_err.p, c32 + 7, st);
-  {
-    SeedArgs sl = sa;
-    sl.list = h->d_ovf_list.p;
-    sl.list_n = c32 + 7;
-    sl.list_hoff = h->d_list_hoff.p;
-    sl.hits_pool = h->d_hits_pool.p;
-    sl.ovf_list = nullptr;
-    sl.counters = nullptr;
-    launch_seed_list(sl, h->num_sms * 2, st);
-  }
+  // reads over capacity: exact-size pool offsets
+  launch_ovf_offsets(h->d_ovf_list.p, c32 + 6, h->d_need.p, h->d_list_hoff.p, h->d_cnt64.p + 8, ovf_slice_hits(h),
+                     ovf_max_slices(h), h->d_err.p, c32 + 7, st);
   h->stats.kernel_launches += 2;
   CK(cudaGetLastError());
-  CK(cudaEventRecord(ev[1], st));
+  return PBW_OK;
+}
+
+// Slice s of the over-capacity reads: seeded again in list mode into the
+// pool (with their read positions when rpos_pool is set) and, when ca is
+// given, clustered from it. Slices past the listed hits exit at once.
+static int ovf_slice(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint64_t* offs, uint32_t r0,
+                     uint32_t nr, uint8_t* rep, uint32_t s, uint16_t* rpos_pool, const ClusterArgs* ca) {
+  cudaStream_t st = h->st;
+  unsigned int* c32 = h->d_cnt32.p;
+  SeedArgs sl{};
+  sl.G = h->G;
+  sl.idx = h->I;
+  sl.bases = bases;
+  sl.offs = offs;
+  sl.r0 = r0;
+  sl.nr = nr;
+  sl.lmax = cfg.lmax;
+  sl.hcap = cfg.hcap;
+  sl.rep = rep;
+  sl.wcap = cfg.wcap;
+  sl.hit_rpos_pool = rpos_pool;
+  sl.need = h->d_need.p;
+  sl.list = h->d_ovf_list.p;
+  sl.list_n = c32 + 7;
+  sl.list_hoff = h->d_list_hoff.p;
+  sl.hits_pool = h->d_hits_pool.p;
+  sl.pool_slice = ovf_slice_hits(h);
+  sl.slice = s;
+  sl.list_total = h->d_cnt64.p + 8;
+  launch_seed_list(sl, h->num_sms * 2, st);
+  h->stats.kernel_launches += 1;
+  if (ca) {
+    ClusterArgs cl = *ca;
+    cl.list = h->d_ovf_list.p;
+    cl.list_n = c32 + 7;
+    cl.list_hoff = h->d_list_hoff.p;
+    cl.hits_pool = h->d_hits_pool.p;
+    cl.need = h->d_need.p;
+    cl.scratch = h->d_cl_scratch.p;
+    cl.pool_slice = ovf_slice_hits(h);
+    cl.slice = s;
+    cl.list_total = h->d_cnt64.p + 8;
+    launch_cluster_list(cl, h->num_sms, st);
+    h->stats.kernel_launches += 1;
+  }
+  CK(cudaGetLastError());
+  return PBW_OK;
+}
+
+// K2 after seed_phase: the first max_out candidates of each read into
+// cand (nr * max_out), the full count into total_cand; the over-capacity
+// reads are seeded into the pool and clustered slice by slice.
+static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint64_t* offs,
+                         uint32_t r0, uint32_t nr, uint8_t* rep, Cand* cand, uint32_t* n_cand, uint32_t* total_cand,
+                         uint32_t max_out, bool ranker_info) {
+  cudaStream_t st = h->st;
+  unsigned int* c32 = h->d_cnt32.p;
   ClusterArgs ca{};
   ca.hits = h->d_hits.p;
   ca.hit_cnt = h->d_hit_cnt.p;
@@ -244,12 +311,12 @@ static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases
   ca.r0 = r0;
   ca.nr = nr;
   ca.group_width = h->opt.group_width;
-  ca.max_out = MAX_CAND;
-  ca.cand = mb.cand;
-  ca.n_cand = mb.n_cand;
-  ca.total_cand = h->d_total_cand.p;
+  ca.max_out = max_out;
+  ca.cand = cand;
+  ca.n_cand = n_cand;
+  ca.total_cand = total_cand;
   ca.err = h->d_err.p;
-  if (feat) {
+  if (ranker_info) {
     ca.sorted_hits = h->d_hits.p;
     ca.hit_src = h->rk.d_hit_src.p;
     ca.cand_span = h->rk.d_span.p;
@@ -258,16 +325,37 @@ static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases
   ca.h_hi = 512;
   launch_cluster(ca, 512, 64, st);
   ca.h_lo = 512;
-  ca.h_hi = cfg.hcap;
-  launch_cluster(ca, cfg.hcap, 256, st);
-  ca.list = h->d_ovf_list.p;
-  ca.list_n = c32 + 7;
-  ca.list_hoff = h->d_list_hoff.p;
-  ca.hits_pool = h->d_hits_pool.p;
-  ca.need = h->d_need.p;
-  ca.scratch = h->d_cl_scratch.p;
-  launch_cluster_list(ca, h->num_sms, st);
-  h->stats.kernel_launches += 1;
+  ca.h_hi = std::min<uint32_t>(cfg.hcap, CL_SMEM_HITS);
+  launch_cluster(ca, ca.h_hi, 256, st);
+  h->stats.kernel_launches += 2;
+  if (cfg.hcap > CL_SMEM_HITS) {
+    ClusterArgs cb = ca;
+    cb.h_lo = CL_SMEM_HITS;
+    cb.h_hi = cfg.hcap;
+    cb.scratch = h->d_cl_big.p;
+    launch_cluster_big(cb, cfg.hcap, cl_big_grid(h), st);
+    h->stats.kernel_launches += 1;
+  }
+  (void)c32;
+  const uint32_t ns = ovf_max_slices(h);
+  for (uint32_t s = 0; s < ns; s++) TRY(ovf_slice(h, cfg, bases, offs, r0, nr, rep, s, nullptr, &ca));
+  CK(cudaGetLastError());
+  return PBW_OK;
+}
+
+// K1 -> K2 for reads [r0, r0+nr) of one read set; with feat, also the
+// ranker's hit-level candidate features. Events ev[0..2] mark the start and
+// the seed / cluster boundaries.
+static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
+                        const uint64_t* offs, uint32_t r0, uint32_t nr, const MateBufs& mb, cudaEvent_t* ev,
+                        float* feat) {
+  cudaStream_t st = h->st;
+  CK(cudaMemsetAsync(mb.n_cand, 0, nr * sizeof(uint32_t), st));
+  CK(cudaEventRecord(ev[0], st));
+  TRY(seed_phase(h, cfg, bases, offs, r0, nr, mb.rep, feat != nullptr, nullptr));
+  CK(cudaEventRecord(ev[1], st));
+  TRY(cluster_phase(h, cfg, bases, offs, r0, nr, mb.rep, mb.cand, mb.n_cand, h->d_total_cand.p, MAX_CAND,
+                    feat != nullptr));
   if (feat) {
     RankFeatArgs fa{};
     fa.hits = h->d_hits.p;
@@ -419,6 +507,7 @@ static int align_candidates(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* b
   aa.tb_global_per_warp = 0;
   aa.counters = h->d_cnt64.p + 3;
   aa.err = h->d_err.p;
+  aa.wait_polls = h->tune.wait_polls;
   if (h->tune.length_bins && cfg.lmin < cfg.lmax) {
     // mixed read lengths: the work queue in length bins, longest first
     launch_job_bins(h->d_jobs.p, c32 + 0, offs, h->d_bins.p, h->d_jobs_b.p, h->num_sms * 4, st);
@@ -519,9 +608,20 @@ static int check_device_errors(pbw_handle* h) {
     return PBW_ERR_LIMIT;
   }
   if (err == 5) {
-    h->err = "seed hits of over-capacity reads exceed the overflow pool";
+    h->err = "seed hits of a chunk's over-capacity reads exceed the overflow pool (16 slices of 16 M hits; "
+             "one read at most 16 M hits)";
     CK(cudaMemset(h->d_err.p, 0, 4));
     return PBW_ERR_LIMIT;
+  }
+  if (err == 3) {
+    h->err = "the CIGAR overflow pool of a chunk is full (alignments with very many CIGAR operations)";
+    CK(cudaMemset(h->d_err.p, 0, 4));
+    return PBW_ERR_CAPACITY;
+  }
+  if (err == 9) {
+    h->err = "a window-DP wavefront wait ran out of polls before its producer published (results discarded)";
+    CK(cudaMemset(h->d_err.p, 0, 4));
+    return PBW_ERR_DEVICE;
   }
   if (err) {
     h->err = "device kernel reported internal error " + std::to_string(err);
@@ -874,6 +974,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, wide_n);
     aa.counters = h->d_cnt64.p + 5;  // cross-alignment jobs and cells, apart from the seeded DP's
     aa.err = h->d_err.p;
+    aa.wait_polls = h->tune.wait_polls;
     // One batch: decide -> cross-alignment DP -> statistics -> resolve, its
     // observations to the host, the fold there (the model of the next batch).
     // With pair_graphs the device side is captured once per super-chunk as a
@@ -1213,6 +1314,7 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
   aa.ref_bytes = h->d_bases2.p;
   aa.counters = h->d_cnt64.p + 3;
   aa.err = h->d_err.p;
+  aa.wait_polls = h->tune.wait_polls;
   CK(cudaMemset(h->d_cnt32.p, 0, 16 * 4));
   if (!js.empty()) {
     CK(cudaMemcpy(h->d_jobs.p, js.data(), js.size() * sizeof(AlnJob), cudaMemcpyHostToDevice));
@@ -1253,7 +1355,19 @@ int pbw_align_batch(pbw_handle* h, uint64_t n, const uint8_t* reads, const uint8
   }
   int err = 0;
   CK(cudaMemcpy(&err, h->d_err.p, 4, cudaMemcpyDeviceToHost));
-  if (err) { h->err = "align kernel error " + std::to_string(err); return PBW_ERR_DEVICE; }
+  if (err) {
+    CK(cudaMemset(h->d_err.p, 0, 4));
+    if (err == 3) {
+      h->err = "the CIGAR overflow pool is full (alignments with very many CIGAR operations)";
+      return PBW_ERR_CAPACITY;
+    }
+    if (err == 9) {
+      h->err = "a window-DP wavefront wait ran out of polls before its producer published (results discarded)";
+      return PBW_ERR_DEVICE;
+    }
+    h->err = "align kernel error " + std::to_string(err);
+    return PBW_ERR_DEVICE;
+  }
   std::vector<AlnOut> outs(n);
   CK(cudaMemcpy(outs.data(), h->d_aln.p, n * sizeof(AlnOut), cudaMemcpyDeviceToHost));
   unsigned int pool_used = 0;
@@ -1372,74 +1486,115 @@ int pbw_mapq_batch(pbw_handle* h, const pbw_reads* reads, const uint64_t* lk_off
 
 int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uint64_t* hits, uint32_t* hit_read_pos,
                    uint64_t hit_cap, uint64_t* win_off, double* repeat_prob, uint64_t win_cap) {
-  if (!h || !reads) return PBW_ERR_ARG;
+  if (!h || !reads || !hit_off || !win_off) return PBW_ERR_ARG;
   cudaSetDevice(h->device);
   uint64_t total;
   int lmax;
   TRY(validate_reads(h, reads, total, lmax));
   const uint64_t n = reads->n;
-  if (n == 0) { hit_off[0] = 0; win_off[0] = 0; return PBW_OK; }
+  hit_off[0] = 0;
+  win_off[0] = 0;
+  if (n == 0) return PBW_OK;
   TRY(upload_reads(h, reads, total, h->d_bases, h->d_quals, h->d_offs));
   ChunkCfg cfg = chunk_cfg(h, n, lmax);
-  cfg.ch = (uint32_t)n;
-  TRY(grow(h, h->d_hits, (size_t)n * cfg.hcap));
-  TRY(grow(h, h->d_hit_rpos, (size_t)n * cfg.hcap));
-  TRY(grow(h, h->d_hit_cnt, n));
-  TRY(grow(h, h->d_overflow, n));
-  TRY(grow(h, h->d_rep, (size_t)n * cfg.wcap));
+  TRY(ensure_chunk(h, cfg));
+  TRY(grow(h, h->d_hit_rpos, (size_t)cfg.ch * cfg.hcap));
+  DevBuf<uint16_t> rpos_pool;
+  TRY(grow(h, rpos_pool, OVF_POOL_HITS));
   CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * 4, h->st));
-  SeedArgs sa{};
-  sa.G = h->G;
-  sa.idx = h->I;
-  sa.bases = h->d_bases.p;
-  sa.offs = h->d_offs.p;
-  sa.r0 = 0;
-  sa.nr = (uint32_t)n;
-  sa.lmax = cfg.lmax;
-  sa.hits = h->d_hits.p;
-  sa.hcap = cfg.hcap;
-  sa.hit_cnt = h->d_hit_cnt.p;
-  sa.overflow = h->d_overflow.p;
-  sa.n_overflow = h->d_cnt32.p + 3;
-  sa.rep = h->d_rep.p;
-  sa.wcap = cfg.wcap;
-  sa.hit_rpos = h->d_hit_rpos.p;
-  sa.counters = nullptr;
-  launch_seed(sa, h->num_sms * 4, h->st);
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(h->st));
-  TRY(check_device_errors(h));
-  std::vector<uint32_t> cnt(n);
-  std::vector<unsigned long long> hw((size_t)n * cfg.hcap);
-  std::vector<uint16_t> rp((size_t)n * cfg.hcap);
-  std::vector<uint8_t> rep((size_t)n * cfg.wcap);
-  CK(cudaMemcpy(cnt.data(), h->d_hit_cnt.p, n * 4, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(hw.data(), h->d_hits.p, hw.size() * 8, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(rp.data(), h->d_hit_rpos.p, rp.size() * 2, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(rep.data(), h->d_rep.p, rep.size(), cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> cnt, need, ovf;
+  std::vector<uint8_t> over, rep;
+  std::vector<unsigned long long> hw, hoff, pool;
+  std::vector<uint16_t> rp, prp;
   uint64_t ho = 0, wo = 0;
-  for (uint64_t r = 0; r < n; r++) {
-    hit_off[r] = ho;
-    win_off[r] = wo;
-    const uint64_t L = reads->offsets[r + 1] - reads->offsets[r];
-    for (uint32_t k = 0; k < cnt[r]; k++) {
-      if (ho >= hit_cap) { h->err = "hit capacity"; return PBW_ERR_CAPACITY; }
-      unsigned long long w = hw[(size_t)r * cfg.hcap + k];
-      uint32_t gk = (uint32_t)(w >> 40);
-      long long diag = (long long)(w & ((1ull << 40) - 1)) - (long long)DIAG_BIAS;
-      uint32_t rpos = rp[(size_t)r * cfg.hcap + k];
-      bool rev = gk & 1u;
-      unsigned long long pos = rev ? (unsigned long long)(diag - rpos) : (unsigned long long)(diag + rpos);
-      hits[ho] = ((unsigned long long)(rev ? 1 : 0) << 63) | ((unsigned long long)(gk >> 1) << 40) | pos;
-      hit_read_pos[ho] = rpos;
-      ho++;
+  for (uint64_t r0 = 0; r0 < n; r0 += cfg.ch) {
+    const uint32_t nr = (uint32_t)std::min<uint64_t>(cfg.ch, n - r0);
+    TRY(seed_phase(h, cfg, h->d_bases.p, h->d_offs.p, (uint32_t)r0, nr, h->d_rep.p, false,
+                   h->d_hit_rpos.p));
+    CK(cudaStreamSynchronize(h->st));
+    TRY(check_device_errors(h));
+    cnt.resize(nr);
+    over.resize(nr);
+    need.resize(nr);
+    hw.resize((size_t)nr * cfg.hcap);
+    rp.resize((size_t)nr * cfg.hcap);
+    rep.resize((size_t)nr * cfg.wcap);
+    unsigned int c32[8];
+    CK(cudaMemcpy(c32, h->d_cnt32.p, sizeof(c32), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cnt.data(), h->d_hit_cnt.p, nr * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(over.data(), h->d_overflow.p, nr, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(need.data(), h->d_need.p, nr * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hw.data(), h->d_hits.p, hw.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(rp.data(), h->d_hit_rpos.p, rp.size() * 2, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(rep.data(), h->d_rep.p, rep.size(), cudaMemcpyDeviceToHost));
+    // over-capacity reads: their hits sit in the pool at list_hoff[item]
+    const uint32_t n_list = c32[7];
+    ovf.resize(n_list);
+    hoff.resize(n_list);
+    uint64_t pool_n = 0;
+    if (n_list) {
+      CK(cudaMemcpy(ovf.data(), h->d_ovf_list.p, n_list * 4, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(hoff.data(), h->d_list_hoff.p, n_list * 8, cudaMemcpyDeviceToHost));
+      for (uint32_t i = 0; i < n_list; i++) pool_n = std::max<uint64_t>(pool_n, hoff[i] + need[ovf[i]]);
+      pool.resize(pool_n);
+      prp.resize(pool_n);
+      // the pool holds one slice at a time: each slice's hits come back
+      // before the next list-mode pass reuses it
+      const uint64_t S = ovf_slice_hits(h);
+      for (uint32_t s = 0; (uint64_t)s * S < pool_n; s++) {
+        TRY(ovf_slice(h, cfg, h->d_bases.p, h->d_offs.p, (uint32_t)r0, nr, h->d_rep.p, s, rpos_pool.p, nullptr));
+        CK(cudaStreamSynchronize(h->st));
+        TRY(check_device_errors(h));
+        uint64_t lo = ~0ull, hi = 0;
+        for (uint32_t i = 0; i < n_list; i++) {
+          if (hoff[i] / S != s) continue;
+          lo = std::min<uint64_t>(lo, hoff[i]);
+          hi = std::max<uint64_t>(hi, hoff[i] + need[ovf[i]]);
+        }
+        if (hi <= lo) continue;
+        const uint64_t base = (uint64_t)s * S;
+        CK(cudaMemcpy(pool.data() + lo, h->d_hits_pool.p + (lo - base), (hi - lo) * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(prp.data() + lo, rpos_pool.p + (lo - base), (hi - lo) * 2, cudaMemcpyDeviceToHost));
+      }
     }
-    const uint64_t nw = L >= 15 ? L - 14 : 0;
-    for (uint64_t w = 0; w < nw; w++) {
-      if (wo >= win_cap) { h->err = "window capacity"; return PBW_ERR_CAPACITY; }
-      uint8_t c = rep[(size_t)r * cfg.wcap + w];
-      const uint8_t q = reads->quals[reads->offsets[r] + w];
-      repeat_prob[wo++] = c == 2 ? 1.0 : (c == 1 ? h->tab_host.nrp[q] : 0.0);
+    std::vector<int64_t> item_of(nr, -1);
+    for (uint32_t i = 0; i < n_list; i++) item_of[ovf[i]] = i;
+    for (uint32_t r = 0; r < nr; r++) {
+      const uint64_t rg = r0 + r;
+      hit_off[rg] = ho;
+      win_off[rg] = wo;
+      const uint64_t L = reads->offsets[rg + 1] - reads->offsets[rg];
+      const unsigned long long* src = hw.data() + (size_t)r * cfg.hcap;
+      const uint16_t* src_rp = rp.data() + (size_t)r * cfg.hcap;
+      uint32_t nh = cnt[r];
+      if (over[r]) {
+        if (item_of[r] < 0) {
+          h->err = "over-capacity read missing from the overflow list";
+          return PBW_ERR_DEVICE;
+        }
+        src = pool.data() + hoff[item_of[r]];
+        src_rp = prp.data() + hoff[item_of[r]];
+        nh = need[r];
+      }
+      for (uint32_t k = 0; k < nh; k++) {
+        if (ho >= hit_cap) { h->err = "hit capacity"; return PBW_ERR_CAPACITY; }
+        const unsigned long long w = src[k];
+        const uint32_t gk = (uint32_t)(w >> 40);
+        const long long diag = (long long)(w & ((1ull << 40) - 1)) - (long long)DIAG_BIAS;
+        const uint32_t rpos = src_rp[k];
+        const bool rev = gk & 1u;
+        const unsigned long long pos = rev ? (unsigned long long)(diag - rpos) : (unsigned long long)(diag + rpos);
+        hits[ho] = ((unsigned long long)(rev ? 1 : 0) << 63) | ((unsigned long long)(gk >> 1) << 40) | pos;
+        hit_read_pos[ho] = rpos;
+        ho++;
+      }
+      const uint64_t nw = L >= 15 ? L - 14 : 0;
+      for (uint64_t w = 0; w < nw; w++) {
+        if (wo >= win_cap) { h->err = "window capacity"; return PBW_ERR_CAPACITY; }
+        const uint8_t c = rep[(size_t)r * cfg.wcap + w];
+        const uint8_t q = reads->quals[reads->offsets[rg] + w];
+        repeat_prob[wo++] = c == 2 ? 1.0 : (c == 1 ? h->tab_host.nrp[q] : 0.0);
+      }
     }
   }
   hit_off[n] = ho;
@@ -1450,7 +1605,7 @@ int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uin
 int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_read, uint32_t* n_cand,
                       uint32_t* total_cand, uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,
                       double* cand_score) {
-  if (!h || !reads) return PBW_ERR_ARG;
+  if (!h || !reads || max_per_read == 0) return PBW_ERR_ARG;
   cudaSetDevice(h->device);
   uint64_t total;
   int lmax;
@@ -1459,67 +1614,34 @@ int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_re
   if (n == 0) return PBW_OK;
   TRY(upload_reads(h, reads, total, h->d_bases, h->d_quals, h->d_offs));
   ChunkCfg cfg = chunk_cfg(h, n, lmax);
-  cfg.ch = (uint32_t)n;
-  TRY(grow(h, h->d_hits, (size_t)n * cfg.hcap));
-  TRY(grow(h, h->d_hit_cnt, n));
-  TRY(grow(h, h->d_overflow, n));
-  TRY(grow(h, h->d_rep, (size_t)n * cfg.wcap));
+  TRY(ensure_chunk(h, cfg));
   DevBuf<Cand> dc;
   DevBuf<uint32_t> dn, dt;
-  TRY(grow(h, dc, (size_t)n * max_per_read));
-  TRY(grow(h, dn, n));
-  TRY(grow(h, dt, n));
+  TRY(grow(h, dc, (size_t)cfg.ch * max_per_read));
+  TRY(grow(h, dn, cfg.ch));
+  TRY(grow(h, dt, cfg.ch));
   CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * 4, h->st));
-  CK(cudaMemsetAsync(dn.p, 0, n * 4, h->st));
-  CK(cudaMemsetAsync(dt.p, 0, n * 4, h->st));
-  SeedArgs sa{};
-  sa.G = h->G;
-  sa.idx = h->I;
-  sa.bases = h->d_bases.p;
-  sa.offs = h->d_offs.p;
-  sa.r0 = 0;
-  sa.nr = (uint32_t)n;
-  sa.lmax = cfg.lmax;
-  sa.hits = h->d_hits.p;
-  sa.hcap = cfg.hcap;
-  sa.hit_cnt = h->d_hit_cnt.p;
-  sa.overflow = h->d_overflow.p;
-  sa.n_overflow = h->d_cnt32.p + 3;
-  sa.rep = h->d_rep.p;
-  sa.wcap = cfg.wcap;
-  launch_seed(sa, h->num_sms * 4, h->st);
-  ClusterArgs ca{};
-  ca.hits = h->d_hits.p;
-  ca.hit_cnt = h->d_hit_cnt.p;
-  ca.overflow = h->d_overflow.p;
-  ca.hcap = cfg.hcap;
-  ca.offs = h->d_offs.p;
-  ca.r0 = 0;
-  ca.nr = (uint32_t)n;
-  ca.group_width = h->opt.group_width;
-  ca.max_out = max_per_read;
-  ca.cand = dc.p;
-  ca.n_cand = dn.p;
-  ca.total_cand = dt.p;
-  ca.err = h->d_err.p;
-  ca.h_lo = 0;
-  ca.h_hi = 512;
-  launch_cluster(ca, 512, 64, h->st);
-  ca.h_lo = 512;
-  ca.h_hi = cfg.hcap;
-  launch_cluster(ca, cfg.hcap, 256, h->st);
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(h->st));
-  TRY(check_device_errors(h));
-  std::vector<Cand> c((size_t)n * max_per_read);
-  CK(cudaMemcpy(c.data(), dc.p, c.size() * sizeof(Cand), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(n_cand, dn.p, n * 4, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(total_cand, dt.p, n * 4, cudaMemcpyDeviceToHost));
-  for (uint64_t i = 0; i < (uint64_t)n * max_per_read; i++) {
-    cand_contig[i] = c[i].contig;
-    cand_pos[i] = c[i].pos;
-    cand_strand[i] = c[i].strand;
-    cand_score[i] = (double)c[i].score;
+  std::vector<Cand> c;
+  for (uint64_t r0 = 0; r0 < n; r0 += cfg.ch) {
+    const uint32_t nr = (uint32_t)std::min<uint64_t>(cfg.ch, n - r0);
+    CK(cudaMemsetAsync(dn.p, 0, nr * 4, h->st));
+    CK(cudaMemsetAsync(dt.p, 0, nr * 4, h->st));
+    TRY(seed_phase(h, cfg, h->d_bases.p, h->d_offs.p, (uint32_t)r0, nr, h->d_rep.p, false, nullptr));
+    TRY(cluster_phase(h, cfg, h->d_bases.p, h->d_offs.p, (uint32_t)r0, nr, h->d_rep.p, dc.p, dn.p, dt.p,
+                      max_per_read, false));
+    CK(cudaStreamSynchronize(h->st));
+    TRY(check_device_errors(h));
+    c.resize((size_t)nr * max_per_read);
+    CK(cudaMemcpy(c.data(), dc.p, c.size() * sizeof(Cand), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(n_cand + r0, dn.p, nr * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(total_cand + r0, dt.p, nr * 4, cudaMemcpyDeviceToHost));
+    const size_t base = (size_t)r0 * max_per_read;
+    for (size_t i = 0; i < c.size(); i++) {
+      cand_contig[base + i] = c[i].contig;
+      cand_pos[base + i] = c[i].pos;
+      cand_strand[base + i] = c[i].strand;
+      cand_score[base + i] = (double)c[i].score;
+    }
   }
   return PBW_OK;
 }

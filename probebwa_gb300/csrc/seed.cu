@@ -120,13 +120,16 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
   const int nwarps = gridDim.x * wpb;
   const bool list_mode = p.list != nullptr;
   const uint32_t nitems = list_mode ? *p.list_n : p.nr;
+  const unsigned long long s_lo = list_mode ? (unsigned long long)p.slice * p.pool_slice : 0ull;
+  if (list_mode && s_lo >= *p.list_total) return;
   for (uint32_t item = gw; item < nitems; item += nwarps) {
+    if (list_mode && p.list_hoff[item] / p.pool_slice != p.slice) continue;
     const uint32_t r = list_mode ? p.list[item] : item;
     const uint64_t rg = (uint64_t)p.r0 + r;
     const uint64_t o0 = p.offs[rg];
     const int L = (int)(p.offs[rg + 1] - o0);
     uint8_t* rep = p.rep + (size_t)r * p.wcap;
-    unsigned long long* hits = list_mode ? p.hits_pool + p.list_hoff[item] : p.hits + (size_t)r * p.hcap;
+    unsigned long long* hits = list_mode ? p.hits_pool + (p.list_hoff[item] - s_lo) : p.hits + (size_t)r * p.hcap;
     const uint32_t hcap = list_mode ? p.need[r] : p.hcap;
     if (L < KMER) {
       if (lane == 0 && !list_mode) { p.hit_cnt[r] = 0; p.overflow[r] = 0; }
@@ -261,6 +264,7 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
           if (slot < hcap) {
             hits[slot] = word;
             if (p.hit_rpos && !list_mode) p.hit_rpos[(size_t)r * p.hcap + slot] = (uint16_t)s_w;
+            if (p.hit_rpos_pool && list_mode) p.hit_rpos_pool[p.list_hoff[item] - s_lo + slot] = (uint16_t)s_w;
             if (p.hit_info && !list_mode) {
               const uint32_t wc = wcnt[s_w];
               const uint32_t l2 = min(32u - (uint32_t)__clz(wc), 31u);
@@ -303,29 +307,64 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
   }
 }
 
-// Exclusive offsets of the overflowed reads' exact hit counts in the pool.
+// Exclusive offsets of the overflowed reads' exact hit counts (one block,
+// a scan of 1024 at a time), their total, and the checks of the slice
+// limits.
 __global__ void k_ovf_offsets(const uint32_t* list, const unsigned int* list_n, const uint32_t* need,
-                              unsigned long long* hoff, unsigned long long pool_cap, int* err,
-                              unsigned int* list_n_out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+                              unsigned long long* hoff, unsigned long long* total, unsigned long long pool_slice,
+                              uint32_t max_slices, int* err, unsigned int* list_n_out) {
+  __shared__ unsigned long long wsum[32];
+  __shared__ unsigned long long carry;
+  __shared__ int bad;
   const unsigned int n = *list_n;
-  unsigned long long acc = 0;
-  for (unsigned int i = 0; i < n; i++) {
-    hoff[i] = acc;
-    acc += need[list[i]];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) {
+    carry = 0;
+    bad = 0;
   }
-  if (acc > pool_cap) {
-    atomicExch(err, 5);
-    *list_n_out = 0;
-  } else {
-    *list_n_out = n;
+  __syncthreads();
+  for (unsigned int base = 0; base < n; base += blockDim.x) {
+    const unsigned int i = base + threadIdx.x;
+    const unsigned long long v = i < n ? need[list[i]] : 0ull;
+    if (v > pool_slice) bad = 1;
+    unsigned long long s = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, s, d);
+      if (lane >= d) s += y;
+    }
+    if (lane == 31) wsum[wid] = s;
+    __syncthreads();
+    if (wid == 0) {
+      unsigned long long t = lane < nw ? wsum[lane] : 0ull;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, t, d);
+        if (lane >= d) t += y;
+      }
+      if (lane < nw) wsum[lane] = t;
+    }
+    __syncthreads();
+    const unsigned long long before = carry + (wid ? wsum[wid - 1] : 0ull) + s - v;
+    if (i < n) hoff[i] = before;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += wsum[nw - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const unsigned long long tot = carry;
+    // items start in slices [0, max_slices) and reach at most one slice past their start
+    const bool over = bad || (tot > 0 && (tot - 1) / pool_slice >= max_slices);
+    if (over) atomicExch(err, 5);
+    *total = over ? 0ull : tot;
+    *list_n_out = over ? 0u : n;
   }
 }
 
 void launch_ovf_offsets(const uint32_t* list, const unsigned int* list_n, const uint32_t* need,
-                        unsigned long long* hoff, unsigned long long pool_cap, int* err, unsigned int* list_n_out,
-                        cudaStream_t st) {
-  k_ovf_offsets<<<1, 32, 0, st>>>(list, list_n, need, hoff, pool_cap, err, list_n_out);
+                        unsigned long long* hoff, unsigned long long* total, unsigned long long pool_slice,
+                        uint32_t max_slices, int* err, unsigned int* list_n_out, cudaStream_t st) {
+  k_ovf_offsets<<<1, 1024, 0, st>>>(list, list_n, need, hoff, total, pool_slice, max_slices, err, list_n_out);
 }
 
 void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st) {

@@ -103,3 +103,21 @@ def test_align_empty_inputs(M, oracle):
     got = M.align_batch(probs)
     for p, g in zip(probs, got):
         assert g == oracle.align(*p)
+
+
+def test_window_wait_limit_gives_an_error(M, oracle):
+    """The whole-window DP's warps wait for their left neighbour with a
+    bounded spin. With the poll limit lowered to 1 the waits of multi-tile
+    windows give up: the call returns PBW_ERR_DEVICE with its reason instead
+    of hanging, and the handle maps correctly again once the limit is back."""
+    import probebwa_gb300 as P
+    probs = _problems(14, 40, "window")
+    M.set_tuning(wait_polls=1)
+    try:
+        with pytest.raises(P.PbwError, match="wavefront wait"):
+            M.align_batch(probs)
+    finally:
+        M.set_tuning(wait_polls=0)
+    assert M.tuning()["wait_polls"] == 0
+    got = M.align_batch(probs)
+    assert got == [oracle.align(*p) for p in probs]

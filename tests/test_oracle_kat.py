@@ -14,7 +14,10 @@ import pytest
 import kat_cases as K
 import sthash_py as SH
 
-REF_INTEGRATION = "/root/reference/tests/integration.rs"
+# The reference checkout, when present, supplies the E. coli literals of its
+# DP known-answer test at run time (they are not copied into this repository).
+REF_INTEGRATION = os.path.join(os.environ.get("PBW_REFERENCE_DIR", os.path.join(os.sep, "root", "reference")),
+                               "tests", "integration.rs")
 
 
 def _index(oracle, tmp_path, contigs, name="ref", **kw):
