@@ -25,6 +25,7 @@ constexpr int MAX_CAND = 20;                     // single.rs:114 take(20)
 constexpr int32_t NEG = INT32_MIN / 2;           // smith_waterman.rs:173
 constexpr uint64_t DIAG_BIAS = 1ull << 16;       // > PBW_MAX_READ_LEN
 constexpr uint32_t REPEAT_SKIP = 64;             // seeds.rs:45
+constexpr int RANK_FEATURES = 12;                // candidate ranker: seed features per candidate
 constexpr int CIG_INLINE = 12;                   // CIGAR ops kept inline per alignment
 
 // Internal base codes. Reference bases: A0 C1 G2 T3 N4. Reads: the same plus

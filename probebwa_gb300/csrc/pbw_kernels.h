@@ -83,19 +83,23 @@ struct ClusterArgs {
   unsigned long long pool_slice;  // as SeedArgs: the slice of the pool in use
   uint32_t slice;
   const unsigned long long* list_total;
-  // optional, for the candidate ranker: sorted hits written back in place,
-  // their emission slots, and each kept candidate's range in that order
-  unsigned long long* sorted_hits;  // nr * hcap (the hits array itself)
-  uint16_t* hit_src;                // nr * hcap
-  uint32_t* cand_span;              // nr * max_out: first | end << 16; 0xFFFFFFFF for list-mode reads
+  // with the candidate ranker: per kept candidate RANK_FEATURES seed features
+  // (list-mode reads, whose hits are in the pool, get feature 0 = -1: no
+  // hit-level features)
+  float* feat;                      // nr * MAX_CAND * RANK_FEATURES
+  const uint16_t* hit_info;         // nr * hcap: read position | log2 bucket << 10 | neighbour << 15
+  const uint8_t* quals;             // the reads' Phred scores (at offs)
 };
-size_t cluster_smem(uint32_t hmax, int threads);
-void launch_cluster(const ClusterArgs& a, uint32_t hmax, int threads, cudaStream_t st);
 void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st);
-// Reads of h_lo < H <= h_hi hits (beyond the shared-memory tiers) from the
-// per-read buffer; a.scratch holds grid slabs of cluster_big_slab_bytes(h_hi).
-size_t cluster_big_slab_bytes(uint32_t hmax);
-void launch_cluster_big(const ClusterArgs& a, uint32_t hmax, int grid, cudaStream_t st);
+// K2 by diagonal bins (no sort of the hits; cluster.cu) for reads of
+// h_lo < H <= h_hi <= hmax hits: the bin table in shared memory, or with
+// table_in_slab in a.scratch, which holds grid slabs of
+// cluster_bins_slab_bytes(hmax, table_in_slab).
+size_t cluster_bins_slab_bytes(uint32_t hmax, bool table_in_slab);
+size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat);
+void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, bool table_in_slab,
+                         cudaStream_t st);
+uint32_t next_pow2_host(uint32_t x);
 void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st);
 // Exclusive offsets of the listed (over-capacity) reads' hit counts, their
 // total, and the list length for the list-mode passes; a read needing more

@@ -132,8 +132,7 @@ struct pbw_handle {
     double label_cut = 0.0;   // training label: lk - lk_max >= label_cut
     pbw::DevBuf<float> d_norm, d_w, d_m, d_v, d_g, d_loss;
     pbw::DevBuf<uint32_t> d_wb;
-    pbw::DevBuf<uint16_t> d_hit_info, d_hit_src;
-    pbw::DevBuf<uint32_t> d_span;
+    pbw::DevBuf<uint16_t> d_hit_info;
     pbw::DevBuf<float> d_feat, d_logit;               // 2 read sets x chunk slots
     pbw::DevBuf<unsigned long long> d_counters;       // kept, pruned, reads kept whole
     pbw::DevBuf<float> c_feat;                        // collection: slot-indexed

@@ -65,8 +65,25 @@ int pipeline_init(pbw_handle* h) {
 constexpr size_t OVF_SLICE_HITS = 16ull << 20;
 constexpr size_t OVF_POOL_HITS = 2 * OVF_SLICE_HITS;
 constexpr uint32_t OVF_MAX_SLICES = 16;
-constexpr uint32_t CL_SMEM_HITS = 4096;  // the largest read K2 sorts in shared memory
-static int cl_big_grid(const pbw_handle* h) { return h->num_sms * 2; }
+// Tiers of the binned K2 (reads up to hmax hits, threads per block, blocks
+// per SM, table in the global slab).
+struct BinTier {
+  uint32_t hmax;
+  int threads, per_sm;
+  bool in_slab;
+};
+constexpr BinTier BIN_TIERS[3] = {{1024, 128, 6, false}, {4096, 256, 2, false}, {0, 512, 2, true}};
+static size_t cluster_scratch_bytes(const pbw_handle* h, uint32_t hcap) {
+  size_t need = 0;
+  uint32_t lo = 0;
+  for (const BinTier& t : BIN_TIERS) {
+    const uint32_t hm = t.hmax ? std::min(t.hmax, hcap) : hcap;
+    if (hm <= lo) continue;
+    need = std::max(need, cluster_bins_slab_bytes(t.hmax ? t.hmax : hcap, t.in_slab) * (size_t)h->num_sms * t.per_sm);
+    lo = hm;
+  }
+  return need;
+}
 // The slice in use: OVF_SLICE_HITS unless pbw_set_tuning lowered it (the
 // total the chunk may hold stays OVF_MAX_SLICES * OVF_SLICE_HITS).
 static uint64_t ovf_slice_hits(const pbw_handle* h) {
@@ -131,7 +148,7 @@ static int ensure_chunk(pbw_handle* h, const ChunkCfg& c) {
   TRY(grow(h, h->d_list_hoff, c.ch));
   TRY(grow(h, h->d_hits_pool, OVF_POOL_HITS));
   TRY(grow(h, h->d_cl_scratch, OVF_POOL_HITS * 112));
-  if (c.hcap > CL_SMEM_HITS) TRY(grow(h, h->d_cl_big, cluster_big_slab_bytes(c.hcap) * (size_t)cl_big_grid(h)));
+  TRY(grow(h, h->d_cl_big, cluster_scratch_bytes(h, c.hcap)));
   if (h->opt.max_indel_len > 31) TRY(ensure_window_slab(h, c.lmax, c.nmax, window_grid(h)));
   else TRY(grow(h, h->d_tb_global, band_tb_slab_bytes(c.lmax, c.nmax, h->num_sms, (int)h->opt.max_indel_len)));
   return PBW_OK;
@@ -185,8 +202,6 @@ struct MateBufs {
 // Ranker buffers of one chunk (ranked or collecting map calls).
 static int ensure_ranker_chunk(pbw_handle* h, const ChunkCfg& c) {
   TRY(grow(h, h->rk.d_hit_info, (size_t)c.ch * c.hcap));
-  TRY(grow(h, h->rk.d_hit_src, (size_t)c.ch * c.hcap));
-  TRY(grow(h, h->rk.d_span, (size_t)c.ch * MAX_CAND));
   TRY(grow(h, h->rk.d_feat, 2 * (size_t)c.ch * MAX_CAND * RK_F));
   TRY(grow(h, h->rk.d_logit, 2 * (size_t)c.ch * MAX_CAND));
   TRY(grow(h, h->rk.d_counters, 4));
@@ -295,13 +310,13 @@ static int ovf_slice(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, c
 }
 
 // K2 after seed_phase: the first max_out candidates of each read into
-// cand (nr * max_out), the full count into total_cand; the over-capacity
+// cand (nr * max_out), the full count into total_cand, and with feat the
+// candidate ranker's features of each kept candidate; the over-capacity
 // reads are seeded into the pool and clustered slice by slice.
-static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint64_t* offs,
-                         uint32_t r0, uint32_t nr, uint8_t* rep, Cand* cand, uint32_t* n_cand, uint32_t* total_cand,
-                         uint32_t max_out, bool ranker_info) {
+static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, const uint8_t* quals,
+                         const uint64_t* offs, uint32_t r0, uint32_t nr, uint8_t* rep, Cand* cand, uint32_t* n_cand,
+                         uint32_t* total_cand, uint32_t max_out, float* feat) {
   cudaStream_t st = h->st;
-  unsigned int* c32 = h->d_cnt32.p;
   ClusterArgs ca{};
   ca.hits = h->d_hits.p;
   ca.hit_cnt = h->d_hit_cnt.p;
@@ -316,27 +331,24 @@ static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* base
   ca.n_cand = n_cand;
   ca.total_cand = total_cand;
   ca.err = h->d_err.p;
-  if (ranker_info) {
-    ca.sorted_hits = h->d_hits.p;
-    ca.hit_src = h->rk.d_hit_src.p;
-    ca.cand_span = h->rk.d_span.p;
+  if (feat) {
+    ca.feat = feat;
+    ca.hit_info = h->rk.d_hit_info.p;
+    ca.quals = quals;
   }
-  ca.h_lo = 0;
-  ca.h_hi = 512;
-  launch_cluster(ca, 512, 64, st);
-  ca.h_lo = 512;
-  ca.h_hi = std::min<uint32_t>(cfg.hcap, CL_SMEM_HITS);
-  launch_cluster(ca, ca.h_hi, 256, st);
-  h->stats.kernel_launches += 2;
-  if (cfg.hcap > CL_SMEM_HITS) {
+  // reads within the per-read buffer, by hit-count tier
+  uint32_t lo = 0;
+  for (const BinTier& t : BIN_TIERS) {
+    const uint32_t hm = t.hmax ? std::min(t.hmax, cfg.hcap) : cfg.hcap;
+    if (hm <= lo) continue;
     ClusterArgs cb = ca;
-    cb.h_lo = CL_SMEM_HITS;
-    cb.h_hi = cfg.hcap;
+    cb.h_lo = lo;
+    cb.h_hi = hm;
     cb.scratch = h->d_cl_big.p;
-    launch_cluster_big(cb, cfg.hcap, cl_big_grid(h), st);
+    launch_cluster_bins(cb, t.hmax ? t.hmax : cfg.hcap, t.threads, h->num_sms * t.per_sm, t.in_slab, st);
     h->stats.kernel_launches += 1;
+    lo = hm;
   }
-  (void)c32;
   const uint32_t ns = ovf_max_slices(h);
   for (uint32_t s = 0; s < ns; s++) TRY(ovf_slice(h, cfg, bases, offs, r0, nr, rep, s, nullptr, &ca));
   CK(cudaGetLastError());
@@ -354,25 +366,8 @@ static int seed_cluster(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases
   CK(cudaEventRecord(ev[0], st));
   TRY(seed_phase(h, cfg, bases, offs, r0, nr, mb.rep, feat != nullptr, nullptr));
   CK(cudaEventRecord(ev[1], st));
-  TRY(cluster_phase(h, cfg, bases, offs, r0, nr, mb.rep, mb.cand, mb.n_cand, h->d_total_cand.p, MAX_CAND,
-                    feat != nullptr));
-  if (feat) {
-    RankFeatArgs fa{};
-    fa.hits = h->d_hits.p;
-    fa.hit_src = h->rk.d_hit_src.p;
-    fa.hit_info = h->rk.d_hit_info.p;
-    fa.hcap = cfg.hcap;
-    fa.cand = mb.cand;
-    fa.n_cand = mb.n_cand;
-    fa.span = h->rk.d_span.p;
-    fa.quals = quals;
-    fa.offs = offs;
-    fa.r0 = r0;
-    fa.nr = nr;
-    fa.feat = feat;
-    launch_rank_features(fa, h->num_sms * 8, st);
-    h->stats.kernel_launches += 1;
-  }
+  TRY(cluster_phase(h, cfg, bases, quals, offs, r0, nr, mb.rep, mb.cand, mb.n_cand, h->d_total_cand.p, MAX_CAND,
+                    feat));
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[2], st));
   return PBW_OK;
@@ -1627,8 +1622,8 @@ int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_re
     CK(cudaMemsetAsync(dn.p, 0, nr * 4, h->st));
     CK(cudaMemsetAsync(dt.p, 0, nr * 4, h->st));
     TRY(seed_phase(h, cfg, h->d_bases.p, h->d_offs.p, (uint32_t)r0, nr, h->d_rep.p, false, nullptr));
-    TRY(cluster_phase(h, cfg, h->d_bases.p, h->d_offs.p, (uint32_t)r0, nr, h->d_rep.p, dc.p, dn.p, dt.p,
-                      max_per_read, false));
+    TRY(cluster_phase(h, cfg, h->d_bases.p, h->d_quals.p, h->d_offs.p, (uint32_t)r0, nr, h->d_rep.p, dc.p, dn.p,
+                      dt.p, max_per_read, nullptr));
     CK(cudaStreamSynchronize(h->st));
     TRY(check_device_errors(h));
     c.resize((size_t)nr * max_per_read);

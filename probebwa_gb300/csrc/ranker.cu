@@ -13,8 +13,10 @@
 //   8 opposite-strand mate candidate on the same contig (pairs)
 //   9 rank i in the candidate list       10 candidate list size
 //  11 mean log2 exact bucket size of the hits' windows (repeat multiplicity)
-// A read whose hits overflowed the per-read buffer has no hit-level
-// features (feature 0 = -1): its candidates are all kept.
+// The clustering kernel (cluster.cu, binned form) computes features 0-6 and
+// 9-11 from its per-bin sums; 7-8 come from the other mate's candidates
+// (k_rank_mate). A read whose hits went to the overflow pool has no
+// hit-level features (feature 0 = -1): its candidates are all kept.
 //
 // Label (plain path): the candidate was aligned and either is the read's
 // select_best winner (the last maximum, bayesian.rs:193-201) or has
@@ -52,75 +54,6 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       "{%0,%1,%2,%3};\n"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-__device__ __forceinline__ float l2p(float x) { return log2f(1.f + x); }
-
-__global__ void __launch_bounds__(256) k_rank_features(RankFeatArgs a) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < a.nr; r += nw) {
-    const uint64_t rg = (uint64_t)a.r0 + r;
-    const uint64_t q0 = a.offs[rg];
-    const uint32_t L = (uint32_t)(a.offs[rg + 1] - q0);
-    uint32_t qs = 0;
-    for (uint32_t k = lane; k < L; k += 32) qs += a.quals[q0 + k];
-    for (int d = 16; d; d >>= 1) qs += __shfl_xor_sync(0xffffffffu, qs, d);
-    const float meanq = L ? (float)qs / (float)L : 0.f;
-    const uint32_t nc = a.n_cand[r];
-    const unsigned long long* hk = a.hits + (size_t)r * a.hcap;
-    const uint16_t* hsrc = a.hit_src + (size_t)r * a.hcap;
-    const uint16_t* hinfo = a.hit_info + (size_t)r * a.hcap;
-    for (uint32_t i = 0; i < (uint32_t)MAX_CAND; i++) {
-      float* f = a.feat + ((size_t)r * MAX_CAND + i) * RK_F;
-      if (i >= nc) {
-        if (lane < RK_F) f[lane] = 0.f;
-        continue;
-      }
-      const uint32_t sp = a.span[(size_t)r * MAX_CAND + i];
-      if (sp == 0xFFFFFFFFu) {
-        if (lane < RK_F) f[lane] = lane == 0 ? -1.f : 0.f;
-        continue;
-      }
-      const uint32_t hs = sp & 0xFFFFu, he = sp >> 16;
-      uint32_t ne = 0, n1 = 0, nd = 0, l2s = 0, rmin = 0xFFFFu, rmax = 0;
-      for (uint32_t k = hs + lane; k < he; k += 32) {
-        const unsigned long long key = hk[k];
-        const uint32_t info = hinfo[hsrc[k]];
-        const uint32_t nb = info >> 15;
-        ne += nb ? 0u : 1u;
-        n1 += nb;
-        nd += (k == hs || hk[k - 1] != key) ? 1u : 0u;
-        const uint32_t rp = info & 0x3FFu;
-        rmin = min(rmin, rp);
-        rmax = max(rmax, rp);
-        l2s += (info >> 10) & 31u;
-      }
-      for (int d = 16; d; d >>= 1) {
-        ne += __shfl_xor_sync(0xffffffffu, ne, d);
-        n1 += __shfl_xor_sync(0xffffffffu, n1, d);
-        nd += __shfl_xor_sync(0xffffffffu, nd, d);
-        l2s += __shfl_xor_sync(0xffffffffu, l2s, d);
-        rmin = min(rmin, __shfl_xor_sync(0xffffffffu, rmin, d));
-        rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, d));
-      }
-      if (lane == 0) {
-        const unsigned long long spread = he > hs ? ((hk[he - 1] - hk[hs]) & ((1ull << 40) - 1)) : 0ull;
-        const uint32_t nh = ne + n1;
-        f[0] = l2p((float)ne);
-        f[1] = l2p((float)n1);
-        f[2] = l2p((float)nd);
-        f[3] = l2p((float)spread);
-        f[4] = l2p(nh ? (float)(rmax - rmin + KMER) : 0.f);
-        f[5] = (float)L;
-        f[6] = meanq;
-        f[7] = 10.f;
-        f[8] = 0.f;
-        f[9] = (float)i;
-        f[10] = (float)nc;
-        f[11] = nh ? (float)l2s / (float)nh : 0.f;
-      }
-    }
-  }
 }
 
 // Thread per candidate slot of read set A.
@@ -426,10 +359,6 @@ __global__ void k_rank_pack(const float* w, uint32_t* wb) {
 
 }  // namespace
 
-void launch_rank_features(const RankFeatArgs& a, int grid, cudaStream_t st) {
-  if (a.nr == 0) return;
-  k_rank_features<<<grid, 256, 0, st>>>(a);
-}
 void launch_rank_mate(const RankMateArgs& a, cudaStream_t st) {
   const uint64_t n = (uint64_t)a.nr * MAX_CAND;
   if (n == 0) return;

@@ -12,7 +12,7 @@
 
 namespace pbw {
 
-constexpr int RK_F = 12;  // features per candidate
+constexpr int RK_F = RANK_FEATURES;  // features per candidate
 constexpr int RK_H = 64;  // hidden width
 // fp32 master parameters: W1[64][12], b1[64], W2[64][64] (row n, column k), b2[64], w3[64], b3
 constexpr int RK_W1 = 0, RK_B1 = RK_W1 + RK_H * RK_F, RK_W2 = RK_B1 + RK_H, RK_B2 = RK_W2 + RK_H * RK_H,
@@ -23,20 +23,6 @@ constexpr int RK_WB_WORDS = (RK_H * 16 + RK_H * RK_H) / 2;
 // label of a candidate slot that was not aligned (excluded from training)
 constexpr uint8_t RK_IGNORE = 255;
 
-// Per-candidate seed features of one read set's chunk (warp per read).
-struct RankFeatArgs {
-  const unsigned long long* hits;  // per read, sorted by K2 (nr * hcap)
-  const uint16_t* hit_src;         // sorted position -> emission slot
-  const uint16_t* hit_info;        // emission slot -> read position | log2 bucket << 10 | neighbour << 15
-  uint32_t hcap;
-  const Cand* cand;
-  const uint32_t* n_cand;
-  const uint32_t* span;            // per slot: first | end << 16 of its sorted hits; 0xFFFFFFFF: none
-  const uint8_t* quals;
-  const uint64_t* offs;
-  uint32_t r0, nr;
-  float* feat;                     // nr * MAX_CAND * RK_F
-};
 
 // Mate-consistency features of read set A against read set B (same pairs).
 struct RankMateArgs {
@@ -77,7 +63,6 @@ struct RankLabelArgs {
   double cut;                      // positive when lk - lk_max >= cut (log units)
 };
 
-void launch_rank_features(const RankFeatArgs& a, int grid, cudaStream_t st);
 void launch_rank_mate(const RankMateArgs& a, cudaStream_t st);
 void launch_rank_infer(const float* feat, uint64_t n_slots, const RankModelDev& m, float* logit, int grid,
                        cudaStream_t st);
