@@ -177,7 +177,8 @@ int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uin
 /* cluster_hits (src/mapper/candidates.rs:30-78) after seeding: per read the
  * first max_per_read candidates in final order (contig, 0-based position,
  * strand, score) and the full candidate count. Row i of the candidate
- * arrays starts at i * max_per_read; its first n_cand[i] entries are set.
+ * arrays starts at i * max_per_read (1 <= max_per_read <= 256); its first
+ * n_cand[i] entries are set.
  * Over-capacity reads are clustered from the overflow pool as in a map call. */
 int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_read, uint32_t* n_cand,
                       uint32_t* total_cand, uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,

@@ -332,221 +332,308 @@ __global__ void k_cluster_list(ClusterArgs p) {
 }
 
 // ---------------------------------------------------------------------------
-// K2 by diagonal bins. The clusters of cluster_hits are the maximal runs of a
-// group's sorted diagonals whose neighbours differ by at most MERGE_DISTANCE
-// (50). Cut the diagonal axis into bins of 51: two hits of one bin are at
-// most 50 apart, so a bin never splits; bins two or more apart are more than
-// 50 apart, so they never join; two adjacent bins join exactly when the lower
-// one's largest diagonal and the upper one's smallest are at most 50 apart.
-// So the hits need no sort: a hash table keyed by (group, bin) collects each
-// bin's hit count, diagonal sum, diagonal set (a 51-bit mask: smallest,
-// largest and distinct diagonals) and first emission index with shared-memory
-// atomics, and only the non-empty bins are sorted. From the sorted bins come
-// the group boundaries, the clusters (runs of joined bins), each group's
-// first emission index -- the FxHashMap insertion order whose SwissTable
-// replay gives the iteration order -- and the cluster order of the
-// reference's stable sort (count desc, group rank, diagonal order).
+// K2 by diagonal bins, without sorting. The clusters of cluster_hits are the
+// maximal runs of a group's sorted diagonals whose neighbours differ by at
+// most MERGE_DISTANCE (50). Cut the diagonal axis into bins of 51: two hits
+// of one bin are at most 50 apart, so a bin never splits; bins two or more
+// apart are more than 50 apart, so they never join; two adjacent bins join
+// exactly when the lower one's largest diagonal and the upper one's smallest
+// are at most 50 apart. Per read (one block):
+//   A. every hit goes into a hash table keyed by (group, bin) -- hit count,
+//      diagonal sum, the bin's diagonal set as a 51-bit mask -- and its group
+//      into a second table holding the group's first emission index (the
+//      FxHashMap insertion order);
+//   B. a bin whose lower neighbour does not join it starts a cluster; its
+//      thread walks the upper neighbours by lookups and records the
+//      cluster's count, diagonal sum, group and first bin;
+//   C. the groups, sorted by first emission, are replayed through std's
+//      SwissTable insertion (FxHasher of rustc-hash 2.1.3, probing by the
+//      group width), which gives each group's iteration rank;
+//   D. the reference's final stable sort orders clusters by (count desc,
+//      group rank, diagonal order); the key (0x7FFF - count) << 49 | rank
+//      << 35 | first bin is unique per cluster, and only the first max_out
+//      are needed: they are picked by repeated block-wide minima.
+// With the candidate ranker, bins and clusters also carry each candidate's
+// seed features (exact hits, bucket sizes, read positions).
 // ---------------------------------------------------------------------------
 constexpr int BIN_W = 51;  // MERGE_DISTANCE + 1 (candidates.rs:27)
 constexpr unsigned long long BIN_EMPTY = ~0ull;
+constexpr uint32_t GRP_EMPTY = 0xFFFFFFFFu;  // group keys (contig << 1 | strand) are below 2^24
+constexpr uint32_t NO_SLOT = 0xFFFFFFFFu;
 constexpr unsigned long long M40 = (1ull << 40) - 1;
+constexpr unsigned long long M35 = (1ull << 35) - 1;
+constexpr uint32_t BIN_TMIN = 64;  // smallest table (room for the SwissTable replay's scratch)
+constexpr uint32_t BIN_MAX_OUT = 256;  // candidates one read may return
 
-__device__ __forceinline__ uint32_t bin_slot(unsigned long long key, uint32_t T) {
+__device__ __forceinline__ uint32_t hash_slot(unsigned long long key, uint32_t T) {
   unsigned long long k = key ^ (key >> 33);
   k *= 0xff51afd7ed558ccdull;
   k ^= k >> 33;
   return (uint32_t)k & (T - 1);
 }
 
-// Per-block scratch of the bin path (global slab): arrays of NPB entries.
-struct BinScratch {
-  unsigned long long *ckey, *cacc, *cmask, *ps, *cinf;
-  uint32_t *cemin, *a, *bb, *pc, *gmin, *ggk, *gfirst, *rank, *clstart, *clgrp, *slots, *crmn, *crmx, *perm;
-  __device__ void carve(unsigned char* base, uint32_t NPB) {
-    unsigned long long* q = (unsigned long long*)base;
-    ckey = q; cacc = q + NPB; cmask = q + 2 * NPB; ps = q + 3 * NPB; cinf = q + 4 * NPB;
-    uint32_t* u = (uint32_t*)(q + 5 * NPB);
-    cemin = u; a = u + NPB; bb = u + 2 * NPB; pc = u + 3 * NPB; gmin = u + 4 * NPB; ggk = u + 5 * NPB;
-    gfirst = u + 6 * NPB; rank = u + 7 * NPB; clstart = u + 8 * NPB; clgrp = u + 9 * NPB + 1;
-    slots = u + 10 * NPB + 2;  // 2 * NPB
-    crmn = u + 12 * NPB + 2; crmx = u + 13 * NPB + 2; perm = u + 14 * NPB + 2;
+// Slot of key in an open-addressed table of T (a power of two) 64-bit keys,
+// inserting it if absent (a table never holds more than T keys).
+__device__ __forceinline__ uint32_t insert64(unsigned long long* keys, unsigned long long key, uint32_t T) {
+  uint32_t s = hash_slot(key, T);
+  for (uint32_t guard = 0; guard < T; guard++) {
+    const unsigned long long cur = keys[s];
+    if (cur == key) return s;
+    if (cur == BIN_EMPTY) {
+      const unsigned long long prev = atomicCAS(&keys[s], BIN_EMPTY, key);
+      if (prev == BIN_EMPTY || prev == key) return s;
+    }
+    s = (s + 1) & (T - 1);
   }
-};
-__host__ __device__ inline size_t bin_scratch_bytes(uint32_t NPB) {
-  return (((size_t)NPB * (5 * 8 + 15 * 4) + 64) + 255) & ~(size_t)255;
+  return NO_SLOT;
 }
-// table entry: key, count | diagonal-offset sum, diagonal mask, first emission
-// (28 bytes); with the ranker's features also exact hits | bucket-size sum
-// and the smallest and largest read position (16 bytes)
-__host__ __device__ inline size_t bin_table_bytes(uint32_t T, bool feat = false) {
-  return (size_t)T * (feat ? 44 : 28);
+__device__ __forceinline__ uint32_t find64(const unsigned long long* keys, unsigned long long key, uint32_t T) {
+  uint32_t s = hash_slot(key, T);
+  for (uint32_t guard = 0; guard < T; guard++) {
+    const unsigned long long cur = keys[s];
+    if (cur == key) return s;
+    if (cur == BIN_EMPTY) return NO_SLOT;
+    s = (s + 1) & (T - 1);
+  }
+  return NO_SLOT;
+}
+__device__ __forceinline__ uint32_t insert32(uint32_t* keys, uint32_t key, uint32_t T) {
+  uint32_t s = hash_slot(key, T);
+  for (uint32_t guard = 0; guard < T; guard++) {
+    const uint32_t cur = keys[s];
+    if (cur == key) return s;
+    if (cur == GRP_EMPTY) {
+      const uint32_t prev = atomicCAS(&keys[s], GRP_EMPTY, key);
+      if (prev == GRP_EMPTY || prev == key) return s;
+    }
+    s = (s + 1) & (T - 1);
+  }
+  return NO_SLOT;
+}
+__device__ __forceinline__ uint32_t find32(const uint32_t* keys, uint32_t key, uint32_t T) {
+  uint32_t s = hash_slot(key, T);
+  for (uint32_t guard = 0; guard < T; guard++) {
+    const uint32_t cur = keys[s];
+    if (cur == key) return s;
+    if (cur == GRP_EMPTY) return NO_SLOT;
+    s = (s + 1) & (T - 1);
+  }
+  return NO_SLOT;
 }
 
-// Clusters one read's H hits with a table of T = next_pow2(H) entries at tab
-// (room for TMAX), scratch S of TMAX entries and sort space of 12 * TMAX
-// bytes at sortbuf.
+// Tables of one read with T entries: bins (key, count << 40 | offset sum,
+// diagonal mask; with the ranker also exact hits << 32 | bucket-size sum and
+// the read-position range) and groups (key, first emission then rank).
+__host__ __device__ inline size_t bin_table_bytes(uint32_t T, bool feat) {
+  return (size_t)T * ((feat ? 40 : 24) + 8);
+}
+// Per-block cluster records in the global slab (TM entries each): diagonal
+// sum, first bin, count, group slot, group key; with the ranker exact hits,
+// bucket-size sum, distinct diagonals, read-position range and diagonal
+// spread; and the SwissTable replay's buckets.
+struct ClusterRecs {
+  unsigned long long *sum, *b0;
+  uint32_t *cnt, *gslot, *gk, *ne, *l2s, *nd, *rmn, *rmx, *spread, *slots;
+  __device__ void carve(unsigned char* base, uint32_t TM) {
+    unsigned long long* q = (unsigned long long*)base;
+    sum = q;
+    b0 = q + TM;
+    uint32_t* u = (uint32_t*)(q + 2 * TM);
+    cnt = u; gslot = u + TM; gk = u + 2 * TM; ne = u + 3 * TM; l2s = u + 4 * TM; nd = u + 5 * TM;
+    rmn = u + 6 * TM; rmx = u + 7 * TM; spread = u + 8 * TM;
+    slots = u + 9 * TM;  // 2 * TM
+  }
+};
+__host__ __device__ inline size_t cluster_recs_bytes(uint32_t TM) {
+  return ((size_t)TM * (2 * 8 + 11 * 4) + 255) & ~(size_t)255;
+}
+
 template <bool FEAT>
 __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
-                                  unsigned char* tab, const BinScratch& S, unsigned char* sortbuf,
-                                  uint32_t* wtmp32, unsigned long long* wtmp64, uint32_t& sh_n) {
-  const uint32_t T = next_pow2(H);  // >= H >= the bins of the read
-  unsigned long long* tkey = (unsigned long long*)tab;
-  unsigned long long* tacc = tkey + T;
-  unsigned long long* tmask = tacc + T;
-  unsigned long long* tinf = tmask + T;                        // FEAT
-  uint32_t* temin = (uint32_t*)(tmask + (FEAT ? 2 : 1) * T);
-  uint32_t* trmn = temin + T;                                  // FEAT
-  uint32_t* trmx = trmn + T;                                   // FEAT
+                                  unsigned char* tab, const ClusterRecs& S, uint32_t* wtmp32,
+                                  unsigned long long* wtmp64, uint32_t& sh_n, uint32_t* sh_sel) {
+  const uint32_t T = max(next_pow2(H), BIN_TMIN);  // >= the bins and the groups of the read
+  unsigned long long* bkey = (unsigned long long*)tab;
+  unsigned long long* bacc = bkey + T;
+  unsigned long long* bmask = bacc + T;
+  unsigned long long* binf = bmask + T;                         // FEAT
+  uint32_t* brmn = (uint32_t*)(bmask + (FEAT ? 2 : 1) * T);     // FEAT
+  uint32_t* brmx = brmn + T;                                    // FEAT
+  uint32_t* gkey = (uint32_t*)tab + (FEAT ? 10 : 6) * T;
+  uint32_t* gval = gkey + T;
   for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
-    tkey[s] = BIN_EMPTY;
-    tacc[s] = 0;
-    tmask[s] = 0;
-    temin[s] = 0xFFFFFFFFu;
+    bkey[s] = BIN_EMPTY;
+    bacc[s] = 0;
+    bmask[s] = 0;
+    gkey[s] = GRP_EMPTY;
+    gval[s] = 0xFFFFFFFFu;
     if (FEAT) {
-      tinf[s] = 0;
-      trmn[s] = 0xFFFFFFFFu;
-      trmx[s] = 0;
+      binf[s] = 0;
+      brmn[s] = 0xFFFFFFFFu;
+      brmx[s] = 0;
     }
   }
   if (threadIdx.x == 0) sh_n = 0;
   __syncthreads();
-  // aggregate: one table entry per (group, bin)
+  // A. bins and groups
   for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
     const unsigned long long w = hits[i];
     const unsigned long long d = w & M40;
     const unsigned long long b = d / BIN_W;
     const uint32_t off = (uint32_t)(d - b * BIN_W);
-    const unsigned long long key = ((w >> 40) << 35) | b;
-    uint32_t s = bin_slot(key, T);
-    for (uint32_t guard = 0; guard < T; guard++) {
-      const unsigned long long prev = atomicCAS(&tkey[s], BIN_EMPTY, key);
-      if (prev == BIN_EMPTY || prev == key) break;
-      s = (s + 1) & (T - 1);
+    const uint32_t gk = (uint32_t)(w >> 40);
+    const uint32_t s = insert64(bkey, ((unsigned long long)gk << 35) | b, T);
+    const uint32_t g = insert32(gkey, gk, T);
+    if (s == NO_SLOT || g == NO_SLOT) {
+      atomicExch(p.err, 1);
+      continue;
     }
-    atomicAdd(&tacc[s], (1ull << 40) | off);
-    atomicOr(&tmask[s], 1ull << off);
-    atomicMin(&temin[s], i);
+    atomicAdd(&bacc[s], (1ull << 40) | off);
+    atomicOr(&bmask[s], 1ull << off);
+    if (gval[g] > i) atomicMin(&gval[g], i);
     if (FEAT) {
       // hit info: read position | log2 exact bucket size << 10 | neighbour << 15
       const uint32_t info = p.hit_info[(size_t)r * p.hcap + i];
-      atomicAdd(&tinf[s], ((info >> 15) ? 0ull : (1ull << 32)) | ((info >> 10) & 31u));
-      atomicMin(&trmn[s], info & 0x3FFu);
-      atomicMax(&trmx[s], info & 0x3FFu);
+      atomicAdd(&binf[s], ((info >> 15) ? 0ull : (1ull << 32)) | ((info >> 10) & 31u));
+      atomicMin(&brmn[s], info & 0x3FFu);
+      atomicMax(&brmx[s], info & 0x3FFu);
     }
   }
   __syncthreads();
-  // compact the non-empty bins (any order: they are sorted next)
+  // B. clusters: runs of joined bins, walked from each run's first bin
   for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
-    if (tkey[s] == BIN_EMPTY) continue;
+    const unsigned long long key = bkey[s];
+    if (key == BIN_EMPTY) continue;
+    const unsigned long long b = key & M35;
+    unsigned long long m = bmask[s];
+    const unsigned long long lo = b * BIN_W + (unsigned long long)(__ffsll((long long)m) - 1);
+    if (b > 0) {
+      const uint32_t q = find64(bkey, key - 1, T);
+      if (q != NO_SLOT &&
+          lo - ((b - 1) * BIN_W + (unsigned long long)(63 - __clzll((long long)bmask[q]))) <= (unsigned)(BIN_W - 1))
+        continue;  // joined to the bin below
+    }
+    uint32_t cnt = 0, ne = 0, l2s = 0, nd = 0, rmn = 0xFFFFFFFFu, rmx = 0;
+    unsigned long long sum = 0, cb = b;
+    uint32_t cur = s;
+    while (true) {
+      const unsigned long long acc = bacc[cur];
+      const uint32_t c = (uint32_t)(acc >> 40);
+      cnt += c;
+      sum += cb * BIN_W * c + (acc & M40);
+      if (FEAT) {
+        ne += (uint32_t)(binf[cur] >> 32);
+        l2s += (uint32_t)(binf[cur] & 0xFFFFFFFFu);
+        nd += (uint32_t)__popcll(m);
+        rmn = min(rmn, brmn[cur]);
+        rmx = max(rmx, brmx[cur]);
+      }
+      const uint32_t q = find64(bkey, key - b + cb + 1, T);
+      if (q == NO_SLOT) break;
+      const unsigned long long mq = bmask[q];
+      const unsigned long long hi = cb * BIN_W + (unsigned long long)(63 - __clzll((long long)m));
+      if ((cb + 1) * BIN_W + (unsigned long long)(__ffsll((long long)mq) - 1) - hi > (unsigned)(BIN_W - 1)) break;
+      cur = q;
+      m = mq;
+      cb++;
+    }
     const uint32_t k = atomicAdd(&sh_n, 1u);
-    S.ckey[k] = tkey[s];
-    S.cacc[k] = tacc[s];
-    S.cmask[k] = tmask[s];
-    S.cemin[k] = temin[s];
+    const uint32_t gk = (uint32_t)(key >> 35);
+    S.cnt[k] = cnt;
+    S.sum[k] = sum;
+    S.b0[k] = b;
+    S.gk[k] = gk;
+    S.gslot[k] = find32(gkey, gk, T);
     if (FEAT) {
-      S.cinf[k] = tinf[s];
-      S.crmn[k] = trmn[s];
-      S.crmx[k] = trmx[s];
+      S.ne[k] = ne;
+      S.l2s[k] = l2s;
+      S.nd[k] = nd;
+      S.rmn[k] = rmn;
+      S.rmx[k] = rmx;
+      S.spread[k] = (uint32_t)(cb * BIN_W + (unsigned long long)(63 - __clzll((long long)m)) - lo);
     }
   }
   __syncthreads();
-  const uint32_t nb = sh_n;
-  // sort the bins by (group, bin)
-  const uint32_t nbp = next_pow2(nb);
-  unsigned long long* skey = (unsigned long long*)sortbuf;
-  uint32_t* sval = (uint32_t*)(skey + nbp);
-  for (uint32_t i = threadIdx.x; i < nbp; i += blockDim.x) {
-    skey[i] = i < nb ? S.ckey[i] : ~0ull;
-    sval[i] = i;
+  const uint32_t C = sh_n;
+  // C. groups in first-emission order, SwissTable replay (the bin table's
+  // space holds the sort); gval becomes the group's iteration rank
+  unsigned long long* okey = bkey;
+  uint32_t* oval = (uint32_t*)(bkey + T);
+  __syncthreads();
+  if (threadIdx.x == 0) sh_n = 0;
+  __syncthreads();
+  for (uint32_t g = threadIdx.x; g < T; g += blockDim.x) {
+    if (gkey[g] == GRP_EMPTY) continue;
+    const uint32_t k = atomicAdd(&sh_n, 1u);
+    okey[k] = ((unsigned long long)gval[g] << 32) | g;
   }
   __syncthreads();
-  bitonic_kv(skey, sval, nbp);
-  // bin i of the sorted order: group and cluster starts, count and diagonal sum
-  for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) {
-    const unsigned long long key = skey[i];
-    const uint32_t e = sval[i];
-    const unsigned long long b = key & ((1ull << 35) - 1);
-    const unsigned long long acc = S.cacc[e];
-    const uint32_t cnt = (uint32_t)(acc >> 40);
-    bool gs = i == 0, cs = i == 0;
-    if (i > 0) {
-      const unsigned long long kp = skey[i - 1];
-      gs = (kp >> 35) != (key >> 35);
-      const unsigned long long bp = kp & ((1ull << 35) - 1);
-      const unsigned long long lo = b * BIN_W + (unsigned long long)(__ffsll((long long)S.cmask[e]) - 1);
-      const unsigned long long hi = bp * BIN_W + (unsigned long long)(63 - __clzll((long long)S.cmask[sval[i - 1]]));
-      cs = gs || bp + 1 != b || lo - hi > (unsigned long long)(BIN_W - 1);
-    }
-    S.a[i] = cs ? 1u : 0u;
-    S.bb[i] = gs ? 1u : 0u;
-    S.pc[i] = cnt;
-    S.ps[i] = b * BIN_W * cnt + (acc & M40);
-    if (FEAT) S.perm[i] = e;
-  }
-  __syncthreads();
-  block_scan_incl<uint32_t>(S.a, nb, wtmp32);
-  block_scan_incl<uint32_t>(S.bb, nb, wtmp32);
-  block_scan_incl<uint32_t>(S.pc, nb, wtmp32);
-  block_scan_incl<unsigned long long>(S.ps, nb, wtmp64);
-  const uint32_t C = S.a[nb - 1], G = S.bb[nb - 1];
-  for (uint32_t g = threadIdx.x; g < G; g += blockDim.x) S.gmin[g] = 0xFFFFFFFFu;
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) {
-    const uint32_t cl = S.a[i] - 1, g = S.bb[i] - 1;
-    const bool cs = i == 0 || S.a[i] != S.a[i - 1];
-    const bool gs = i == 0 || S.bb[i] != S.bb[i - 1];
-    if (gs) {
-      S.ggk[g] = (uint32_t)(skey[i] >> 35);
-      S.gfirst[g] = cl;
-    }
-    if (cs) {
-      S.clstart[cl] = i;
-      S.clgrp[cl] = g;
-    }
-    atomicMin(&S.gmin[g], S.cemin[sval[i]]);
-  }
-  if (threadIdx.x == 0) S.clstart[C] = nb;
-  __syncthreads();
-  // group insertion order = ascending first emission index; SwissTable replay
+  const uint32_t G = sh_n;
   const uint32_t ng = next_pow2(G);
-  for (uint32_t g = threadIdx.x; g < ng; g += blockDim.x) {
-    skey[g] = g < G ? (((unsigned long long)S.gmin[g] << 32) | g) : ~0ull;
-    sval[g] = g;
+  for (uint32_t k = threadIdx.x; k < ng; k += blockDim.x) {
+    if (k >= G) okey[k] = ~0ull;
+    oval[k] = k;
   }
   __syncthreads();
-  bitonic_kv(skey, sval, ng);
-  // (a table of G items never needs more than 2 * next_pow2(G) buckets, and
-  // a small one starts at 4 or 8)
-  if (threadIdx.x == 0 && !swiss_replay(skey, G, S.ggk, S.slots, max(16u, 2 * ng), S.rank, p.group_width))
+  bitonic_kv(okey, oval, ng);
+  if (threadIdx.x == 0 && !swiss_replay(okey, G, gkey, S.slots, max(16u, 2 * ng), gval, p.group_width))
     atomicExch(p.err, 1);
   __syncthreads();
-  // clusters by (count desc, group rank, diagonal order)
-  const uint32_t nc = next_pow2(C);
-  for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
-    unsigned long long key = ~0ull;
-    if (c < C) {
-      const uint32_t g = S.clgrp[c];
-      const uint32_t s = S.clstart[c], e = S.clstart[c + 1];
-      const uint32_t cnt = S.pc[e - 1] - (s > 0 ? S.pc[s - 1] : 0u);
-      key = ((unsigned long long)(0xFFFFFu - cnt) << 44) | ((unsigned long long)S.rank[g] << 24) |
-            (unsigned long long)(c - S.gfirst[g]);
-    }
-    skey[c] = key;
-    sval[c] = c;
-  }
+  // D. cluster order keys (count desc, group rank, diagonal order); the first
+  // max_out by repeated block-wide minima
+  unsigned long long* ck = bkey;
+  for (uint32_t c = threadIdx.x; c < C; c += blockDim.x)
+    ck[c] = ((unsigned long long)(0x7FFFu - S.cnt[c]) << 49) | ((unsigned long long)gval[S.gslot[c]] << 35) | S.b0[c];
   __syncthreads();
-  bitonic_kv(skey, sval, nc);
+  const uint32_t nout = min(min(C, p.max_out), BIN_MAX_OUT);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned long long last = 0;
+  for (uint32_t o = 0; o < nout; o++) {
+    unsigned long long best = ~0ull;
+    uint32_t bi = 0;
+    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+      const unsigned long long v = ck[c];
+      if ((o == 0 || v > last) && v < best) {
+        best = v;
+        bi = c;
+      }
+    }
+    for (int d = 16; d; d >>= 1) {
+      const unsigned long long ov = __shfl_xor_sync(0xffffffffu, best, d);
+      const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, d);
+      if (ov < best) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      wtmp64[wid] = best;
+      wtmp32[wid] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long bv = wtmp64[0];
+      uint32_t bx = wtmp32[0];
+      for (int w2 = 1; w2 < nw; w2++)
+        if (wtmp64[w2] < bv) {
+          bv = wtmp64[w2];
+          bx = wtmp32[w2];
+        }
+      sh_sel[o] = bx;
+      wtmp64[0] = bv;
+    }
+    __syncthreads();
+    last = wtmp64[0];
+    __syncthreads();
+  }
   const uint64_t rg = (uint64_t)p.r0 + r;
   const long long L = (long long)(p.offs[rg + 1] - p.offs[rg]);
-  const uint32_t nout = min(C, p.max_out);
   for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
-    const uint32_t c = sval[i];
-    const uint32_t s = S.clstart[c], e = S.clstart[c + 1];
-    const uint32_t cnt = S.pc[e - 1] - (s > 0 ? S.pc[s - 1] : 0u);
-    const unsigned long long sumb = S.ps[e - 1] - (s > 0 ? S.ps[s - 1] : 0ull);
-    const long long sum = (long long)sumb - (long long)cnt * (long long)DIAG_BIAS;
+    const uint32_t c = sh_sel[i];
+    const uint32_t cnt = S.cnt[c];
+    const long long sum = (long long)S.sum[c] - (long long)cnt * (long long)DIAG_BIAS;
     const long long avg = sum / (long long)cnt;  // truncation toward zero, as Rust's i64 '/'
-    const uint32_t gk = S.ggk[S.clgrp[c]];
+    const uint32_t gk = S.gk[c];
     const long long posi = (gk & 1u) ? avg - L + KMER : avg;
     Cand cd;
     cd.pos = posi > 0 ? (unsigned long long)posi : 0ull;
@@ -557,59 +644,39 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     p.cand[(size_t)r * p.max_out + i] = cd;
   }
   if (FEAT) {
-    // the candidate ranker's seed features of each kept candidate (a warp per
-    // candidate): exact and one-mismatch hits, distinct diagonals, diagonal
-    // spread, read span of the hits, read length, mean base quality, rank and
-    // list size, mean log2 exact-bucket size (slots 7 and 8 are the mate
-    // features, filled for pairs later)
+    // the candidate ranker's seed features of each kept candidate: exact and
+    // one-mismatch hits, distinct diagonals, diagonal spread, read span of
+    // the hits, read length, mean base quality, rank and list size, mean
+    // log2 exact-bucket size (7 and 8, the mate features, come later)
     uint32_t qs = 0;
     const uint64_t q0 = p.offs[rg];
     for (uint32_t k = threadIdx.x; k < (uint32_t)L; k += blockDim.x) qs += p.quals[q0 + k];
     for (int d = 16; d; d >>= 1) qs += __shfl_xor_sync(0xffffffffu, qs, d);
-    if ((threadIdx.x & 31) == 0) wtmp32[threadIdx.x >> 5] = qs;
+    if (lane == 0) wtmp32[wid] = qs;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t t = 0;
-      for (uint32_t w = 0; w < blockDim.x / 32; w++) t += wtmp32[w];
-      sh_n = t;
-    }
-    __syncthreads();
-    const float meanq = L ? (float)sh_n / (float)L : 0.f;
+    uint32_t qt = 0;
+    for (int w2 = 0; w2 < nw; w2++) qt += wtmp32[w2];
+    const float meanq = L ? (float)qt / (float)L : 0.f;
     for (uint32_t i = threadIdx.x; i < (uint32_t)MAX_CAND; i += blockDim.x) {
       float* f = p.feat + ((size_t)r * MAX_CAND + i) * RANK_FEATURES;
       if (i >= nout) {
         for (int k = 0; k < RANK_FEATURES; k++) f[k] = 0.f;
         continue;
       }
-      const uint32_t c = sval[i];
-      const uint32_t s = S.clstart[c], e = S.clstart[c + 1];
-      uint32_t ne = 0, nd = 0, l2s = 0, rmin = 0xFFFFFFFFu, rmax = 0;
-      for (uint32_t k = s; k < e; k++) {
-        const uint32_t ce = S.perm[k];
-        ne += (uint32_t)(S.cinf[ce] >> 32);
-        l2s += (uint32_t)(S.cinf[ce] & 0xFFFFFFFFu);
-        nd += (uint32_t)__popcll(S.cmask[ce]);
-        rmin = min(rmin, S.crmn[ce]);
-        rmax = max(rmax, S.crmx[ce]);
-      }
-      const uint32_t cf = S.perm[s], cl = S.perm[e - 1];
-      const unsigned long long lo = (S.ckey[cf] & ((1ull << 35) - 1)) * BIN_W +
-                                    (unsigned long long)(__ffsll((long long)S.cmask[cf]) - 1);
-      const unsigned long long hi = (S.ckey[cl] & ((1ull << 35) - 1)) * BIN_W +
-                                    (unsigned long long)(63 - __clzll((long long)S.cmask[cl]));
-      const uint32_t nh = S.pc[e - 1] - (s > 0 ? S.pc[s - 1] : 0u);
+      const uint32_t c = sh_sel[i];
+      const uint32_t nh = S.cnt[c], ne = S.ne[c];
       f[0] = log2f(1.f + (float)ne);
       f[1] = log2f(1.f + (float)(nh - ne));
-      f[2] = log2f(1.f + (float)nd);
-      f[3] = log2f(1.f + (float)(hi - lo));
-      f[4] = log2f(1.f + (nh ? (float)(rmax - rmin + KMER) : 0.f));
+      f[2] = log2f(1.f + (float)S.nd[c]);
+      f[3] = log2f(1.f + (float)S.spread[c]);
+      f[4] = log2f(1.f + (nh ? (float)(S.rmx[c] - S.rmn[c] + KMER) : 0.f));
       f[5] = (float)L;
       f[6] = meanq;
       f[7] = 10.f;
       f[8] = 0.f;
       f[9] = (float)i;
       f[10] = (float)nout;
-      f[11] = nh ? (float)l2s / (float)nh : 0.f;
+      f[11] = nh ? (float)S.l2s[c] / (float)nh : 0.f;
     }
   }
   if (threadIdx.x == 0) {
@@ -619,20 +686,20 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   __syncthreads();
 }
 
-// Reads of h_lo < H <= h_hi hits (h_hi <= T) from the per-read buffer. The
-// table sits in shared memory, or with GT in the block's slab; FEAT adds the
-// candidate ranker's features.
+// Reads of h_lo < H <= h_hi hits (h_hi <= TM) from the per-read buffer. The
+// tables sit in shared memory, or with GT in the block's slab after the
+// cluster records; FEAT adds the candidate ranker's features.
 template <bool GT, bool FEAT>
-__global__ void k_cluster_bins(ClusterArgs p, uint32_t T, size_t slab_bytes) {
+__global__ void k_cluster_bins(ClusterArgs p, uint32_t TM, size_t slab_bytes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long wtmp64[32];
   __shared__ uint32_t wtmp32[32];
   __shared__ uint32_t sh_n;
+  __shared__ uint32_t sh_sel[BIN_MAX_OUT];
   unsigned char* slab = p.scratch + (size_t)blockIdx.x * slab_bytes;
-  BinScratch S;
-  S.carve(slab, T);
-  unsigned char* tab = GT ? slab + bin_scratch_bytes(T) : smem_raw;
-  unsigned char* sortbuf = GT ? tab + bin_table_bytes(T, FEAT) : smem_raw;
+  ClusterRecs S;
+  S.carve(slab, TM);
+  unsigned char* tab = GT ? slab + cluster_recs_bytes(TM) : smem_raw;
   for (uint32_t r = blockIdx.x; r < p.nr; r += gridDim.x) {
     const uint32_t H = p.hit_cnt[r];
     if (p.overflow[r]) continue;
@@ -642,41 +709,60 @@ __global__ void k_cluster_bins(ClusterArgs p, uint32_t T, size_t slab_bytes) {
         p.n_cand[r] = 0;
         if (p.total_cand) p.total_cand[r] = 0;
       }
+      if (FEAT)
+        for (uint32_t i = threadIdx.x; i < (uint32_t)MAX_CAND * RANK_FEATURES; i += blockDim.x)
+          p.feat[(size_t)r * MAX_CAND * RANK_FEATURES + i] = 0.f;
       continue;
     }
-    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, S, sortbuf, wtmp32, wtmp64, sh_n);
+    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, S, wtmp32, wtmp64, sh_n, sh_sel);
   }
 }
 
+static uint32_t bins_tmax(uint32_t hmax) { return std::max(next_pow2_host(hmax), BIN_TMIN); }
+
 size_t cluster_bins_slab_bytes(uint32_t hmax, bool table_in_slab) {
-  const uint32_t T = next_pow2_host(hmax);
-  return bin_scratch_bytes(T) + (table_in_slab ? bin_table_bytes(T, true) + (size_t)T * 12 : 0);
+  const uint32_t TM = bins_tmax(hmax);
+  return cluster_recs_bytes(TM) + (table_in_slab ? bin_table_bytes(TM, true) : 0);
 }
 
-size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat) {
-  // the table, later reused as sort space (12 bytes per entry)
-  const uint32_t T = next_pow2_host(hmax);
-  return std::max(bin_table_bytes(T, feat), (size_t)T * 12);
+size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat) { return bin_table_bytes(bins_tmax(hmax), feat); }
+
+template <bool GT, bool FEAT>
+static int bins_blocks_per_sm(uint32_t TM, int threads) {
+  const size_t sm = GT ? 0 : bin_table_bytes(TM, FEAT);
+  if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cluster_bins<GT, FEAT>, threads, sm) != cudaSuccess) n = 1;
+  return std::max(n, 1);
+}
+
+// Resident blocks of the binned K2 on num_sms SMs (the kernel loops over
+// reads, so its grid is what fits at once); the table-in-slab tier runs one
+// block per SM, which keeps its tables within L2.
+int cluster_bins_grid(uint32_t hmax, int threads, bool table_in_slab, bool feat, int num_sms) {
+  if (table_in_slab) return num_sms;
+  const uint32_t TM = bins_tmax(hmax);
+  return num_sms * (feat ? bins_blocks_per_sm<false, true>(TM, threads) : bins_blocks_per_sm<false, false>(TM, threads));
 }
 
 template <bool GT, bool FEAT>
-static void launch_bins(const ClusterArgs& a, uint32_t T, int threads, int grid, size_t slab, cudaStream_t st) {
-  const size_t sm = GT ? 0 : cluster_bins_smem_bytes(T, FEAT);
+static void launch_bins(const ClusterArgs& a, uint32_t TM, int threads, int grid, size_t slab, cudaStream_t st) {
+  const size_t sm = GT ? 0 : bin_table_bytes(TM, FEAT);
   if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_cluster_bins<GT, FEAT><<<grid, threads, sm, st>>>(a, T, slab);
+  k_cluster_bins<GT, FEAT><<<grid, threads, sm, st>>>(a, TM, slab);
 }
 
 void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, bool table_in_slab,
                          cudaStream_t st) {
-  const uint32_t T = next_pow2_host(hmax);
+  const uint32_t TM = bins_tmax(hmax);
   const size_t slab = cluster_bins_slab_bytes(hmax, table_in_slab);
   const bool feat = a.feat != nullptr;
   if (table_in_slab) {
-    if (feat) launch_bins<true, true>(a, T, threads, grid, slab, st);
-    else launch_bins<true, false>(a, T, threads, grid, slab, st);
+    if (feat) launch_bins<true, true>(a, TM, threads, grid, slab, st);
+    else launch_bins<true, false>(a, TM, threads, grid, slab, st);
   } else {
-    if (feat) launch_bins<false, true>(a, T, threads, grid, slab, st);
-    else launch_bins<false, false>(a, T, threads, grid, slab, st);
+    if (feat) launch_bins<false, true>(a, TM, threads, grid, slab, st);
+    else launch_bins<false, false>(a, TM, threads, grid, slab, st);
   }
 }
 

@@ -46,7 +46,8 @@ struct SeedArgs {
 };
 __host__ __device__ inline size_t seed_smem_per_warp(int lmax) {
   int W = lmax - KMER + 1 > 0 ? lmax - KMER + 1 : 1;
-  size_t s = (size_t)(4 * W + 1) * 4 + (size_t)lmax;
+  // prefix counts (lmax + 1 words of 8 bytes), then the window arrays and the codes
+  size_t s = (size_t)(lmax + 1) * 8 + (size_t)(4 * W + 1) * 4 + (size_t)lmax;
   return (s + 15) & ~(size_t)15;
 }
 void launch_seed(const SeedArgs& a, int grid, cudaStream_t st);
@@ -97,6 +98,7 @@ void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st);
 // cluster_bins_slab_bytes(hmax, table_in_slab).
 size_t cluster_bins_slab_bytes(uint32_t hmax, bool table_in_slab);
 size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat);
+int cluster_bins_grid(uint32_t hmax, int threads, bool table_in_slab, bool feat, int num_sms);
 void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, bool table_in_slab,
                          cudaStream_t st);
 uint32_t next_pow2_host(uint32_t x);

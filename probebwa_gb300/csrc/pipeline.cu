@@ -65,21 +65,24 @@ int pipeline_init(pbw_handle* h) {
 constexpr size_t OVF_SLICE_HITS = 16ull << 20;
 constexpr size_t OVF_POOL_HITS = 2 * OVF_SLICE_HITS;
 constexpr uint32_t OVF_MAX_SLICES = 16;
-// Tiers of the binned K2 (reads up to hmax hits, threads per block, blocks
-// per SM, table in the global slab).
+// Tiers of the binned K2: reads up to hmax hits (0: the per-read buffer's
+// capacity), threads per block, tables in the global slab.
 struct BinTier {
   uint32_t hmax;
-  int threads, per_sm;
+  int threads;
   bool in_slab;
 };
-constexpr BinTier BIN_TIERS[3] = {{1024, 128, 6, false}, {4096, 256, 2, false}, {0, 512, 2, true}};
+constexpr BinTier BIN_TIERS[4] = {{1024, 128, false}, {2048, 256, false}, {4096, 512, false}, {0, 1024, true}};
 static size_t cluster_scratch_bytes(const pbw_handle* h, uint32_t hcap) {
   size_t need = 0;
   uint32_t lo = 0;
   for (const BinTier& t : BIN_TIERS) {
     const uint32_t hm = t.hmax ? std::min(t.hmax, hcap) : hcap;
     if (hm <= lo) continue;
-    need = std::max(need, cluster_bins_slab_bytes(t.hmax ? t.hmax : hcap, t.in_slab) * (size_t)h->num_sms * t.per_sm);
+    const uint32_t hx = t.hmax ? t.hmax : hcap;
+    const int grid = std::max(cluster_bins_grid(hx, t.threads, t.in_slab, false, h->num_sms),
+                              cluster_bins_grid(hx, t.threads, t.in_slab, true, h->num_sms));
+    need = std::max(need, cluster_bins_slab_bytes(hx, t.in_slab) * (size_t)grid);
     lo = hm;
   }
   return need;
@@ -345,7 +348,9 @@ static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* base
     cb.h_lo = lo;
     cb.h_hi = hm;
     cb.scratch = h->d_cl_big.p;
-    launch_cluster_bins(cb, t.hmax ? t.hmax : cfg.hcap, t.threads, h->num_sms * t.per_sm, t.in_slab, st);
+    const uint32_t hx = t.hmax ? t.hmax : cfg.hcap;
+    launch_cluster_bins(cb, hx, t.threads, cluster_bins_grid(hx, t.threads, t.in_slab, feat != nullptr, h->num_sms),
+                        t.in_slab, st);
     h->stats.kernel_launches += 1;
     lo = hm;
   }
@@ -1601,6 +1606,10 @@ int pbw_cluster_batch(pbw_handle* h, const pbw_reads* reads, uint32_t max_per_re
                       uint32_t* total_cand, uint32_t* cand_contig, uint64_t* cand_pos, uint8_t* cand_strand,
                       double* cand_score) {
   if (!h || !reads || max_per_read == 0) return PBW_ERR_ARG;
+  if (max_per_read > 256) {
+    h->err = "pbw_cluster_batch: max_per_read is at most 256";
+    return PBW_ERR_LIMIT;
+  }
   cudaSetDevice(h->device);
   uint64_t total;
   int lmax;

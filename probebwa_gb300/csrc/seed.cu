@@ -42,62 +42,63 @@ __device__ __forceinline__ bool nb_probed(int rp, int L) {
   return (rp % 15) < 5;
 }
 
-// Count A/C/G/T over [s, s+n) of a code array.
-__device__ __forceinline__ void fp_read(const uint8_t* c, int s, int n, int& a, int& cc, int& g, int& t) {
-  for (int i = 0; i < n; i++) {
-    uint8_t x = c[s + i];
-    a += x == 0;
-    cc += x == 1;
-    g += x == 2;
-    t += x == 3;
-  }
-}
-
-// passes_similarity_filter (seeds.rs:162-219) for one bucket entry.
-__device__ bool similarity_ok(const DevGenome& G, const uint8_t* fwd, int L, int rp, bool rev, uint32_t cid,
-                              uint64_t ref_pos, bool neighbour) {
-  // read side, oriented like the genome (rc(read) for a reverse hit)
-  const int k = KMER;
-  int ws = rev ? L - rp - k : rp;
-  int ra_s = min(ws + k, L), ra_e = min(ra_s + 8, L);
-  int rb_e = min(ws, L), rb_s = rb_e >= 4 ? rb_e - 4 : 0;
-  // genome side
-  uint64_t clen = __ldg(&G.clen[cid]);
-  uint64_t reg_s = ref_pos >= 4 ? ref_pos - 4 : 0;
-  uint64_t reg_e = min(ref_pos + (uint64_t)k + 8, clen);
-  if (reg_s >= reg_e) return true;
-  int glen = (int)(reg_e - reg_s);
-  int gws = (int)(ref_pos - reg_s);
-  int ga_s = min(gws + k, glen), ga_e = min(ga_s + 8, glen);
-  int gb_e = min(gws, glen), gb_s = gb_e >= 4 ? gb_e - 4 : 0;
-  int after = min(ra_e - ra_s, ga_e - ga_s);
-  int before = min(rb_e - rb_s, gb_e - gb_s);
-  if (after + before < 12) return true;
-  int a = 0, c = 0, g = 0, t = 0;
+// passes_similarity_filter (seeds.rs:162-219) for one bucket entry. The
+// flanks are up to 8 bases after and 4 before the 15-mer, clipped to the
+// read and to the genome (clip_flanks); a hit whose flanks are not both whole
+// has after + before < 12 and passes. Otherwise the filter is the L1 distance
+// between the A/C/G/T counts of those 12 read bases (in the hit's
+// orientation) and of the 12 genome bases, at most 10 (8 for a neighbour
+// hit). Read counts come from the read's prefix counts (pc4: four 16-bit
+// fields A C G T per position), genome counts from the 27-base window
+// [ref_pos - 4, ref_pos + 23) read as 2-bit words, by mask and popcount, N
+// bases (the contig's N runs) counting as none of the four.
+__device__ __forceinline__ bool similarity_ok(const DevGenome& G, const unsigned long long* pc4, int L, int rp,
+                                              bool rev, uint32_t cid, uint64_t ref_pos, bool neighbour) {
+  constexpr int k = KMER;
+  const uint64_t clen = __ldg(&G.clen[cid]);
+  if (ref_pos < 4 || ref_pos + k + 8 > clen) return true;
+  unsigned long long rc;  // read counts in genome orientation
   if (!rev) {
-    fp_read(fwd, ra_s, after, a, c, g, t);
-    fp_read(fwd, rb_e - before, before, a, c, g, t);
+    if (rp < 4 || rp + k + 8 > L) return true;
+    rc = pc4[rp + k + 8] - pc4[rp + k] + pc4[rp] - pc4[rp - 4];
   } else {
-    // rc index i <-> forward index L-1-i, complemented
-    for (int i = ra_s; i < ra_s + after; i++) {
-      uint8_t x = comp_code(fwd[L - 1 - i]);
-      a += x == 0; c += x == 1; g += x == 2; t += x == 3;
+    // the reverse-complemented read's flanks: after = [rp - 8, rp) and
+    // before = [rp + 15, rp + 19) of the forward read, complemented
+    if (rp < 8 || rp + k + 4 > L) return true;
+    const unsigned long long f = pc4[rp] - pc4[rp - 8] + pc4[rp + k + 4] - pc4[rp + k];
+    rc = (f << 48) | ((f >> 16 & 0xFFFFull) << 32) | ((f >> 32 & 0xFFFFull) << 16) | (f >> 48);
+  }
+  const uint64_t gs = __ldg(&G.cbase[cid]) + ref_pos - 4;
+  const uint32_t sh = (uint32_t)(gs & 31);
+  const uint64_t wi = gs >> 5;
+  unsigned long long X = __ldg(&G.bits[wi]);
+  uint32_t NM = __ldg(&G.nmask[wi]);
+  if (sh) {
+    X >>= 2 * sh;
+    NM >>= sh;
+    if (sh > 5) {  // the window reaches into the next word
+      X |= __ldg(&G.bits[wi + 1]) << (64 - 2 * sh);
+      NM |= __ldg(&G.nmask[wi + 1]) << (32 - sh);
     }
-    for (int i = rb_e - before; i < rb_e; i++) {
-      uint8_t x = comp_code(fwd[L - 1 - i]);
-      a += x == 0; c += x == 1; g += x == 2; t += x == 3;
-    }
   }
-  uint64_t base = __ldg(&G.cbase[cid]) + reg_s;
-  for (int i = ga_s; i < ga_s + after; i++) {
-    uint8_t x = gcode(G, base + i);
-    a -= x == 0; c -= x == 1; g -= x == 2; t -= x == 3;
+  // bases 0-3 and 19-26 of the window, one bit per base at even positions
+  unsigned long long valid = 0x55ull | (0x5555ull << 38);
+  if (NM & 0x7FFFFFFu) {
+    unsigned long long n = NM;
+    n = (n | (n << 16)) & 0x0000FFFF0000FFFFull;
+    n = (n | (n << 8)) & 0x00FF00FF00FF00FFull;
+    n = (n | (n << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    n = (n | (n << 2)) & 0x3333333333333333ull;
+    n = (n | (n << 1)) & 0x5555555555555555ull;
+    valid &= ~n;
   }
-  for (int i = gb_e - before; i < gb_e; i++) {
-    uint8_t x = gcode(G, base + i);
-    a -= x == 0; c -= x == 1; g -= x == 2; t -= x == 3;
+  int d = 0;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const unsigned long long t = ~(X ^ (0x5555555555555555ull * (unsigned long long)c));
+    const int g = __popcll(t & (t >> 1) & valid);
+    d += abs((int)((rc >> (16 * c)) & 0xFFFFull) - g);
   }
-  int d = abs(a) + abs(c) + abs(g) + abs(t);
   return d <= (neighbour ? 8 : 10);
 }
 
@@ -109,7 +110,8 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
   const int W = p.lmax - KMER + 1 > 0 ? p.lmax - KMER + 1 : 1;
   const size_t per_warp = seed_smem_per_warp(p.lmax);
   unsigned char* my = smem_raw + per_warp * wib;
-  uint32_t* wcode = (uint32_t*)my;
+  unsigned long long* pc4 = (unsigned long long*)my;  // lmax + 1 prefix counts
+  uint32_t* wcode = (uint32_t*)(pc4 + p.lmax + 1);
   uint32_t* woff = wcode + W;
   uint32_t* wcnt = woff + W;
   uint32_t* iofs = wcnt + W;
@@ -136,7 +138,22 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
       continue;
     }
     const int nw = L - KMER + 1;
-    for (int i = lane; i < L; i += 32) codes[i] = base_code(p.bases[o0 + i]);
+    // base codes and their prefix counts (A C G T in four 16-bit fields)
+    unsigned long long run = 0;
+    if (lane == 0) pc4[0] = 0;
+    for (int i0 = 0; i0 < L; i0 += 32) {
+      const int i = i0 + lane;
+      const uint8_t c = i < L ? base_code(p.bases[o0 + i]) : (uint8_t)4;
+      if (i < L) codes[i] = c;
+      unsigned long long v = c < 4 ? 1ull << (16 * c) : 0ull;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += y;
+      }
+      if (i < L) pc4[i + 1] = run + v;
+      run += __shfl_sync(0xffffffffu, v, 31);
+    }
     __syncwarp();
     // exact lookups, one lane per window
     for (int w = lane; w < nw; w += 32) {
@@ -248,7 +265,7 @@ __global__ void __launch_bounds__(256) k_seed(SeedArgs p) {
           uint32_t cid = (uint32_t)((pk >> 40) & ((1ull << 23) - 1));
           uint64_t rpos = pk & ((1ull << 40) - 1);
           if (cid < p.G.ncontig) {
-            pass = similarity_ok(p.G, codes, L, s_w, rev, cid, rpos, s_nb);
+            pass = similarity_ok(p.G, pc4, L, s_w, rev, cid, rpos, s_nb);
           } else {
             pass = false;  // cannot happen with a validated index
           }
