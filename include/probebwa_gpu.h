@@ -120,6 +120,8 @@ typedef struct {
   uint64_t kernel_launches;   /* kernels launched by the call */
   uint64_t window_jobs;       /* paired path: mate rescue / shortlist cross-alignments (also in dp_jobs) */
   uint64_t window_cells;      /* their DP cells (also in dp_cells) */
+  double ms_compute;          /* device span of the mapping work, input copy and record copy excluded; the
+                                 phases above overlap in paired calls, so their sum can exceed it */
 } pbw_stats;
 
 void pbw_default_options(pbw_options* opt);

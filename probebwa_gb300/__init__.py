@@ -95,7 +95,8 @@ class StatsC(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("ms_total", "ms_h2d", "ms_seed", "ms_cluster", "ms_align", "ms_finalize",
                                            "ms_pair", "ms_d2h")] + \
                [(k, C.c_uint64) for k in ("seed_probes", "seed_entries", "seed_hits", "dp_jobs", "dp_cells",
-                                          "kernel_launches", "window_jobs", "window_cells")]
+                                          "kernel_launches", "window_jobs", "window_cells")] + \
+               [("ms_compute", C.c_double)]
 
 
 _lib = None

@@ -352,7 +352,8 @@ __global__ void k_cluster_list(ClusterArgs p) {
 //   D. the reference's final stable sort orders clusters by (count desc,
 //      group rank, diagonal order); the key (0x7FFF - count) << 49 | rank
 //      << 35 | first bin is unique per cluster, and only the first max_out
-//      are needed: they are picked by repeated block-wide minima.
+//      are needed: a radix select finds the max_out-th key and the keys up
+//      to it are sorted.
 // With the candidate ranker, bins and clusters also carry each candidate's
 // seed features (exact hits, bucket sizes, read positions).
 // ---------------------------------------------------------------------------
@@ -362,14 +363,30 @@ constexpr uint32_t GRP_EMPTY = 0xFFFFFFFFu;  // group keys (contig << 1 | strand
 constexpr uint32_t NO_SLOT = 0xFFFFFFFFu;
 constexpr unsigned long long M40 = (1ull << 40) - 1;
 constexpr unsigned long long M35 = (1ull << 35) - 1;
-constexpr uint32_t BIN_TMIN = 64;  // smallest table (room for the SwissTable replay's scratch)
+// smallest bin table: room, after the cluster keys, for the selection
+// (Tb + 384 of the bin region's 3Tb words)
+constexpr uint32_t BIN_TMIN = 256;
 constexpr uint32_t BIN_MAX_OUT = 256;  // candidates one read may return
+
+// Table sizes of a read of H hits: bins at load <= 0.625 (a read's hits are
+// mostly in bins of their own, and probe runs of a fuller open-addressed
+// table grow fast), groups in a power of two at least as large.
+__host__ __device__ inline uint32_t np2(uint32_t x) {
+  uint32_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+__host__ __device__ inline uint32_t bin_tsize(uint32_t H) {
+  const uint32_t t = ((uint32_t)(((uint64_t)H * 8 + 4) / 5) + 31) & ~31u;
+  return t < BIN_TMIN ? BIN_TMIN : t;
+}
+__host__ __device__ inline uint32_t grp_tsize(uint32_t H) { return np2(bin_tsize(H)); }
 
 __device__ __forceinline__ uint32_t hash_slot(unsigned long long key, uint32_t T) {
   unsigned long long k = key ^ (key >> 33);
   k *= 0xff51afd7ed558ccdull;
   k ^= k >> 33;
-  return (uint32_t)k & (T - 1);
+  return (uint32_t)(((k & 0xFFFFFFFFull) * T) >> 32);  // any T
 }
 
 // Slot of key in an open-addressed table of T (a power of two) 64-bit keys,
@@ -383,7 +400,7 @@ __device__ __forceinline__ uint32_t insert64(unsigned long long* keys, unsigned 
       const unsigned long long prev = atomicCAS(&keys[s], BIN_EMPTY, key);
       if (prev == BIN_EMPTY || prev == key) return s;
     }
-    s = (s + 1) & (T - 1);
+    s = s + 1 < T ? s + 1 : 0;
   }
   return NO_SLOT;
 }
@@ -393,7 +410,7 @@ __device__ __forceinline__ uint32_t find64(const unsigned long long* keys, unsig
     const unsigned long long cur = keys[s];
     if (cur == key) return s;
     if (cur == BIN_EMPTY) return NO_SLOT;
-    s = (s + 1) & (T - 1);
+    s = s + 1 < T ? s + 1 : 0;
   }
   return NO_SLOT;
 }
@@ -406,7 +423,7 @@ __device__ __forceinline__ uint32_t insert32(uint32_t* keys, uint32_t key, uint3
       const uint32_t prev = atomicCAS(&keys[s], GRP_EMPTY, key);
       if (prev == GRP_EMPTY || prev == key) return s;
     }
-    s = (s + 1) & (T - 1);
+    s = s + 1 < T ? s + 1 : 0;
   }
   return NO_SLOT;
 }
@@ -416,16 +433,17 @@ __device__ __forceinline__ uint32_t find32(const uint32_t* keys, uint32_t key, u
     const uint32_t cur = keys[s];
     if (cur == key) return s;
     if (cur == GRP_EMPTY) return NO_SLOT;
-    s = (s + 1) & (T - 1);
+    s = s + 1 < T ? s + 1 : 0;
   }
   return NO_SLOT;
 }
 
-// Tables of one read with T entries: bins (key, count << 40 | offset sum,
-// diagonal mask; with the ranker also exact hits << 32 | bucket-size sum and
-// the read-position range) and groups (key, first emission then rank).
-__host__ __device__ inline size_t bin_table_bytes(uint32_t T, bool feat) {
-  return (size_t)T * ((feat ? 40 : 24) + 8);
+// Tables of one read of up to hmax hits: bins (key, count << 40 | offset
+// sum, diagonal mask; with the ranker also exact hits << 32 | bucket-size
+// sum and the read-position range) and groups (key, first emission then
+// rank).
+__host__ __device__ inline size_t bin_table_bytes(uint32_t hmax, bool feat) {
+  return (size_t)bin_tsize(hmax) * (feat ? 40 : 24) + (size_t)grp_tsize(hmax) * 8;
 }
 // Per-block cluster records in the global slab (TM entries each): diagonal
 // sum, first bin, count, group slot, group key; with the ranker exact hits,
@@ -434,25 +452,27 @@ __host__ __device__ inline size_t bin_table_bytes(uint32_t T, bool feat) {
 struct ClusterRecs {
   unsigned long long *sum, *b0;
   uint32_t *cnt, *gslot, *gk, *ne, *l2s, *nd, *rmn, *rmx, *spread, *slots;
-  __device__ void carve(unsigned char* base, uint32_t TM) {
+  __device__ void carve(unsigned char* base, uint32_t hmax) {
+    const uint32_t TM = bin_tsize(hmax);
     unsigned long long* q = (unsigned long long*)base;
     sum = q;
     b0 = q + TM;
     uint32_t* u = (uint32_t*)(q + 2 * TM);
     cnt = u; gslot = u + TM; gk = u + 2 * TM; ne = u + 3 * TM; l2s = u + 4 * TM; nd = u + 5 * TM;
     rmn = u + 6 * TM; rmx = u + 7 * TM; spread = u + 8 * TM;
-    slots = u + 9 * TM;  // 2 * TM
+    slots = u + 9 * TM;  // 2 * grp_tsize(hmax)
   }
 };
-__host__ __device__ inline size_t cluster_recs_bytes(uint32_t TM) {
-  return ((size_t)TM * (2 * 8 + 11 * 4) + 255) & ~(size_t)255;
+__host__ __device__ inline size_t cluster_recs_bytes(uint32_t hmax) {
+  return ((size_t)bin_tsize(hmax) * (2 * 8 + 9 * 4) + (size_t)grp_tsize(hmax) * 8 + 255) & ~(size_t)255;
 }
 
 template <bool FEAT>
 __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
                                   unsigned char* tab, const ClusterRecs& S, uint32_t* wtmp32,
-                                  unsigned long long* wtmp64, uint32_t& sh_n, uint32_t* sh_sel) {
-  const uint32_t T = max(next_pow2(H), BIN_TMIN);  // >= the bins and the groups of the read
+                                  unsigned long long* wtmp64, uint32_t& sh_n, uint32_t* sh_sel, uint32_t* sh_hist) {
+  const uint32_t T = bin_tsize(H);   // bin slots (the bins and clusters of the read <= H)
+  const uint32_t TG = grp_tsize(H);  // group slots
   unsigned long long* bkey = (unsigned long long*)tab;
   unsigned long long* bacc = bkey + T;
   unsigned long long* bmask = bacc + T;
@@ -460,13 +480,15 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   uint32_t* brmn = (uint32_t*)(bmask + (FEAT ? 2 : 1) * T);     // FEAT
   uint32_t* brmx = brmn + T;                                    // FEAT
   uint32_t* gkey = (uint32_t*)tab + (FEAT ? 10 : 6) * T;
-  uint32_t* gval = gkey + T;
+  uint32_t* gval = gkey + TG;
+  for (uint32_t s = threadIdx.x; s < TG; s += blockDim.x) {
+    gkey[s] = GRP_EMPTY;
+    gval[s] = 0xFFFFFFFFu;
+  }
   for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
     bkey[s] = BIN_EMPTY;
     bacc[s] = 0;
     bmask[s] = 0;
-    gkey[s] = GRP_EMPTY;
-    gval[s] = 0xFFFFFFFFu;
     if (FEAT) {
       binf[s] = 0;
       brmn[s] = 0xFFFFFFFFu;
@@ -483,7 +505,7 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     const uint32_t off = (uint32_t)(d - b * BIN_W);
     const uint32_t gk = (uint32_t)(w >> 40);
     const uint32_t s = insert64(bkey, ((unsigned long long)gk << 35) | b, T);
-    const uint32_t g = insert32(gkey, gk, T);
+    const uint32_t g = insert32(gkey, gk, TG);
     if (s == NO_SLOT || g == NO_SLOT) {
       atomicExch(p.err, 1);
       continue;
@@ -543,7 +565,7 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     S.sum[k] = sum;
     S.b0[k] = b;
     S.gk[k] = gk;
-    S.gslot[k] = find32(gkey, gk, T);
+    S.gslot[k] = find32(gkey, gk, TG);
     if (FEAT) {
       S.ne[k] = ne;
       S.l2s[k] = l2s;
@@ -557,12 +579,12 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   const uint32_t C = sh_n;
   // C. groups in first-emission order, SwissTable replay (the bin table's
   // space holds the sort); gval becomes the group's iteration rank
-  unsigned long long* okey = bkey;
-  uint32_t* oval = (uint32_t*)(bkey + T);
+  unsigned long long* okey = bkey;               // ng <= TG <= 2T words
+  uint32_t* oval = (uint32_t*)(bkey + 2 * T);    // ng <= 2T half-words
   __syncthreads();
   if (threadIdx.x == 0) sh_n = 0;
   __syncthreads();
-  for (uint32_t g = threadIdx.x; g < T; g += blockDim.x) {
+  for (uint32_t g = threadIdx.x; g < TG; g += blockDim.x) {
     if (gkey[g] == GRP_EMPTY) continue;
     const uint32_t k = atomicAdd(&sh_n, 1u);
     okey[k] = ((unsigned long long)gval[g] << 32) | g;
@@ -587,45 +609,77 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   __syncthreads();
   const uint32_t nout = min(min(C, p.max_out), BIN_MAX_OUT);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  unsigned long long last = 0;
-  for (uint32_t o = 0; o < nout; o++) {
-    unsigned long long best = ~0ull;
-    uint32_t bi = 0;
-    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-      const unsigned long long v = ck[c];
-      if ((o == 0 || v > last) && v < best) {
-        best = v;
-        bi = c;
+  // the nout-th smallest key by an MSB-first radix select (8 bits a pass);
+  // the keys are unique, so exactly nout keys are <= it
+  unsigned long long prefix = 0, pmask = 0;
+  if (nout < C) {
+    uint32_t need = nout;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+      for (uint32_t q = threadIdx.x; q < 256; q += blockDim.x) sh_hist[q] = 0;
+      __syncthreads();
+      for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+        const unsigned long long v = ck[c];
+        if ((v & pmask) == prefix) atomicAdd(&sh_hist[(v >> shift) & 255u], 1u);
       }
-    }
-    for (int d = 16; d; d >>= 1) {
-      const unsigned long long ov = __shfl_xor_sync(0xffffffffu, best, d);
-      const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, d);
-      if (ov < best) {
-        best = ov;
-        bi = oi;
-      }
-    }
-    if (lane == 0) {
-      wtmp64[wid] = best;
-      wtmp32[wid] = bi;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned long long bv = wtmp64[0];
-      uint32_t bx = wtmp32[0];
-      for (int w2 = 1; w2 < nw; w2++)
-        if (wtmp64[w2] < bv) {
-          bv = wtmp64[w2];
-          bx = wtmp32[w2];
+      __syncthreads();
+      if (wid == 0) {
+        // warp scan over 256 bins, 8 per lane
+        uint32_t loc[8], tot = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          loc[q] = sh_hist[lane * 8 + q];
+          tot += loc[q];
         }
-      sh_sel[o] = bx;
-      wtmp64[0] = bv;
+        uint32_t incl = tot;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+          if (lane >= d) incl += y;
+        }
+        uint32_t before = incl - tot;
+        if (before < need && need <= incl) {
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            if (before < need && need <= before + loc[q]) {
+              wtmp32[0] = (uint32_t)(lane * 8 + q);
+              wtmp32[1] = need - before;
+            }
+            before += loc[q];
+          }
+        }
+      }
+      __syncthreads();
+      prefix |= (unsigned long long)wtmp32[0] << shift;
+      pmask |= 255ull << shift;
+      need = wtmp32[1];
+      __syncthreads();
     }
-    __syncthreads();
-    last = wtmp64[0];
-    __syncthreads();
+  } else {
+    prefix = ~0ull;
   }
+  // the selected keys, sorted (at most BIN_MAX_OUT of them)
+  if (threadIdx.x == 0) sh_n = 0;
+  __syncthreads();
+  unsigned long long* selk = ck + T;
+  uint32_t* selv = (uint32_t*)(selk + BIN_MAX_OUT);
+  for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+    const unsigned long long v = ck[c];
+    if (v <= prefix) {
+      const uint32_t q = atomicAdd(&sh_n, 1u);
+      if (q < BIN_MAX_OUT) {
+        selk[q] = v;
+        selv[q] = c;
+      }
+    }
+  }
+  __syncthreads();
+  const uint32_t ns = next_pow2(nout);
+  for (uint32_t q = threadIdx.x; q < ns; q += blockDim.x)
+    if (q >= nout) selk[q] = ~0ull;
+  __syncthreads();
+  bitonic_kv(selk, selv, ns);
+  for (uint32_t q = threadIdx.x; q < nout; q += blockDim.x) sh_sel[q] = selv[q];
+  __syncthreads();
   const uint64_t rg = (uint64_t)p.r0 + r;
   const long long L = (long long)(p.offs[rg + 1] - p.offs[rg]);
   for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
@@ -690,16 +744,17 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
 // tables sit in shared memory, or with GT in the block's slab after the
 // cluster records; FEAT adds the candidate ranker's features.
 template <bool GT, bool FEAT>
-__global__ void k_cluster_bins(ClusterArgs p, uint32_t TM, size_t slab_bytes) {
+__global__ void k_cluster_bins(ClusterArgs p, uint32_t hmax, size_t slab_bytes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long wtmp64[32];
   __shared__ uint32_t wtmp32[32];
   __shared__ uint32_t sh_n;
   __shared__ uint32_t sh_sel[BIN_MAX_OUT];
+  __shared__ uint32_t sh_hist[256];
   unsigned char* slab = p.scratch + (size_t)blockIdx.x * slab_bytes;
   ClusterRecs S;
-  S.carve(slab, TM);
-  unsigned char* tab = GT ? slab + cluster_recs_bytes(TM) : smem_raw;
+  S.carve(slab, hmax);
+  unsigned char* tab = GT ? slab + cluster_recs_bytes(hmax) : smem_raw;
   for (uint32_t r = blockIdx.x; r < p.nr; r += gridDim.x) {
     const uint32_t H = p.hit_cnt[r];
     if (p.overflow[r]) continue;
@@ -714,22 +769,23 @@ __global__ void k_cluster_bins(ClusterArgs p, uint32_t TM, size_t slab_bytes) {
           p.feat[(size_t)r * MAX_CAND * RANK_FEATURES + i] = 0.f;
       continue;
     }
-    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, S, wtmp32, wtmp64, sh_n, sh_sel);
+    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, S, wtmp32, wtmp64, sh_n, sh_sel, sh_hist);
   }
 }
 
-static uint32_t bins_tmax(uint32_t hmax) { return std::max(next_pow2_host(hmax), BIN_TMIN); }
-
 size_t cluster_bins_slab_bytes(uint32_t hmax, bool table_in_slab) {
-  const uint32_t TM = bins_tmax(hmax);
-  return cluster_recs_bytes(TM) + (table_in_slab ? bin_table_bytes(TM, true) : 0);
+  return cluster_recs_bytes(hmax) + (table_in_slab ? bin_table_bytes(hmax, true) : 0);
 }
 
-size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat) { return bin_table_bytes(bins_tmax(hmax), feat); }
+size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat) { return bin_table_bytes(hmax, feat); }
+
+// Whether a tier's tables go to the global slab: more than one block's
+// shared memory.
+bool cluster_bins_in_slab(uint32_t hmax, bool feat) { return bin_table_bytes(hmax, feat) > 220 * 1024; }
 
 template <bool GT, bool FEAT>
-static int bins_blocks_per_sm(uint32_t TM, int threads) {
-  const size_t sm = GT ? 0 : bin_table_bytes(TM, FEAT);
+static int bins_blocks_per_sm(uint32_t hmax, int threads) {
+  const size_t sm = GT ? 0 : bin_table_bytes(hmax, FEAT);
   if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cluster_bins<GT, FEAT>, threads, sm) != cudaSuccess) n = 1;
@@ -738,31 +794,30 @@ static int bins_blocks_per_sm(uint32_t TM, int threads) {
 
 // Resident blocks of the binned K2 on num_sms SMs (the kernel loops over
 // reads, so its grid is what fits at once); the table-in-slab tier runs one
-// block per SM, which keeps its tables within L2.
-int cluster_bins_grid(uint32_t hmax, int threads, bool table_in_slab, bool feat, int num_sms) {
-  if (table_in_slab) return num_sms;
-  const uint32_t TM = bins_tmax(hmax);
-  return num_sms * (feat ? bins_blocks_per_sm<false, true>(TM, threads) : bins_blocks_per_sm<false, false>(TM, threads));
+// block per SM.
+int cluster_bins_grid(uint32_t hmax, int threads, bool feat, int num_sms) {
+  if (cluster_bins_in_slab(hmax, feat)) return num_sms;
+  return num_sms * (feat ? bins_blocks_per_sm<false, true>(hmax, threads)
+                         : bins_blocks_per_sm<false, false>(hmax, threads));
 }
 
 template <bool GT, bool FEAT>
-static void launch_bins(const ClusterArgs& a, uint32_t TM, int threads, int grid, size_t slab, cudaStream_t st) {
-  const size_t sm = GT ? 0 : bin_table_bytes(TM, FEAT);
+static void launch_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, size_t slab, cudaStream_t st) {
+  const size_t sm = GT ? 0 : bin_table_bytes(hmax, FEAT);
   if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_cluster_bins<GT, FEAT><<<grid, threads, sm, st>>>(a, TM, slab);
+  k_cluster_bins<GT, FEAT><<<grid, threads, sm, st>>>(a, hmax, slab);
 }
 
-void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, bool table_in_slab,
-                         cudaStream_t st) {
-  const uint32_t TM = bins_tmax(hmax);
-  const size_t slab = cluster_bins_slab_bytes(hmax, table_in_slab);
+void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, cudaStream_t st) {
   const bool feat = a.feat != nullptr;
-  if (table_in_slab) {
-    if (feat) launch_bins<true, true>(a, TM, threads, grid, slab, st);
-    else launch_bins<true, false>(a, TM, threads, grid, slab, st);
+  const bool gt = cluster_bins_in_slab(hmax, feat);
+  const size_t slab = cluster_bins_slab_bytes(hmax, gt);
+  if (gt) {
+    if (feat) launch_bins<true, true>(a, hmax, threads, grid, slab, st);
+    else launch_bins<true, false>(a, hmax, threads, grid, slab, st);
   } else {
-    if (feat) launch_bins<false, true>(a, TM, threads, grid, slab, st);
-    else launch_bins<false, false>(a, TM, threads, grid, slab, st);
+    if (feat) launch_bins<false, true>(a, hmax, threads, grid, slab, st);
+    else launch_bins<false, false>(a, hmax, threads, grid, slab, st);
   }
 }
 

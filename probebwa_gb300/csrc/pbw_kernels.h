@@ -93,14 +93,15 @@ struct ClusterArgs {
 };
 void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st);
 // K2 by diagonal bins (no sort of the hits; cluster.cu) for reads of
-// h_lo < H <= h_hi <= hmax hits: the bin table in shared memory, or with
-// table_in_slab in a.scratch, which holds grid slabs of
-// cluster_bins_slab_bytes(hmax, table_in_slab).
+// h_lo < H <= h_hi <= hmax hits, one block per read: the tables in shared
+// memory, or, when they do not fit (cluster_bins_in_slab), in a.scratch.
+// a.scratch holds grid slabs of cluster_bins_slab_bytes(hmax, in_slab);
+// the grid is cluster_bins_grid (the blocks that are resident at once).
 size_t cluster_bins_slab_bytes(uint32_t hmax, bool table_in_slab);
 size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat);
-int cluster_bins_grid(uint32_t hmax, int threads, bool table_in_slab, bool feat, int num_sms);
-void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, bool table_in_slab,
-                         cudaStream_t st);
+bool cluster_bins_in_slab(uint32_t hmax, bool feat);
+int cluster_bins_grid(uint32_t hmax, int threads, bool feat, int num_sms);
+void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, cudaStream_t st);
 uint32_t next_pow2_host(uint32_t x);
 void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st);
 // Exclusive offsets of the listed (over-capacity) reads' hit counts, their

@@ -96,6 +96,7 @@ struct pbw_handle {
   pbw::DevBuf<unsigned long long> d_cnt64;  // 0 probes, 1 entries, 2 hits, 3 dp jobs, 4 dp cells
   pbw::DevBuf<unsigned int> d_scan_sums;
   pbw::DevBuf<unsigned char> d_tb_global;
+  pbw::DevBuf<unsigned char> d_tb_pair;  // the pair batches' window-DP traceback slab
   // reads with more seed hits than the per-read capacity
   pbw::DevBuf<uint32_t> d_need, d_ovf_list;
   pbw::DevBuf<unsigned long long> d_list_hoff, d_hits_pool;
@@ -160,12 +161,14 @@ struct pbw_handle {
   std::vector<cudaEvent_t> events;
   // paired calls: reads go up on a copy stream, one event per super-chunk
   cudaStream_t st_up = nullptr;
+  cudaStream_t st_pair = nullptr;  // paired calls: the pair batches, beside the next super-chunk's seeding
   std::vector<cudaEvent_t> up_ev;
   pbw_stats stats{};
   ~pbw_handle() {
     for (auto e : events) cudaEventDestroy(e);
     for (auto e : up_ev) cudaEventDestroy(e);
     if (st_up) cudaStreamDestroy(st_up);
+    if (st_pair) cudaStreamDestroy(st_pair);
     if (st) cudaStreamDestroy(st);
   }
 };

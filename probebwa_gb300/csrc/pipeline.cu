@@ -48,7 +48,7 @@ static int grow(pbw_handle* h, DevBuf<T>& b, size_t n) {
 int pipeline_init(pbw_handle* h) {
   TRY(grow(h, h->d_cnt32, 16));
   TRY(grow(h, h->d_cnt64, 16));
-  for (int i = 0; i < 32; i++) {
+  for (int i = 0; i < 64; i++) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     h->events.push_back(e);
@@ -66,13 +66,13 @@ constexpr size_t OVF_SLICE_HITS = 16ull << 20;
 constexpr size_t OVF_POOL_HITS = 2 * OVF_SLICE_HITS;
 constexpr uint32_t OVF_MAX_SLICES = 16;
 // Tiers of the binned K2: reads up to hmax hits (0: the per-read buffer's
-// capacity), threads per block, tables in the global slab.
+// capacity) and threads per block; a tier whose tables do not fit shared
+// memory keeps them in the global slab.
 struct BinTier {
   uint32_t hmax;
   int threads;
-  bool in_slab;
 };
-constexpr BinTier BIN_TIERS[4] = {{1024, 128, false}, {2048, 256, false}, {4096, 512, false}, {0, 1024, true}};
+constexpr BinTier BIN_TIERS[5] = {{512, 128}, {1024, 256}, {2048, 512}, {4096, 1024}, {0, 1024}};
 static size_t cluster_scratch_bytes(const pbw_handle* h, uint32_t hcap) {
   size_t need = 0;
   uint32_t lo = 0;
@@ -80,9 +80,11 @@ static size_t cluster_scratch_bytes(const pbw_handle* h, uint32_t hcap) {
     const uint32_t hm = t.hmax ? std::min(t.hmax, hcap) : hcap;
     if (hm <= lo) continue;
     const uint32_t hx = t.hmax ? t.hmax : hcap;
-    const int grid = std::max(cluster_bins_grid(hx, t.threads, t.in_slab, false, h->num_sms),
-                              cluster_bins_grid(hx, t.threads, t.in_slab, true, h->num_sms));
-    need = std::max(need, cluster_bins_slab_bytes(hx, t.in_slab) * (size_t)grid);
+    for (const bool feat : {false, true}) {
+      const bool gt = cluster_bins_in_slab(hx, feat);
+      need = std::max(need, cluster_bins_slab_bytes(hx, gt) * (size_t)cluster_bins_grid(hx, t.threads, feat,
+                                                                                       h->num_sms));
+    }
     lo = hm;
   }
   return need;
@@ -200,6 +202,10 @@ struct MateBufs {
   AlnOut* aln;
   uint8_t* rep;
   uint8_t mate;
+  // CIGAR overflow pool and its cursor (none: the handle's pool and cnt32[2])
+  uint32_t* pool = nullptr;
+  unsigned int* pool_used = nullptr;
+  uint32_t pool_cap = 0;
 };
 
 // Ranker buffers of one chunk (ranked or collecting map calls).
@@ -349,8 +355,7 @@ static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* base
     cb.h_hi = hm;
     cb.scratch = h->d_cl_big.p;
     const uint32_t hx = t.hmax ? t.hmax : cfg.hcap;
-    launch_cluster_bins(cb, hx, t.threads, cluster_bins_grid(hx, t.threads, t.in_slab, feat != nullptr, h->num_sms),
-                        t.in_slab, st);
+    launch_cluster_bins(cb, hx, t.threads, cluster_bins_grid(hx, t.threads, feat != nullptr, h->num_sms), st);
     h->stats.kernel_launches += 1;
     lo = hm;
   }
@@ -434,13 +439,13 @@ static int band_dp(pbw_handle* h, const AlignArgs& aa, const ChunkCfg& cfg) {
   unsigned long long* c64 = h->d_cnt64.p;
   cudaEvent_t* e = &h->events[24];
   // snapshot: CIGAR pool cursor, DP job and cell counters
-  CK(cudaMemcpyAsync(c32 + 12, c32 + 2, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c32 + 12, aa.cig_pool_used, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(c64 + 12, c64 + 3, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
   CK(cudaEventRecord(e[0], st));
   launch_align_band_lanes(aa, h->num_sms, band, 8, st);
   CK(cudaEventRecord(e[1], st));
   CK(cudaMemsetAsync(aa.next_job, 0, sizeof(unsigned int), st));
-  CK(cudaMemcpyAsync(c32 + 2, c32 + 12, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(aa.cig_pool_used, c32 + 12, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(c64 + 3, c64 + 12, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
   CK(cudaEventRecord(e[2], st));
   launch_align_band_lanes(aa, h->num_sms, band, 16, st);
@@ -463,7 +468,11 @@ static int align_candidates(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* b
                             bool reset_pool, bool prune, uint8_t* labels) {
   cudaStream_t st = h->st;
   unsigned int* c32 = h->d_cnt32.p;
-  CK(cudaMemsetAsync(c32, 0, (reset_pool ? 3 : 2) * sizeof(unsigned int), st));  // n_jobs, next_job[, cig_pool_used]
+  uint32_t* pool = mb.pool ? mb.pool : h->d_cig_pool.p;
+  unsigned int* pool_used = mb.pool ? mb.pool_used : c32 + 2;
+  const uint32_t pool_cap = mb.pool ? mb.pool_cap : (uint32_t)h->d_cig_pool.cap;
+  CK(cudaMemsetAsync(c32, 0, 2 * sizeof(unsigned int), st));  // n_jobs, next_job
+  if (reset_pool) CK(cudaMemsetAsync(pool_used, 0, sizeof(unsigned int), st));
   MakeJobsArgs ma{};
   ma.G = h->G;
   ma.offs = offs;
@@ -496,9 +505,9 @@ static int align_candidates(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* b
   aa.n_jobs = c32 + 0;
   aa.next_job = c32 + 1;
   aa.out = mb.aln;
-  aa.cig_pool = h->d_cig_pool.p;
-  aa.cig_pool_used = c32 + 2;
-  aa.cig_pool_cap = (uint32_t)h->d_cig_pool.cap;
+  aa.cig_pool = pool;
+  aa.cig_pool_used = pool_used;
+  aa.cig_pool_cap = pool_cap;
   aa.ref_bytes = nullptr;
   aa.lmax = cfg.lmax;
   aa.nmax = cfg.nmax;
@@ -731,6 +740,7 @@ static int map_single_dev(pbw_handle* h, const uint8_t* d_bases, const uint8_t* 
   CK(cudaEventRecord(e2, h->st));
   CK(cudaStreamSynchronize(h->st));
   h->stats.ms_d2h = ms_between(e1, e2);
+  h->stats.ms_compute = ms_between(e0, e1);
   return PBW_OK;
 }
 
@@ -794,6 +804,8 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
                           uint64_t tot1, uint64_t tot2, int lmax, pbw_records* o1, pbw_records* o2,
                           const std::vector<cudaEvent_t>* up_ev) {
   cudaStream_t st = h->st;
+  if (!h->st_pair) CK(cudaStreamCreateWithFlags(&h->st_pair, cudaStreamNonBlocking));
+  cudaStream_t sp = h->st_pair;
   const auto batches = pair_batches(n);
   // super-chunks: whole batches, at most chunk_reads pairs
   const uint64_t S = pair_super_chunk_pairs(h);
@@ -807,18 +819,26 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   TRY(ensure_chunk(h, cfg));
   if (h->rk.enabled || h->rk.collect) TRY(ensure_ranker_chunk(h, cfg));
   const uint32_t ch = cfg.ch;
-  TRY(grow(h, h->d_cand2, (size_t)ch * MAX_CAND));
-  TRY(grow(h, h->d_n_cand2, ch));
-  TRY(grow(h, h->d_aln2, (size_t)ch * MAX_CAND));
-  TRY(grow(h, h->d_rep2, (size_t)ch * cfg.wcap));
-  TRY(grow(h, h->d_sum, 2 * (size_t)ch));
+  // Two buffer sets: super-chunk k's candidates, alignments, repeat marks,
+  // read summaries and CIGAR pool live in set k % 2, so that k + 1 can be
+  // seeded and aligned (stream st) while k's pair batches run (stream sp).
+  const size_t pool_ops = (size_t)ch * (2 * MAX_CAND + MAX_CROSS) * 16 + 4096;
+  TRY(grow(h, h->d_cand, 2 * (size_t)ch * MAX_CAND));
+  TRY(grow(h, h->d_n_cand, 2 * (size_t)ch));
+  TRY(grow(h, h->d_aln, 2 * (size_t)ch * MAX_CAND));
+  TRY(grow(h, h->d_rep, 2 * (size_t)ch * cfg.wcap));
+  TRY(grow(h, h->d_cand2, 2 * (size_t)ch * MAX_CAND));
+  TRY(grow(h, h->d_n_cand2, 2 * (size_t)ch));
+  TRY(grow(h, h->d_aln2, 2 * (size_t)ch * MAX_CAND));
+  TRY(grow(h, h->d_rep2, 2 * (size_t)ch * cfg.wcap));
+  TRY(grow(h, h->d_sum, 4 * (size_t)ch));
+  TRY(grow(h, h->d_cig_pool, 2 * pool_ops));
   TRY(grow(h, h->d_work, ch));
   TRY(grow(h, h->d_xout, (size_t)ch * MAX_CROSS));
   TRY(grow(h, h->d_xmeta, (size_t)ch * MAX_CROSS));
   TRY(grow(h, h->d_xjobs, (size_t)2000 * MAX_CROSS));
   TRY(grow(h, h->d_obs, ch));
   TRY(grow(h, h->d_model, 1));
-  TRY(grow(h, h->d_cig_pool, (size_t)ch * (2 * MAX_CAND + MAX_CROSS) * 16 + 4096));
   const uint64_t n2 = 2 * n;
   TRY(ensure_outputs(h, std::max<uint64_t>(n2, 1), 2 * tot1 + 2 * n + 16));
   TRY(grow(h, h->o_cig_off2, n + 1));
@@ -828,7 +848,9 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   // wide DP: window = L + 2 * (ceil(5 sd) + L); slabs sized for 8192 columns
   const int wide_n = 8192;
   const int grid_w = window_grid(h);
-  TRY(ensure_window_slab(h, cfg.lmax, wide_n, grid_w));
+  // the pair batches' window DP has a traceback slab of its own (the next
+  // super-chunk's seeded DP uses d_tb_global meanwhile)
+  TRY(grow(h, h->d_tb_pair, window_slab_bytes(cfg.lmax, wide_n) * (size_t)grid_w));
   PairModel pm;
   pm.mean = model->mean;
   pm.sd = model->sd;
@@ -840,55 +862,69 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   }
   PairModel* h_pm = (PairModel*)h->h_fold.p;
   double* h_obs = (double*)((char*)h->h_fold.p + sizeof(PairModel));
+  uint32_t* h_batch = (uint32_t*)((char*)h->h_fold.p + sizeof(PairModel) + 2000 * sizeof(double));
   *h_pm = pm;
+  unsigned int* c32 = h->d_cnt32.p;
   CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(pm), cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * sizeof(unsigned int), st));
+  CK(cudaMemsetAsync(c32, 0, 16 * sizeof(unsigned int), st));
   CK(cudaMemsetAsync(h->d_cnt64.p, 0, 16 * sizeof(unsigned long long), st));
-  cudaEvent_t* ev = &h->events[2];
+  // events: [0] start; per set s at 1 + 12 s: phase A of mate 1 (4), mate 2
+  // (4), pair batches start / end, gather end, phase A end
+  cudaEvent_t* E = &h->events[32];
+  auto evA1 = [&](int s) { return E + 1 + 12 * s; };
+  auto evA2 = [&](int s) { return E + 5 + 12 * s; };
+  auto evB = [&](int s) { return E + 9 + 12 * s; };  // 0 batches start, 1 batches end, 2 gather end
+  auto evAdone = [&](int s) { return E[12 + 12 * s]; };
+  CK(cudaEventRecord(E[0], st));
   double t_seed = 0, t_cl = 0, t_al = 0, t_pair = 0, t_fin = 0;
-  for (size_t sc = 0; sc < chunks.size(); sc++) {
-    const uint64_t a = chunks[sc].a, b = chunks[sc].b;
-    const size_t bi = chunks[sc].bi, be = chunks[sc].be;
-    const uint32_t nr = (uint32_t)(b - a);
-    // this super-chunk's reads are on the device
-    if (up_ev) CK(cudaStreamWaitEvent(st, (*up_ev)[sc], 0));
-    // phase A: both mates through K1-K3 and the per-read summaries
-    MateBufs m1{h->d_cand.p, h->d_n_cand.p, h->d_aln.p, h->d_rep.p, 0};
-    MateBufs m2{h->d_cand2.p, h->d_n_cand2.p, h->d_aln2.p, h->d_rep2.p, 0};
-    if (!(h->rk.enabled || h->rk.collect)) {
-      TRY(run_seed_align(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, true));
-      CK(cudaEventSynchronize(ev[3]));
-      t_seed += ms_between(ev[0], ev[1]);
-      t_cl += ms_between(ev[1], ev[2]);
-      t_al += ms_between(ev[2], ev[3]);
-      TRY(run_seed_align(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev, false));
-      CK(cudaEventSynchronize(ev[3]));
-      t_seed += ms_between(ev[0], ev[1]);
-      t_cl += ms_between(ev[1], ev[2]);
-      t_al += ms_between(ev[2], ev[3]);
+  const bool ranked = h->rk.enabled || h->rk.collect;
+  auto mates = [&](int s, MateBufs& m1, MateBufs& m2) {
+    const size_t cs = (size_t)s * ch * MAX_CAND, rs = (size_t)s * ch, ws = (size_t)s * ch * cfg.wcap;
+    m1 = MateBufs{h->d_cand.p + cs, h->d_n_cand.p + rs, h->d_aln.p + cs, h->d_rep.p + ws, 0};
+    m2 = MateBufs{h->d_cand2.p + cs, h->d_n_cand2.p + rs, h->d_aln2.p + cs, h->d_rep2.p + ws, 0};
+    m1.pool = m2.pool = h->d_cig_pool.p + (size_t)s * pool_ops;
+    m1.pool_used = m2.pool_used = c32 + (s ? 10 : 2);
+    m1.pool_cap = m2.pool_cap = (uint32_t)pool_ops;
+  };
+  auto collect_times_A = [&](int s) {
+    cudaEvent_t* e1 = evA1(s);
+    cudaEvent_t* e2 = evA2(s);
+    t_seed += ms_between(e1[0], e1[1]) + ms_between(e2[0], e2[1]);
+    t_cl += ms_between(e1[1], e1[2]) + ms_between(e2[1], e2[2]);
+    t_al += ranked ? ms_between(e2[2], e2[3]) : ms_between(e1[2], e1[3]) + ms_between(e2[2], e2[3]);
+  };
+  // phase A of super-chunk k on st: both mates through K1-K3 and the read
+  // summaries. The ranker's mate feature uses the insert model the host holds
+  // when k is enqueued (after the batches of super-chunk k - 2).
+  auto phase_A = [&](size_t k) -> int {
+    const int s = (int)(k & 1);
+    const uint64_t a = chunks[k].a;
+    const uint32_t nr = (uint32_t)(chunks[k].b - a);
+    if (up_ev) CK(cudaStreamWaitEvent(st, (*up_ev)[k], 0));
+    if (k >= 2) CK(cudaStreamWaitEvent(st, evB(s)[2], 0));  // k - 2 is done with set s
+    MateBufs m1, m2;
+    mates(s, m1, m2);
+    if (!ranked) {
+      TRY(run_seed_align(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, evA1(s), true));
+      TRY(run_seed_align(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, evA2(s), false));
     } else {
       // ranker: both read sets' candidates first (the mate features need
       // both), then pruning and the seeded DP of each read set
-      cudaEvent_t* ev2 = &h->events[10];
       float* f1 = rank_feat(h, ch, 0, (uint32_t)a);
       float* f2 = rank_feat(h, ch, 1, (uint32_t)a);
-      TRY(seed_cluster(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, f1));
-      TRY(seed_cluster(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev2, f2));
+      TRY(seed_cluster(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, evA1(s), f1));
+      TRY(seed_cluster(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, evA2(s), f2));
       rank_mate_features(h, m1, m2, of1, of2, (uint32_t)a, nr, f1, f2, h_pm->mean, h_pm->sd);
       const bool prune = h->rk.enabled && !h->rk.collect;
       if (prune) {
         rank_decide(h, f1, h->rk.d_logit.p, m1, nr);
         rank_decide(h, f2, h->rk.d_logit.p + (size_t)ch * MAX_CAND, m2, nr);
       }
-      TRY(align_candidates(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, ev, true, prune, rank_label(h, 0, (uint32_t)a)));
-      TRY(align_candidates(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, ev2, false, prune,
+      TRY(align_candidates(h, cfg, b1, q1, of1, (uint32_t)a, nr, m1, evA1(s), true, prune,
+                           rank_label(h, 0, (uint32_t)a)));
+      TRY(align_candidates(h, cfg, b2, q2, of2, (uint32_t)a, nr, m2, evA2(s), false, prune,
                            rank_label(h, 1, (uint32_t)a)));
-      CK(cudaEventSynchronize(ev2[3]));
-      t_seed += ms_between(ev[0], ev[1]) + ms_between(ev2[0], ev2[1]);
-      t_cl += ms_between(ev[1], ev[2]) + ms_between(ev2[1], ev2[2]);
-      t_al += ms_between(ev2[2], ev2[3]);
     }
-    CK(cudaEventRecord(ev[0], st));
     for (int mate = 0; mate < 2; mate++) {
       ReadSummaryArgs ra{};
       ra.tab = h->d_tab.p;
@@ -899,14 +935,29 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       ra.offs = mate ? of2 : of1;
       ra.r0 = (uint32_t)a;
       ra.nr = nr;
-      ra.aln = mate ? h->d_aln2.p : h->d_aln.p;
-      ra.n_cand = mate ? h->d_n_cand2.p : h->d_n_cand.p;
-      ra.rep = mate ? h->d_rep2.p : h->d_rep.p;
+      ra.aln = mate ? m2.aln : m1.aln;
+      ra.n_cand = mate ? m2.n_cand : m1.n_cand;
+      ra.rep = mate ? m2.rep : m1.rep;
       ra.wcap = cfg.wcap;
-      ra.sum = h->d_sum.p + (size_t)mate * ch;
+      ra.sum = h->d_sum.p + (size_t)(2 * s + mate) * ch;
       launch_read_summary(ra, st);
     }
-    // phase B: batches
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(evAdone(s), st));
+    return PBW_OK;
+  };
+  // phase B of super-chunk k on sp: the pair batches in order (each batch's
+  // observations folded into the model on the host before the next), then
+  // the super-chunk's packed CIGARs.
+  auto phase_B = [&](size_t k) -> int {
+    const int s = (int)(k & 1);
+    const uint64_t a = chunks[k].a, b = chunks[k].b;
+    const size_t bi = chunks[k].bi, be = chunks[k].be;
+    const uint32_t nr = (uint32_t)(b - a);
+    MateBufs m1, m2;
+    mates(s, m1, m2);
+    CK(cudaStreamWaitEvent(sp, evAdone(s), 0));
+    CK(cudaEventRecord(evB(s)[0], sp));
     PairArgs pa{};
     pa.G = h->G;
     pa.tab = h->d_tab.p;
@@ -916,19 +967,19 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     pa.offs1 = of1;
     pa.offs2 = of2;
     pa.read0 = (uint32_t)a;
-    pa.sum[0] = h->d_sum.p;
-    pa.sum[1] = h->d_sum.p + ch;
-    pa.aln[0] = h->d_aln.p;
-    pa.aln[1] = h->d_aln2.p;
-    pa.cand[0] = h->d_cand.p;
-    pa.cand[1] = h->d_cand2.p;
+    pa.sum[0] = h->d_sum.p + (size_t)(2 * s) * ch;
+    pa.sum[1] = h->d_sum.p + (size_t)(2 * s + 1) * ch;
+    pa.aln[0] = m1.aln;
+    pa.aln[1] = m2.aln;
+    pa.cand[0] = m1.cand;
+    pa.cand[1] = m2.cand;
     pa.work = h->d_work.p;
     pa.model = h->d_model.p;
     pa.sv_prior_log_prob = h->tab_host.sv_prior_log_prob;
     pa.gap_open = h->tab_host.gap_open;
     pa.gap_extend = h->tab_host.gap_extend;
     pa.jobs = h->d_xjobs.p;
-    pa.n_jobs = h->d_cnt32.p + 8;
+    pa.n_jobs = c32 + 8;
     pa.xout = h->d_xout.p;
     pa.xmeta = h->d_xmeta.p;
     pa.obs = h->d_obs.p;
@@ -960,17 +1011,17 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     aa.quals2 = q2;
     aa.offs2 = of2;
     aa.jobs = h->d_xjobs.p;
-    aa.n_jobs = h->d_cnt32.p + 8;
-    aa.next_job = h->d_cnt32.p + 9;
+    aa.n_jobs = c32 + 8;
+    aa.next_job = c32 + 9;
     aa.out = h->d_xout.p;
-    aa.cig_pool = h->d_cig_pool.p;
-    aa.cig_pool_used = h->d_cnt32.p + 2;
-    aa.cig_pool_cap = (uint32_t)h->d_cig_pool.cap;
+    aa.cig_pool = m1.pool;
+    aa.cig_pool_used = m1.pool_used;
+    aa.cig_pool_cap = m1.pool_cap;
     aa.ref_bytes = nullptr;
     aa.lmax = cfg.lmax;
     aa.nmax = wide_n;
     aa.tb_smem = 0;
-    aa.tb_global = h->d_tb_global.p;
+    aa.tb_global = h->d_tb_pair.p;
     aa.tb_global_per_warp = window_slab_bytes(cfg.lmax, wide_n);
     aa.counters = h->d_cnt64.p + 5;  // cross-alignment jobs and cells, apart from the seeded DP's
     aa.err = h->d_err.p;
@@ -983,7 +1034,6 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     // replayed per batch; a capture the runtime refuses falls back to the
     // launches below.
     cudaGraphExec_t gexec = nullptr;
-    uint32_t* h_batch = (uint32_t*)((char*)h->h_fold.p + sizeof(PairModel) + 2000 * sizeof(double));
     if (h->tune.pair_graphs) {
       TRY(grow(h, h->d_batch, 2));
       TRY(grow(h, h->d_obs_batch, 2000));
@@ -992,76 +1042,92 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
       pg.obs_batch = h->d_obs_batch.p;
       pg.np = 2000;
       cudaGraph_t graph = nullptr;
-      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(h->d_batch.p, h_batch, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-        cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st);
-        launch_pair_decide(pg, st);
-        launch_align_window(aa, grid_w, st, true);
-        launch_aln_stats(aa, (uint64_t)2000 * MAX_CROSS, st);
-        launch_pair_resolve(pg, st);
-        cudaMemcpyAsync(h_obs, h->d_obs_batch.p, 2000 * sizeof(double), cudaMemcpyDeviceToHost, st);
-        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+      if (cudaStreamBeginCapture(sp, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, sp);
+        cudaMemcpyAsync(h->d_batch.p, h_batch, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, sp);
+        cudaMemsetAsync(c32 + 8, 0, 2 * sizeof(unsigned int), sp);
+        launch_pair_decide(pg, sp);
+        launch_align_window(aa, grid_w, sp, true);
+        launch_aln_stats(aa, (uint64_t)2000 * MAX_CROSS, sp);
+        launch_pair_resolve(pg, sp);
+        cudaMemcpyAsync(h_obs, h->d_obs_batch.p, 2000 * sizeof(double), cudaMemcpyDeviceToHost, sp);
+        const cudaError_t ec = cudaStreamEndCapture(sp, &graph);
         if (ec != cudaSuccess || !graph || cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
         if (graph) cudaGraphDestroy(graph);
       }
       cudaGetLastError();  // a refused capture leaves no sticky error
     }
-    for (size_t k = bi; k < be; k++) {
-      pa.p0 = (uint32_t)(batches[k].first - a);
-      pa.np = (uint32_t)batches[k].second;
+    for (size_t q = bi; q < be; q++) {
+      pa.p0 = (uint32_t)(batches[q].first - a);
+      pa.np = (uint32_t)batches[q].second;
       if (gexec) {
         h_batch[0] = pa.p0;
         h_batch[1] = pa.np;
-        CK(cudaGraphLaunch(gexec, st));
-        CK(cudaStreamSynchronize(st));
+        CK(cudaGraphLaunch(gexec, sp));
+        CK(cudaStreamSynchronize(sp));
         fold_insert_model(pm, h_obs, pa.np);
         *h_pm = pm;
         h->stats.kernel_launches += 4;
         continue;
       }
-      CK(cudaMemsetAsync(h->d_cnt32.p + 8, 0, 2 * sizeof(unsigned int), st));
-      launch_pair_decide(pa, st);
+      CK(cudaMemsetAsync(c32 + 8, 0, 2 * sizeof(unsigned int), sp));
+      launch_pair_decide(pa, sp);
       const int gw = (int)std::min<uint64_t>((uint64_t)grid_w, (uint64_t)pa.np * MAX_CROSS);
-      launch_align_window(aa, std::max(gw, 1), st, true);
-      launch_aln_stats(aa, (uint64_t)pa.np * MAX_CROSS, st);
-      launch_pair_resolve(pa, st);
+      launch_align_window(aa, std::max(gw, 1), sp, true);
+      launch_aln_stats(aa, (uint64_t)pa.np * MAX_CROSS, sp);
+      launch_pair_resolve(pa, sp);
       // the next batch sees the model updated by this batch's observations
-      CK(cudaMemcpyAsync(h_obs, h->d_obs.p + pa.p0, (size_t)pa.np * sizeof(double), cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
+      CK(cudaMemcpyAsync(h_obs, h->d_obs.p + pa.p0, (size_t)pa.np * sizeof(double), cudaMemcpyDeviceToHost, sp));
+      CK(cudaStreamSynchronize(sp));
       fold_insert_model(pm, h_obs, pa.np);
       *h_pm = pm;
-      CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, sp));
       h->stats.kernel_launches += 4;
     }
     if (gexec) {
       // the model the graph path left on the host goes to the device for the
       // next super-chunk's direct launches, if any
-      CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(h->d_model.p, h_pm, sizeof(PairModel), cudaMemcpyHostToDevice, sp));
       cudaGraphExecDestroy(gexec);
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ev[1], st));
+    CK(cudaEventRecord(evB(s)[1], sp));
     // packed CIGARs of this super-chunk's records, mate 1 then mate 2
-    launch_scan_excl(h->o_nops.p + a, nr, h->o_cig_off.p + a, h->d_scan_sums.p, h->d_cnt32.p + 4, h->d_cnt32.p + 4,
-                     st);
-    launch_pair_cigar_gather(pa, h->o_cig_off.p, h->d_cig_pool.p, h->o_cigar.p, a, nr, st);
+    launch_scan_excl(h->o_nops.p + a, nr, h->o_cig_off.p + a, h->d_scan_sums.p, c32 + 4, c32 + 4, sp);
+    launch_pair_cigar_gather(pa, h->o_cig_off.p, m1.pool, h->o_cigar.p, a, nr, sp);
     // mate 2 records live at n + pair; their offsets go to o_cig_off2
     {
       PairArgs pb = pa;
       pb.o_cigsrc = h->o_cigsrc.p + n;
       pb.o_len = h->o_len.p + n;
-      launch_scan_excl(h->o_nops.p + n + a, nr, h->o_cig_off2.p + a, h->d_scan_sums.p, h->d_cnt32.p + 5,
-                       h->d_cnt32.p + 5, st);
-      launch_pair_cigar_gather(pb, h->o_cig_off2.p, h->d_cig_pool.p, h->o_cigar2.p, a, nr, st);
+      launch_scan_excl(h->o_nops.p + n + a, nr, h->o_cig_off2.p + a, h->d_scan_sums.p, c32 + 5, c32 + 5, sp);
+      launch_pair_cigar_gather(pb, h->o_cig_off2.p, m1.pool, h->o_cigar2.p, a, nr, sp);
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ev[2], st));
-    CK(cudaEventSynchronize(ev[2]));
-    t_pair += ms_between(ev[0], ev[1]);
-    t_fin += ms_between(ev[1], ev[2]);
+    CK(cudaEventRecord(evB(s)[2], sp));
+    return PBW_OK;
+  };
+  for (size_t k = 0; k < chunks.size(); k++) {
+    if (k >= 2) {
+      // the set's previous super-chunk is through both phases: its times
+      CK(cudaEventSynchronize(evB((int)(k & 1))[2]));
+      collect_times_A((int)(k & 1));
+      t_pair += ms_between(evB((int)(k & 1))[0], evB((int)(k & 1))[1]);
+      t_fin += ms_between(evB((int)(k & 1))[1], evB((int)(k & 1))[2]);
+    }
+    TRY(phase_A(k));
+    if (k >= 1) TRY(phase_B(k - 1));
   }
+  TRY(phase_B(chunks.size() - 1));
+  CK(cudaStreamSynchronize(sp));
   CK(cudaStreamSynchronize(st));
+  for (size_t k = chunks.size() >= 2 ? chunks.size() - 2 : 0; k < chunks.size(); k++) {
+    const int s = (int)(k & 1);
+    collect_times_A(s);
+    t_pair += ms_between(evB(s)[0], evB(s)[1]);
+    t_fin += ms_between(evB(s)[1], evB(s)[2]);
+  }
+  const double t_span = ms_between(E[0], evB((int)((chunks.size() - 1) & 1))[2]);
   TRY(check_device_errors(h));
   h->stats.ms_seed = t_seed;
   h->stats.ms_cluster = t_cl;
@@ -1079,15 +1145,15 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   h->stats.window_cells = c64[6];
   // outputs
   unsigned int tot[2];
-  CK(cudaMemcpy(tot, h->d_cnt32.p + 4, 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(tot, c32 + 4, 8, cudaMemcpyDeviceToHost));
   if (o1->cigar_cap < tot[0] || o2->cigar_cap < tot[1]) {
     h->err = "cigar_cap too small";
     return PBW_ERR_CAPACITY;
   }
   cudaEvent_t e1 = h->events[20], e2 = h->events[21];
   CK(cudaEventRecord(e1, st));
-  CK(cudaMemcpyAsync(h->o_cig_off.p + n, h->d_cnt32.p + 4, 4, cudaMemcpyDeviceToDevice, st));
-  CK(cudaMemcpyAsync(h->o_cig_off2.p + n, h->d_cnt32.p + 5, 4, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(h->o_cig_off.p + n, c32 + 4, 4, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(h->o_cig_off2.p + n, c32 + 5, 4, cudaMemcpyDeviceToDevice, st));
   pbw_records* outs[2] = {o1, o2};
   for (int k = 0; k < 2; k++) {
     pbw_records* o = outs[k];
@@ -1111,6 +1177,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   CK(cudaEventRecord(e2, st));
   CK(cudaStreamSynchronize(st));
   h->stats.ms_d2h = ms_between(e1, e2);
+  h->stats.ms_compute = t_span;
   model->mean = pm.mean;
   model->sd = pm.sd;
   model->n_observed = pm.n;
