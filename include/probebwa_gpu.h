@@ -341,10 +341,13 @@ int pbw_build_hash(const char* genome_prefix, const char* out_prefix, uint64_t k
  *   with a bounded spin; after this many polls (0 = the default, 2^22) the
  *   wait gives up, the call discards its results and returns PBW_ERR_DEVICE.
  *   Lowering it only serves to exercise that path.
- * ovf_slice_hits: reads with more than 4096 seed hits are seeded again into
- *   an overflow pool one slice of this many hits at a time (0 = the default,
- *   16 M; larger values are clamped to it). A chunk's over-capacity reads may
- *   hold 16 default slices in all, and one read one slice.
+ * ovf_slice_hits: reads with more seed hits than the per-read buffer holds
+ *   (4096, or 16384 when the longest read of the call exceeds 160 bases) are
+ *   seeded again into an overflow pool one slice of this many hits at a time
+ *   (0 = the default, 16 M; larger values are clamped to it). The pool and its
+ *   clustering scratch hold two slices, so a smaller slice also takes less
+ *   device memory. A chunk's over-capacity reads may hold 16 default slices in
+ *   all, and one read one slice.
  * pbw_set_tuning reads the inputs and clears the tuned choices. */
 typedef struct {
   int32_t autotune;

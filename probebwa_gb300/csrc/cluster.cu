@@ -6,21 +6,12 @@
 // at gaps > 50, emits one candidate per cluster (truncating mean diagonal),
 // then stable-sorts candidates by hit count, descending.
 //
-// Reads whose hits fit the per-read buffer take the binned form
-// (cluster_read_bins, below the shared helpers): no sort of the hits, a hash
-// table of 51-wide diagonal bins. Reads seeded into the overflow pool take
-// the sorted form (cluster_read), in global scratch:
-//   1. the read's hit words ((contig, strand) << 40 | diagonal) are sorted
-//      (bitonic, key + emission index), which makes every group contiguous
-//      with ascending diagonals;
-//   2. block scans mark group and cluster boundaries and give cluster sums;
-//   3. each group's first emission index gives the FxHashMap insertion
-//      order, and one thread replays std's SwissTable insertion for those
-//      keys (FxHasher of rustc-hash 2.1.3, probing by the group width) to get
-//      the iteration rank of every group;
-//   4. clusters are sorted by (count desc, group rank, diagonal order) --
-//      exactly the stable sort of the reference -- and the first max_out
-//      are written.
+// Every read takes the binned form (cluster_read_bins, below the shared
+// helpers): no sort of the hits, a hash table of 51-wide diagonal bins. Reads
+// within the per-read hit buffer run by hit-count tier with their tables in
+// shared memory or, for the largest tier, a per-block global slab; reads
+// seeded into the overflow pool (list mode) keep their tables in global
+// scratch beside their pooled hits.
 #include "pbw_common.cuh"
 #include "pbw_kernels.h"
 
@@ -60,39 +51,6 @@ __device__ void bitonic_kv(unsigned long long* k, uint32_t* v, uint32_t n) {
       }
       __syncthreads();
     }
-  }
-}
-
-// In-place inclusive block scan (sum) of n elements.
-template <class T>
-__device__ void block_scan_incl(T* a, uint32_t n, T* warp_tmp) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  T carry = 0;
-  for (uint32_t base = 0; base < n; base += blockDim.x) {
-    uint32_t i = base + threadIdx.x;
-    T x = i < n ? a[i] : (T)0;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      T y = __shfl_up_sync(0xffffffffu, x, d);
-      if (lane >= d) x += y;
-    }
-    if (lane == 31) warp_tmp[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-      T s = lane < nw ? warp_tmp[lane] : (T)0;
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        T y = __shfl_up_sync(0xffffffffu, s, d);
-        if (lane >= d) s += y;
-      }
-      if (lane < nw) warp_tmp[lane] = s;
-    }
-    __syncthreads();
-    T add = carry + (wid > 0 ? warp_tmp[wid - 1] : (T)0);
-    if (i < n) a[i] = x + add;
-    T tot = warp_tmp[nw - 1];
-    __syncthreads();
-    carry += tot;
   }
 }
 
@@ -178,158 +136,93 @@ __device__ bool swiss_replay(const unsigned long long* order, uint32_t G, const 
   return true;
 }
 
-uint32_t next_pow2_host(uint32_t x) {
-  uint32_t p = 1;
-  while (p < x) p <<= 1;
-  return p;
+// swiss_find by one warp: the lanes test the W buckets of a probe group (or
+// the nb buckets of a small table from pos on) at once, and the lowest empty
+// one in probe order wins.
+__device__ __forceinline__ uint32_t swiss_find_warp(const uint32_t* t, uint32_t nb, unsigned long long h, int W,
+                                                    int lane) {
+  const uint32_t mask = nb - 1;
+  uint32_t pos = (uint32_t)(h & mask);
+  if (nb <= (uint32_t)W) {
+    const bool e = (uint32_t)lane < nb && t[(pos + lane) & mask] == 0xFFFFFFFFu;
+    const unsigned b = __ballot_sync(0xffffffffu, e);
+    return b ? (pos + (uint32_t)__ffs((int)b) - 1) & mask : 0u;
+  }
+  uint32_t stride = 0;
+  for (uint32_t guard = 0; guard <= nb; guard++) {
+    const bool e = lane < W && t[(pos + lane) & mask] == 0xFFFFFFFFu;
+    const unsigned b = __ballot_sync(0xffffffffu, e);
+    if (b) return (pos + (uint32_t)__ffs((int)b) - 1) & mask;
+    stride += W;
+    pos = (pos + stride) & mask;
+  }
+  return 0xFFFFFFFFu;
+}
+
+constexpr uint32_t SWISS_WARP_SLOTS = 512;  // buckets of the shared-memory replay (groups <= 256)
+
+// swiss_replay by one warp over shared memory (all 32 lanes call it): the
+// same insertions and rehashes (old buckets in bucket order), with each
+// probe group tested by the lanes together. aux holds 1280 words: ord, the
+// group slots in insertion order (<= 256, the input), the groups' keys in
+// that order (<= 256), the buckets (cap2 <= 512, each holding an insertion
+// index) and the rehash copy of the old buckets (<= 256). rank[g] receives
+// each group's iteration position and gk_by_rank[rank] its key.
+__device__ bool swiss_replay_warp(uint32_t G, const uint32_t* ggk, uint32_t* aux, uint32_t cap2, uint32_t* rank,
+                                  uint32_t* gk_by_rank, int W, int lane) {
+  constexpr uint32_t EMPTY = 0xFFFFFFFFu;
+  const uint32_t* ord = aux;
+  uint32_t* gks = aux + 256;
+  uint32_t* slots = aux + 512;
+  uint32_t* olds = aux + 512 + SWISS_WARP_SLOTS;
+  for (uint32_t t = lane; t < G; t += 32) gks[t] = ggk[ord[t]];
+  __syncwarp();
+  uint32_t nb = 0, items = 0;
+  for (uint32_t t = 0; t < G; t++) {
+    if (items + 1 > swiss_cap(nb)) {
+      const uint32_t need = max(items + 1, swiss_cap(nb) + 1);
+      const uint32_t nnb = swiss_buckets(need);
+      if (nnb > cap2) return false;
+      for (uint32_t s = lane; s < nb; s += 32) olds[s] = slots[s];
+      __syncwarp();
+      for (uint32_t s = lane; s < nnb; s += 32) slots[s] = EMPTY;
+      __syncwarp();
+      for (uint32_t s = 0; s < nb; s++) {
+        const uint32_t ot = olds[s];
+        if (ot == EMPTY) continue;
+        const uint32_t ogk = gks[ot];
+        const uint32_t q = swiss_find_warp(slots, nnb, fx_hash_group(ogk >> 1, ogk & 1u), W, lane);
+        if (lane == 0) slots[q] = ot;
+        __syncwarp();
+      }
+      nb = nnb;
+    }
+    const uint32_t gk = gks[t];
+    const uint32_t q = swiss_find_warp(slots, nb, fx_hash_group(gk >> 1, gk & 1u), W, lane);
+    if (q == EMPTY) return false;
+    if (lane == 0) slots[q] = t;
+    __syncwarp();
+    items++;
+  }
+  // iteration rank = position among the occupied buckets
+  uint32_t rk = 0;
+  for (uint32_t s0 = 0; s0 < nb; s0 += 32) {
+    const uint32_t s = s0 + lane;
+    const bool occ = s < nb && slots[s] != EMPTY;
+    const unsigned b = __ballot_sync(0xffffffffu, occ);
+    if (occ) {
+      const uint32_t t = slots[s];
+      const uint32_t rr = rk + (uint32_t)__popc(b & ((1u << lane) - 1u));
+      rank[ord[t]] = rr;
+      gk_by_rank[rr] = gks[t];
+    }
+    rk += (uint32_t)__popc(b);
+  }
+  __syncwarp();
+  return true;
 }
 
 
-// Clusters one read's H hits. Work arrays are carved from base (shared
-// memory, or a global scratch slab for reads with very many hits) for
-// NP = next_pow2(H) or more elements.
-__device__ void cluster_read(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
-                             unsigned char* base, uint32_t NP, uint32_t* wtmp32, unsigned long long* wtmp64,
-                             uint32_t& sh_G, uint32_t& sh_C) {
-  unsigned long long* keys = (unsigned long long*)base;
-  unsigned long long* pre = keys + NP;           // NP + 1
-  uint32_t* vals = (uint32_t*)(pre + NP + 1);
-  uint32_t* a = vals + NP;                       // a and b contiguous: reused as 2*NP slots
-  uint32_t* b = a + NP;
-  uint32_t* gmin = b + NP;
-  uint32_t* gfirst = gmin + NP;
-  uint32_t* ggk = gfirst + NP;
-  uint32_t* rank = ggk + NP;
-  uint32_t* clstart = rank + NP;                 // NP + 1
-  uint32_t* clgrp = clstart + NP + 1;
-  const uint64_t rg = (uint64_t)p.r0 + r;
-  const long long L = (long long)(p.offs[rg + 1] - p.offs[rg]);
-  const uint32_t n = next_pow2(H);
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-    keys[i] = i < H ? hits[i] : ~0ull;
-    vals[i] = i;
-  }
-  __syncthreads();
-  bitonic_kv(keys, vals, n);
-  // boundaries
-  for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
-    unsigned long long k = keys[i];
-    uint32_t gk = (uint32_t)(k >> 40);
-    long long d = (long long)(k & ((1ull << 40) - 1));
-    bool gs = i == 0, cs = i == 0;
-    if (i > 0) {
-      unsigned long long kp = keys[i - 1];
-      gs = (uint32_t)(kp >> 40) != gk;
-      long long dp = (long long)(kp & ((1ull << 40) - 1));
-      cs = gs || (d - dp > 50);  // MERGE_DISTANCE (candidates.rs:27)
-    }
-    a[i] = cs ? 1u : 0u;
-    b[i] = gs ? 1u : 0u;
-    pre[i] = (unsigned long long)d;
-  }
-  __syncthreads();
-  block_scan_incl<uint32_t>(a, H, wtmp32);
-  block_scan_incl<uint32_t>(b, H, wtmp32);
-  block_scan_incl<unsigned long long>(pre, H, wtmp64);
-  if (threadIdx.x == 0) {
-    sh_C = a[H - 1];
-    sh_G = b[H - 1];
-  }
-  __syncthreads();
-  const uint32_t C = sh_C, G = sh_G;
-  for (uint32_t g = threadIdx.x; g < G; g += blockDim.x) gmin[g] = 0xFFFFFFFFu;
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
-    uint32_t cl = a[i] - 1, g = b[i] - 1;
-    bool cs = i == 0 || a[i] != a[i - 1];
-    bool gs = i == 0 || b[i] != b[i - 1];
-    if (gs) {
-      ggk[g] = (uint32_t)(keys[i] >> 40);
-      gfirst[g] = cl;
-    }
-    if (cs) {
-      clstart[cl] = i;
-      clgrp[cl] = g;
-    }
-    atomicMin(&gmin[g], vals[i]);
-  }
-  if (threadIdx.x == 0) clstart[C] = H;
-  __syncthreads();
-  // group insertion order = ascending first emission index
-  const uint32_t ng = next_pow2(G);
-  for (uint32_t g = threadIdx.x; g < ng; g += blockDim.x) {
-    keys[g] = g < G ? (((unsigned long long)gmin[g] << 32) | g) : ~0ull;
-    vals[g] = g;
-  }
-  __syncthreads();
-  bitonic_kv(keys, vals, ng);
-  // replay SwissTable insertion (single thread); slots live in a|b
-  if (threadIdx.x == 0 && !swiss_replay(keys, G, ggk, a, 2 * NP, rank, p.group_width)) atomicExch(p.err, 1);
-  __syncthreads();
-  // cluster order keys: count desc, group rank asc, diagonal order asc
-  const uint32_t nc = next_pow2(C);
-  for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
-    unsigned long long key = ~0ull;
-    if (c < C) {
-      uint32_t g = clgrp[c];
-      uint32_t cnt = clstart[c + 1] - clstart[c];
-      key = ((unsigned long long)(0xFFFFFu - cnt) << 44) | ((unsigned long long)rank[g] << 24) |
-            (unsigned long long)(c - gfirst[g]);
-    }
-    keys[c] = key;
-    vals[c] = c;
-  }
-  __syncthreads();
-  bitonic_kv(keys, vals, nc);
-  const uint32_t nout = min(C, p.max_out);
-  for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
-    uint32_t c = vals[i];
-    uint32_t s = clstart[c], e = clstart[c + 1];
-    uint32_t cnt = e - s;
-    unsigned long long sumb = pre[e - 1] - (s > 0 ? pre[s - 1] : 0ull);
-    long long sum = (long long)sumb - (long long)cnt * (long long)DIAG_BIAS;
-    long long avg = sum / (long long)cnt;  // truncation toward zero, as Rust's i64 '/'
-    uint32_t gk = ggk[clgrp[c]];
-    long long posi = (gk & 1u) ? avg - L + KMER : avg;
-    Cand cd;
-    cd.pos = posi > 0 ? (unsigned long long)posi : 0ull;
-    cd.contig = gk >> 1;
-    cd.strand = (uint8_t)(gk & 1u);
-    cd.score = cnt;
-    cd.pad[0] = 1;
-    p.cand[(size_t)r * p.max_out + i] = cd;
-  }
-  if (p.feat) {
-    // no hit-level features for reads clustered from the pool: feature 0 = -1
-    // makes the ranker keep all their candidates
-    for (uint32_t i = threadIdx.x; i < (uint32_t)MAX_CAND * RANK_FEATURES; i += blockDim.x)
-      p.feat[(size_t)r * MAX_CAND * RANK_FEATURES + i] =
-          (i % RANK_FEATURES == 0 && i / RANK_FEATURES < nout) ? -1.f : 0.f;
-  }
-  if (threadIdx.x == 0) {
-    p.n_cand[r] = nout;
-    if (p.total_cand) p.total_cand[r] = C;
-  }
-  __syncthreads();
-}
-
-// Overflowed reads (list mode): hits in the pool, arrays in global scratch.
-__global__ void k_cluster_list(ClusterArgs p) {
-  __shared__ unsigned long long wtmp64[32];
-  __shared__ uint32_t wtmp32[32];
-  __shared__ uint32_t sh_G, sh_C;
-  const unsigned int n = *p.list_n;
-  const unsigned long long s_lo = (unsigned long long)p.slice * p.pool_slice;
-  if (s_lo >= *p.list_total) return;
-  for (uint32_t w = blockIdx.x; w < n; w += gridDim.x) {
-    if (p.list_hoff[w] / p.pool_slice != p.slice) continue;
-    const uint32_t r = p.list[w];
-    const uint32_t H = p.need[r];
-    const unsigned long long off = p.list_hoff[w] - s_lo;
-    uint32_t NP = next_pow2(H);
-    cluster_read(p, r, H, p.hits_pool + off, p.scratch + 2 * off * 56, NP, wtmp32, wtmp64, sh_G, sh_C);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // K2 by diagonal bins, without sorting. The clusters of cluster_hits are the
@@ -370,7 +263,8 @@ constexpr uint32_t BIN_MAX_OUT = 256;  // candidates one read may return
 
 // Table sizes of a read of H hits: bins at load <= 0.625 (a read's hits are
 // mostly in bins of their own, and probe runs of a fuller open-addressed
-// table grow fast), groups in a power of two at least as large.
+// table grow fast); groups at load <= 0.5 of the distinct (contig, strand)
+// keys the read can have, min(H, gmax) with gmax = 2 * contigs.
 __host__ __device__ inline uint32_t np2(uint32_t x) {
   uint32_t p = 1;
   while (p < x) p <<= 1;
@@ -380,7 +274,10 @@ __host__ __device__ inline uint32_t bin_tsize(uint32_t H) {
   const uint32_t t = ((uint32_t)(((uint64_t)H * 8 + 4) / 5) + 31) & ~31u;
   return t < BIN_TMIN ? BIN_TMIN : t;
 }
-__host__ __device__ inline uint32_t grp_tsize(uint32_t H) { return np2(bin_tsize(H)); }
+__host__ __device__ inline uint32_t grp_tsize(uint32_t H, uint32_t gmax) {
+  const uint32_t g = H < gmax ? H : gmax;
+  return np2(g < 8 ? 16 : 2 * g);
+}
 
 __device__ __forceinline__ uint32_t hash_slot(unsigned long long key, uint32_t T) {
   unsigned long long k = key ^ (key >> 33);
@@ -438,256 +335,424 @@ __device__ __forceinline__ uint32_t find32(const uint32_t* keys, uint32_t key, u
   return NO_SLOT;
 }
 
-// Tables of one read of up to hmax hits: bins (key, count << 40 | offset
-// sum, diagonal mask; with the ranker also exact hits << 32 | bucket-size
-// sum and the read-position range) and groups (key, first emission then
-// rank).
-__host__ __device__ inline size_t bin_table_bytes(uint32_t hmax, bool feat) {
-  return (size_t)bin_tsize(hmax) * (feat ? 40 : 24) + (size_t)grp_tsize(hmax) * 8;
+// Tables of one read of up to hmax hits: bins (64-bit key; 32-bit count,
+// offset sum and two diagonal-mask halves; with the ranker also 32-bit exact
+// hits, bucket-size sum and read-position range), the clusters' 64-bit
+// order keys, and groups (key, first emission then rank, key by rank).
+__host__ __device__ inline size_t bin_table_bytes(uint32_t hmax, uint32_t gmax, bool feat) {
+  return (size_t)bin_tsize(hmax) * (feat ? 48 : 32) + (size_t)grp_tsize(hmax, gmax) * 12;
 }
-// Per-block cluster records in the global slab (TM entries each): diagonal
-// sum, first bin, count, group slot, group key; with the ranker exact hits,
-// bucket-size sum, distinct diagonals, read-position range and diagonal
-// spread; and the SwissTable replay's buckets.
-struct ClusterRecs {
-  unsigned long long *sum, *b0;
-  uint32_t *cnt, *gslot, *gk, *ne, *l2s, *nd, *rmn, *rmx, *spread, *slots;
-  __device__ void carve(unsigned char* base, uint32_t hmax) {
-    const uint32_t TM = bin_tsize(hmax);
-    unsigned long long* q = (unsigned long long*)base;
-    sum = q;
-    b0 = q + TM;
-    uint32_t* u = (uint32_t*)(q + 2 * TM);
-    cnt = u; gslot = u + TM; gk = u + 2 * TM; ne = u + 3 * TM; l2s = u + 4 * TM; nd = u + 5 * TM;
-    rmn = u + 6 * TM; rmx = u + 7 * TM; spread = u + 8 * TM;
-    slots = u + 9 * TM;  // 2 * grp_tsize(hmax)
+// Global scratch of the rare paths (per block, or per read in list mode):
+// the block-wide group order when a read has more than 256 groups, and the
+// exact cluster order when a count or a rank does not fit the 64-bit key.
+struct BinScratch {
+  unsigned long long *okey, *khi, *klo;
+  uint32_t *oval, *slots;
+  __device__ void carve(unsigned char* base, uint32_t hmax, uint32_t gmax) {
+    const uint32_t TG = grp_tsize(hmax, gmax), NP = np2(bin_tsize(hmax));
+    okey = (unsigned long long*)base;
+    khi = okey + TG;
+    klo = khi + NP;
+    oval = (uint32_t*)(klo + NP);
+    slots = oval + TG;
   }
 };
-__host__ __device__ inline size_t cluster_recs_bytes(uint32_t hmax) {
-  return ((size_t)bin_tsize(hmax) * (2 * 8 + 9 * 4) + (size_t)grp_tsize(hmax) * 8 + 255) & ~(size_t)255;
+__host__ __device__ inline size_t bin_scratch_bytes(uint32_t hmax, uint32_t gmax) {
+  const size_t TG = grp_tsize(hmax, gmax), NP = np2(bin_tsize(hmax));
+  return (TG * 16 + NP * 16 + 255) & ~(size_t)255;
+}
+
+// The bin table of one read.
+struct BinTab {
+  unsigned long long* key;
+  uint32_t *cnt, *sum, *mlo, *mhi, *ne, *l2s, *rmn, *rmx;
+  uint32_t T;
+  __device__ unsigned long long mask(uint32_t s) const { return ((unsigned long long)mhi[s] << 32) | mlo[s]; }
+  // Whether occupied slot s starts a cluster: its lower neighbour bin is
+  // absent or more than MERGE_DISTANCE below its smallest diagonal.
+  __device__ bool starts(uint32_t s, unsigned long long k) const {
+    const unsigned long long b = k & M35;
+    if (b == 0) return true;
+    const uint32_t q = find64(key, k - 1, T);
+    if (q == NO_SLOT) return true;
+    const unsigned long long lo = b * BIN_W + (unsigned long long)(__ffsll((long long)mask(s)) - 1);
+    const unsigned long long hi = (b - 1) * BIN_W + (unsigned long long)(63 - __clzll((long long)mask(q)));
+    return lo - hi > (unsigned)(BIN_W - 1);
+  }
+  // Next slot of the cluster after slot cur (bin cb, mask m), or NO_SLOT.
+  __device__ uint32_t next(unsigned long long k, unsigned long long b0, unsigned long long cb,
+                           unsigned long long m) const {
+    const uint32_t q = find64(key, k - b0 + cb + 1, T);
+    if (q == NO_SLOT) return NO_SLOT;
+    const unsigned long long hi = cb * BIN_W + (unsigned long long)(63 - __clzll((long long)m));
+    if ((cb + 1) * BIN_W + (unsigned long long)(__ffsll((long long)mask(q)) - 1) - hi > (unsigned)(BIN_W - 1))
+      return NO_SLOT;
+    return q;
+  }
+  // Hit count of the cluster starting at slot s.
+  __device__ uint32_t count(uint32_t s, unsigned long long k) const {
+    const unsigned long long b0 = k & M35;
+    uint32_t c = 0, cur = s;
+    unsigned long long cb = b0;
+    while (true) {
+      c += cnt[cur];
+      const uint32_t q = next(k, b0, cb, mask(cur));
+      if (q == NO_SLOT) return c;
+      cur = q;
+      cb++;
+    }
+  }
+};
+
+// Cluster order key: count descending (16 bits), group rank (13 bits), first
+// bin (35 bits); unique per cluster. Counts above 0xFFFF or ranks above
+// 0x1FFF take the exact path instead.
+constexpr uint32_t KEY_CNT_MAX = 0xFFFFu, KEY_RANK_MAX = 0x1FFFu;
+__device__ __forceinline__ unsigned long long cluster_key(uint32_t cnt, uint32_t rank, unsigned long long b0) {
+  return ((unsigned long long)(KEY_CNT_MAX - min(cnt, KEY_CNT_MAX)) << 48) |
+         ((unsigned long long)min(rank, KEY_RANK_MAX) << 35) | b0;
+}
+
+// Keys-only block bitonic sort of 64-bit keys, n a power of two.
+__device__ void bitonic_k(unsigned long long* k, uint32_t n) {
+  for (uint32_t size = 2; size <= n; size <<= 1) {
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t t = threadIdx.x; t < n / 2; t += blockDim.x) {
+        const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
+        const unsigned long long a = k[i], b = k[j];
+        if ((a > b) == ((i & size) == 0)) {
+          k[i] = b;
+          k[j] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+// Block bitonic sort of 128-bit keys (hi, lo), n a power of two.
+__device__ void bitonic_k2(unsigned long long* hi, unsigned long long* lo, uint32_t n) {
+  for (uint32_t size = 2; size <= n; size <<= 1) {
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t t = threadIdx.x; t < n / 2; t += blockDim.x) {
+        const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
+        const unsigned long long ah = hi[i], al = lo[i], bh = hi[j], bl = lo[j];
+        const bool gt = ah > bh || (ah == bh && al > bl);
+        if (gt == ((i & size) == 0)) {
+          hi[i] = bh;
+          lo[i] = bl;
+          hi[j] = ah;
+          lo[j] = al;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Group ranks for reads of more than 256 groups: first-emission sort and the
+// serial replay, in global scratch.
+__device__ void group_ranks_block(const ClusterArgs& p, uint32_t TG, const uint32_t* gkey, uint32_t* gval,
+                                  uint32_t* grk, const BinScratch& X, uint32_t& sh_n) {
+  if (threadIdx.x == 0) sh_n = 0;
+  __syncthreads();
+  for (uint32_t g = threadIdx.x; g < TG; g += blockDim.x) {
+    if (gkey[g] == GRP_EMPTY) continue;
+    const uint32_t k = atomicAdd(&sh_n, 1u);
+    X.okey[k] = ((unsigned long long)gval[g] << 32) | g;
+  }
+  __syncthreads();
+  const uint32_t G = sh_n, ng = np2(G);
+  for (uint32_t k = threadIdx.x; k < ng; k += blockDim.x) {
+    if (k >= G) X.okey[k] = ~0ull;
+    X.oval[k] = k;
+  }
+  __syncthreads();
+  bitonic_kv(X.okey, X.oval, ng);
+  if (threadIdx.x == 0 && !swiss_replay(X.okey, G, gkey, X.slots, max(16u, 2 * ng), gval, p.group_width))
+    atomicExch(p.err, 1);
+  __syncthreads();
+  for (uint32_t g = threadIdx.x; g < TG; g += blockDim.x)
+    if (gkey[g] != GRP_EMPTY && gval[g] < TG) grk[gval[g]] = gkey[g];
+  __syncthreads();
 }
 
 template <bool FEAT>
 __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
-                                  unsigned char* tab, const ClusterRecs& S, uint32_t* wtmp32,
-                                  unsigned long long* wtmp64, uint32_t& sh_n, uint32_t* sh_sel, uint32_t* sh_hist) {
-  const uint32_t T = bin_tsize(H);   // bin slots (the bins and clusters of the read <= H)
-  const uint32_t TG = grp_tsize(H);  // group slots
-  unsigned long long* bkey = (unsigned long long*)tab;
-  unsigned long long* bacc = bkey + T;
-  unsigned long long* bmask = bacc + T;
-  unsigned long long* binf = bmask + T;                         // FEAT
-  uint32_t* brmn = (uint32_t*)(bmask + (FEAT ? 2 : 1) * T);     // FEAT
-  uint32_t* brmx = brmn + T;                                    // FEAT
-  uint32_t* gkey = (uint32_t*)tab + (FEAT ? 10 : 6) * T;
-  uint32_t* gval = gkey + TG;
+                                  unsigned char* tab, const BinScratch& X, uint32_t* wtmp32, uint32_t& sh_n,
+                                  uint32_t* sh_aux) {
+  const uint32_t T = bin_tsize(H);            // bin slots (the bins and clusters of the read <= H)
+  const uint32_t TG = grp_tsize(H, p.gmax);   // group slots
+  const int lane = threadIdx.x & 31;
+  BinTab B;
+  B.T = T;
+  B.key = (unsigned long long*)tab;
+  B.cnt = (uint32_t*)(B.key + T);
+  B.sum = B.cnt + T;
+  B.mlo = B.cnt + 2 * T;
+  B.mhi = B.cnt + 3 * T;
+  B.ne = B.cnt + 4 * T;   // FEAT
+  B.l2s = B.cnt + 5 * T;  // FEAT
+  B.rmn = B.cnt + 6 * T;  // FEAT
+  B.rmx = B.cnt + 7 * T;  // FEAT
+  unsigned long long* ck = (unsigned long long*)(B.cnt + (FEAT ? 8 : 4) * T);  // cluster keys
+  uint32_t* gkey = (uint32_t*)(ck + T);
+  uint32_t* gval = gkey + TG;  // first emission index, then iteration rank
+  uint32_t* grk = gval + TG;   // group key by rank
   for (uint32_t s = threadIdx.x; s < TG; s += blockDim.x) {
     gkey[s] = GRP_EMPTY;
     gval[s] = 0xFFFFFFFFu;
   }
   for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
-    bkey[s] = BIN_EMPTY;
-    bacc[s] = 0;
-    bmask[s] = 0;
+    B.key[s] = BIN_EMPTY;
+    B.cnt[s] = 0;
+    B.sum[s] = 0;
+    B.mlo[s] = 0;
+    B.mhi[s] = 0;
     if (FEAT) {
-      binf[s] = 0;
-      brmn[s] = 0xFFFFFFFFu;
-      brmx[s] = 0;
+      B.ne[s] = 0;
+      B.l2s[s] = 0;
+      B.rmn[s] = 0xFFFFFFFFu;
+      B.rmx[s] = 0;
     }
   }
-  if (threadIdx.x == 0) sh_n = 0;
+  if (threadIdx.x == 0) {
+    sh_n = 0;
+    wtmp32[30] = 0;  // exact-path flag
+  }
   __syncthreads();
-  // A. bins and groups
+  // A. bins and groups (32-bit counters: same-address 32-bit adds from one
+  // warp combine in the shared-memory unit, 64-bit ones serialise)
   for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
     const unsigned long long w = hits[i];
     const unsigned long long d = w & M40;
     const unsigned long long b = d / BIN_W;
     const uint32_t off = (uint32_t)(d - b * BIN_W);
     const uint32_t gk = (uint32_t)(w >> 40);
-    const uint32_t s = insert64(bkey, ((unsigned long long)gk << 35) | b, T);
+    const uint32_t s = insert64(B.key, ((unsigned long long)gk << 35) | b, T);
     const uint32_t g = insert32(gkey, gk, TG);
     if (s == NO_SLOT || g == NO_SLOT) {
       atomicExch(p.err, 1);
       continue;
     }
-    atomicAdd(&bacc[s], (1ull << 40) | off);
-    atomicOr(&bmask[s], 1ull << off);
+    atomicAdd(&B.cnt[s], 1u);
+    atomicAdd(&B.sum[s], off);
+    atomicOr(off < 32 ? &B.mlo[s] : &B.mhi[s], 1u << (off & 31u));
     if (gval[g] > i) atomicMin(&gval[g], i);
     if (FEAT) {
       // hit info: read position | log2 exact bucket size << 10 | neighbour << 15
       const uint32_t info = p.hit_info[(size_t)r * p.hcap + i];
-      atomicAdd(&binf[s], ((info >> 15) ? 0ull : (1ull << 32)) | ((info >> 10) & 31u));
-      atomicMin(&brmn[s], info & 0x3FFu);
-      atomicMax(&brmx[s], info & 0x3FFu);
+      atomicAdd(&B.ne[s], (info >> 15) ? 0u : 1u);
+      atomicAdd(&B.l2s[s], (info >> 10) & 31u);
+      atomicMin(&B.rmn[s], info & 0x3FFu);
+      atomicMax(&B.rmx[s], info & 0x3FFu);
     }
   }
   __syncthreads();
-  // B. clusters: runs of joined bins, walked from each run's first bin
-  for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
-    const unsigned long long key = bkey[s];
-    if (key == BIN_EMPTY) continue;
-    const unsigned long long b = key & M35;
-    unsigned long long m = bmask[s];
-    const unsigned long long lo = b * BIN_W + (unsigned long long)(__ffsll((long long)m) - 1);
-    if (b > 0) {
-      const uint32_t q = find64(bkey, key - 1, T);
-      if (q != NO_SLOT &&
-          lo - ((b - 1) * BIN_W + (unsigned long long)(63 - __clzll((long long)bmask[q]))) <= (unsigned)(BIN_W - 1))
-        continue;  // joined to the bin below
-    }
-    uint32_t cnt = 0, ne = 0, l2s = 0, nd = 0, rmn = 0xFFFFFFFFu, rmx = 0;
-    unsigned long long sum = 0, cb = b;
-    uint32_t cur = s;
-    while (true) {
-      const unsigned long long acc = bacc[cur];
-      const uint32_t c = (uint32_t)(acc >> 40);
-      cnt += c;
-      sum += cb * BIN_W * c + (acc & M40);
-      if (FEAT) {
-        ne += (uint32_t)(binf[cur] >> 32);
-        l2s += (uint32_t)(binf[cur] & 0xFFFFFFFFu);
-        nd += (uint32_t)__popcll(m);
-        rmn = min(rmn, brmn[cur]);
-        rmx = max(rmx, brmx[cur]);
+  // B. group iteration ranks: the groups in first-emission order (counting
+  // rank; first-emission indices are distinct) replayed through std's
+  // SwissTable insertion, by one warp in shared memory; more than 256 groups
+  // take the block-wide form in global scratch
+  if (threadIdx.x < 32) {
+    unsigned long long* pairs = (unsigned long long*)(sh_aux + 512);  // 256 (first emission << 32 | slot)
+    uint32_t G = 0;
+    for (uint32_t g0 = 0; g0 < TG; g0 += 32) {
+      const uint32_t g = g0 + lane;
+      const bool occ = g < TG && gkey[g] != GRP_EMPTY;
+      const unsigned bal = __ballot_sync(0xffffffffu, occ);
+      if (occ) {
+        const uint32_t e = G + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+        if (e < 256) pairs[e] = ((unsigned long long)gval[g] << 32) | g;
       }
-      const uint32_t q = find64(bkey, key - b + cb + 1, T);
-      if (q == NO_SLOT) break;
-      const unsigned long long mq = bmask[q];
-      const unsigned long long hi = cb * BIN_W + (unsigned long long)(63 - __clzll((long long)m));
-      if ((cb + 1) * BIN_W + (unsigned long long)(__ffsll((long long)mq) - 1) - hi > (unsigned)(BIN_W - 1)) break;
-      cur = q;
-      m = mq;
-      cb++;
+      G += (uint32_t)__popc(bal);
     }
-    const uint32_t k = atomicAdd(&sh_n, 1u);
-    const uint32_t gk = (uint32_t)(key >> 35);
-    S.cnt[k] = cnt;
-    S.sum[k] = sum;
-    S.b0[k] = b;
-    S.gk[k] = gk;
-    S.gslot[k] = find32(gkey, gk, TG);
-    if (FEAT) {
-      S.ne[k] = ne;
-      S.l2s[k] = l2s;
-      S.nd[k] = nd;
-      S.rmn[k] = rmn;
-      S.rmx[k] = rmx;
-      S.spread[k] = (uint32_t)(cb * BIN_W + (unsigned long long)(63 - __clzll((long long)m)) - lo);
+    if (lane == 0) wtmp32[31] = G;
+    if (G <= 256) {
+      __syncwarp();
+      for (uint32_t e = lane; e < G; e += 32) {
+        const unsigned long long v = pairs[e];
+        uint32_t rk = 0;
+        for (uint32_t f = 0; f < G; f++) rk += pairs[f] < v ? 1u : 0u;
+        sh_aux[rk] = (uint32_t)v;
+      }
+      __syncwarp();
+      if (!swiss_replay_warp(G, gkey, sh_aux, max(16u, 2 * np2(G)), gval, grk, p.group_width, lane) && lane == 0)
+        atomicExch(p.err, 1);
     }
+  }
+  __syncthreads();
+  const uint32_t G = wtmp32[31];
+  if (G > 256) group_ranks_block(p, TG, gkey, gval, grk, X, sh_n);
+  if (threadIdx.x == 0) sh_n = 0;
+  __syncthreads();
+  // C. clusters: runs of joined bins, each counted from its first bin, its
+  // order key into ck
+  for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
+    const unsigned long long k = B.key[s];
+    if (k == BIN_EMPTY || !B.starts(s, k)) continue;
+    const uint32_t cnt = B.count(s, k);
+    const uint32_t gk = (uint32_t)(k >> 35);
+    const uint32_t rank = gval[find32(gkey, gk, TG)];
+    if (cnt > KEY_CNT_MAX || rank > KEY_RANK_MAX) wtmp32[30] = 1;
+    ck[atomicAdd(&sh_n, 1u)] = cluster_key(cnt, rank, k & M35);
   }
   __syncthreads();
   const uint32_t C = sh_n;
-  // C. groups in first-emission order, SwissTable replay (the bin table's
-  // space holds the sort); gval becomes the group's iteration rank
-  unsigned long long* okey = bkey;               // ng <= TG <= 2T words
-  uint32_t* oval = (uint32_t*)(bkey + 2 * T);    // ng <= 2T half-words
-  __syncthreads();
-  if (threadIdx.x == 0) sh_n = 0;
-  __syncthreads();
-  for (uint32_t g = threadIdx.x; g < TG; g += blockDim.x) {
-    if (gkey[g] == GRP_EMPTY) continue;
-    const uint32_t k = atomicAdd(&sh_n, 1u);
-    okey[k] = ((unsigned long long)gval[g] << 32) | g;
-  }
-  __syncthreads();
-  const uint32_t G = sh_n;
-  const uint32_t ng = next_pow2(G);
-  for (uint32_t k = threadIdx.x; k < ng; k += blockDim.x) {
-    if (k >= G) okey[k] = ~0ull;
-    oval[k] = k;
-  }
-  __syncthreads();
-  bitonic_kv(okey, oval, ng);
-  if (threadIdx.x == 0 && !swiss_replay(okey, G, gkey, S.slots, max(16u, 2 * ng), gval, p.group_width))
-    atomicExch(p.err, 1);
-  __syncthreads();
-  // D. cluster order keys (count desc, group rank, diagonal order); the first
-  // max_out by repeated block-wide minima
-  unsigned long long* ck = bkey;
-  for (uint32_t c = threadIdx.x; c < C; c += blockDim.x)
-    ck[c] = ((unsigned long long)(0x7FFFu - S.cnt[c]) << 49) | ((unsigned long long)gval[S.gslot[c]] << 35) | S.b0[c];
-  __syncthreads();
+  const bool exact = wtmp32[30] != 0;
   const uint32_t nout = min(min(C, p.max_out), BIN_MAX_OUT);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // the nout-th smallest key by an MSB-first radix select (8 bits a pass);
-  // the keys are unique, so exactly nout keys are <= it
-  unsigned long long prefix = 0, pmask = 0;
-  if (nout < C) {
-    uint32_t need = nout;
-    for (int shift = 56; shift >= 0; shift -= 8) {
-      for (uint32_t q = threadIdx.x; q < 256; q += blockDim.x) sh_hist[q] = 0;
-      __syncthreads();
-      for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-        const unsigned long long v = ck[c];
-        if ((v & pmask) == prefix) atomicAdd(&sh_hist[(v >> shift) & 255u], 1u);
-      }
-      __syncthreads();
-      if (wid == 0) {
-        // warp scan over 256 bins, 8 per lane
-        uint32_t loc[8], tot = 0;
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-          loc[q] = sh_hist[lane * 8 + q];
-          tot += loc[q];
+  __syncthreads();  // every thread holds C before sh_n is counted again
+  // D. the first nout clusters in order. Fast path: the nout-th smallest key
+  // by an MSB-first radix select (8 bits a pass; the keys are unique, so
+  // exactly nout keys are <= it), then those keys sorted. Exact path: every
+  // cluster's (count, rank, first bin) sorted as 128-bit keys in scratch.
+  unsigned long long* selk = (unsigned long long*)(sh_aux + 256);  // BIN_MAX_OUT sorted keys
+  if (!exact) {
+    uint32_t* sh_hist = sh_aux;
+    unsigned long long prefix = 0, pmask = 0;
+    if (nout < C) {
+      uint32_t need = nout;
+      const int wid = threadIdx.x >> 5;
+      for (int shift = 56; shift >= 0; shift -= 8) {
+        for (uint32_t q = threadIdx.x; q < 256; q += blockDim.x) sh_hist[q] = 0;
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+          const unsigned long long v = ck[c];
+          if ((v & pmask) == prefix) atomicAdd(&sh_hist[(v >> shift) & 255u], 1u);
         }
-        uint32_t incl = tot;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-          if (lane >= d) incl += y;
-        }
-        uint32_t before = incl - tot;
-        if (before < need && need <= incl) {
+        __syncthreads();
+        if (wid == 0) {
+          // warp scan over 256 bins, 8 per lane
+          uint32_t loc[8], tot = 0;
 #pragma unroll
           for (int q = 0; q < 8; q++) {
-            if (before < need && need <= before + loc[q]) {
-              wtmp32[0] = (uint32_t)(lane * 8 + q);
-              wtmp32[1] = need - before;
+            loc[q] = sh_hist[lane * 8 + q];
+            tot += loc[q];
+          }
+          uint32_t incl = tot;
+#pragma unroll
+          for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+          }
+          uint32_t before = incl - tot;
+          if (before < need && need <= incl) {
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+              if (before < need && need <= before + loc[q]) {
+                wtmp32[0] = (uint32_t)(lane * 8 + q);
+                wtmp32[1] = need - before;
+              }
+              before += loc[q];
             }
-            before += loc[q];
           }
         }
+        __syncthreads();
+        prefix |= (unsigned long long)wtmp32[0] << shift;
+        pmask |= 255ull << shift;
+        need = wtmp32[1];
+        __syncthreads();
       }
-      __syncthreads();
-      prefix |= (unsigned long long)wtmp32[0] << shift;
-      pmask |= 255ull << shift;
-      need = wtmp32[1];
-      __syncthreads();
+    } else {
+      prefix = ~0ull;
     }
+    if (threadIdx.x == 0) sh_n = 0;
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+      const unsigned long long v = ck[c];
+      if (v <= prefix) {
+        const uint32_t q = atomicAdd(&sh_n, 1u);
+        if (q < BIN_MAX_OUT) selk[q] = v;
+      }
+    }
+    __syncthreads();
+    const uint32_t ns = np2(nout);
+    for (uint32_t q = threadIdx.x; q < ns; q += blockDim.x)
+      if (q >= nout) selk[q] = ~0ull;
+    __syncthreads();
+    bitonic_k(selk, ns);
   } else {
-    prefix = ~0ull;
-  }
-  // the selected keys, sorted (at most BIN_MAX_OUT of them)
-  if (threadIdx.x == 0) sh_n = 0;
-  __syncthreads();
-  unsigned long long* selk = ck + T;
-  uint32_t* selv = (uint32_t*)(selk + BIN_MAX_OUT);
-  for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-    const unsigned long long v = ck[c];
-    if (v <= prefix) {
+    if (threadIdx.x == 0) sh_n = 0;
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
+      const unsigned long long k = B.key[s];
+      if (k == BIN_EMPTY || !B.starts(s, k)) continue;
+      const uint32_t cnt = B.count(s, k);
+      const uint32_t rank = gval[find32(gkey, (uint32_t)(k >> 35), TG)];
       const uint32_t q = atomicAdd(&sh_n, 1u);
-      if (q < BIN_MAX_OUT) {
-        selk[q] = v;
-        selv[q] = c;
-      }
+      X.khi[q] = ((unsigned long long)(~cnt) << 32) | rank;
+      X.klo[q] = k & M35;
     }
+    __syncthreads();
+    const uint32_t nc = np2(C);
+    for (uint32_t q = C + threadIdx.x; q < nc; q += blockDim.x) {
+      X.khi[q] = ~0ull;
+      X.klo[q] = ~0ull;
+    }
+    __syncthreads();
+    bitonic_k2(X.khi, X.klo, nc);
   }
-  __syncthreads();
-  const uint32_t ns = next_pow2(nout);
-  for (uint32_t q = threadIdx.x; q < ns; q += blockDim.x)
-    if (q >= nout) selk[q] = ~0ull;
-  __syncthreads();
-  bitonic_kv(selk, selv, ns);
-  for (uint32_t q = threadIdx.x; q < nout; q += blockDim.x) sh_sel[q] = selv[q];
-  __syncthreads();
+  // E. the candidates: each selected cluster walked again from its first
+  // bin for its diagonal sum (and the ranker's seed features)
   const uint64_t rg = (uint64_t)p.r0 + r;
   const long long L = (long long)(p.offs[rg + 1] - p.offs[rg]);
-  for (uint32_t i = threadIdx.x; i < nout; i += blockDim.x) {
-    const uint32_t c = sh_sel[i];
-    const uint32_t cnt = S.cnt[c];
-    const long long sum = (long long)S.sum[c] - (long long)cnt * (long long)DIAG_BIAS;
-    const long long avg = sum / (long long)cnt;  // truncation toward zero, as Rust's i64 '/'
-    const uint32_t gk = S.gk[c];
+  float meanq = 0.f;
+  if (FEAT) {
+    uint32_t qs = 0;
+    const uint64_t q0 = p.offs[rg];
+    for (uint32_t k = threadIdx.x; k < (uint32_t)L; k += blockDim.x) qs += p.quals[q0 + k];
+    for (int d = 16; d; d >>= 1) qs += __shfl_xor_sync(0xffffffffu, qs, d);
+    if (lane == 0) wtmp32[threadIdx.x >> 5] = qs;
+    __syncthreads();
+    uint32_t qt = 0;
+    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); w2++) qt += wtmp32[w2];
+    meanq = L ? (float)qt / (float)L : 0.f;
+  }
+  for (uint32_t i = threadIdx.x; i < (FEAT ? max(nout, (uint32_t)MAX_CAND) : nout); i += blockDim.x) {
+    if (FEAT && i >= nout) {
+      if (i < (uint32_t)MAX_CAND) {
+        float* f = p.feat + ((size_t)r * MAX_CAND + i) * RANK_FEATURES;
+        for (int q = 0; q < RANK_FEATURES; q++) f[q] = 0.f;
+      }
+      continue;
+    }
+    uint32_t rank;
+    unsigned long long b0;
+    if (!exact) {
+      const unsigned long long v = selk[i];
+      rank = (uint32_t)(v >> 35) & KEY_RANK_MAX;
+      b0 = v & M35;
+    } else {
+      rank = (uint32_t)X.khi[i];
+      b0 = X.klo[i];
+    }
+    const uint32_t gk = grk[rank];
+    const unsigned long long k = ((unsigned long long)gk << 35) | b0;
+    const uint32_t s0 = find64(B.key, k, T);
+    uint32_t cur = s0;
+    uint32_t cnt = 0, ne = 0, l2s = 0, nd = 0, rmn = 0xFFFFFFFFu, rmx = 0;
+    unsigned long long sum = 0, cb = b0, m = 0;
+    while (cur != NO_SLOT) {
+      const uint32_t c = B.cnt[cur];
+      m = B.mask(cur);
+      cnt += c;
+      sum += cb * BIN_W * c + B.sum[cur];
+      if (FEAT) {
+        ne += B.ne[cur];
+        l2s += B.l2s[cur];
+        nd += (uint32_t)__popcll(m);
+        rmn = min(rmn, B.rmn[cur]);
+        rmx = max(rmx, B.rmx[cur]);
+      }
+      const uint32_t q = B.next(k, b0, cb, m);
+      if (q == NO_SLOT) break;
+      cur = q;
+      cb++;
+    }
+    if (cnt == 0) {  // a selected cluster must exist
+      atomicExch(p.err, 1);
+      continue;
+    }
+    const long long sm = (long long)sum - (long long)cnt * (long long)DIAG_BIAS;
+    const long long avg = sm / (long long)cnt;  // truncation toward zero, as Rust's i64 '/'
     const long long posi = (gk & 1u) ? avg - L + KMER : avg;
     Cand cd;
     cd.pos = posi > 0 ? (unsigned long long)posi : 0ull;
@@ -696,41 +761,26 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     cd.score = cnt;
     cd.pad[0] = 1;
     p.cand[(size_t)r * p.max_out + i] = cd;
-  }
-  if (FEAT) {
-    // the candidate ranker's seed features of each kept candidate: exact and
-    // one-mismatch hits, distinct diagonals, diagonal spread, read span of
-    // the hits, read length, mean base quality, rank and list size, mean
-    // log2 exact-bucket size (7 and 8, the mate features, come later)
-    uint32_t qs = 0;
-    const uint64_t q0 = p.offs[rg];
-    for (uint32_t k = threadIdx.x; k < (uint32_t)L; k += blockDim.x) qs += p.quals[q0 + k];
-    for (int d = 16; d; d >>= 1) qs += __shfl_xor_sync(0xffffffffu, qs, d);
-    if (lane == 0) wtmp32[wid] = qs;
-    __syncthreads();
-    uint32_t qt = 0;
-    for (int w2 = 0; w2 < nw; w2++) qt += wtmp32[w2];
-    const float meanq = L ? (float)qt / (float)L : 0.f;
-    for (uint32_t i = threadIdx.x; i < (uint32_t)MAX_CAND; i += blockDim.x) {
+    if (FEAT && i < (uint32_t)MAX_CAND) {
+      // the candidate ranker's seed features: exact and one-mismatch hits,
+      // distinct diagonals, diagonal spread, read span of the hits, read
+      // length, mean base quality, rank and list size, mean log2
+      // exact-bucket size (7 and 8, the mate features, come later)
+      const unsigned long long lo = b0 * BIN_W + (unsigned long long)(__ffsll((long long)B.mask(s0)) - 1);
+      const uint32_t spread = (uint32_t)(cb * BIN_W + (unsigned long long)(63 - __clzll((long long)m)) - lo);
       float* f = p.feat + ((size_t)r * MAX_CAND + i) * RANK_FEATURES;
-      if (i >= nout) {
-        for (int k = 0; k < RANK_FEATURES; k++) f[k] = 0.f;
-        continue;
-      }
-      const uint32_t c = sh_sel[i];
-      const uint32_t nh = S.cnt[c], ne = S.ne[c];
       f[0] = log2f(1.f + (float)ne);
-      f[1] = log2f(1.f + (float)(nh - ne));
-      f[2] = log2f(1.f + (float)S.nd[c]);
-      f[3] = log2f(1.f + (float)S.spread[c]);
-      f[4] = log2f(1.f + (nh ? (float)(S.rmx[c] - S.rmn[c] + KMER) : 0.f));
+      f[1] = log2f(1.f + (float)(cnt - ne));
+      f[2] = log2f(1.f + (float)nd);
+      f[3] = log2f(1.f + (float)spread);
+      f[4] = log2f(1.f + (cnt ? (float)(rmx - rmn + KMER) : 0.f));
       f[5] = (float)L;
       f[6] = meanq;
       f[7] = 10.f;
       f[8] = 0.f;
       f[9] = (float)i;
       f[10] = (float)nout;
-      f[11] = nh ? (float)S.l2s[c] / (float)nh : 0.f;
+      f[11] = cnt ? (float)l2s / (float)cnt : 0.f;
     }
   }
   if (threadIdx.x == 0) {
@@ -740,21 +790,16 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   __syncthreads();
 }
 
-// Reads of h_lo < H <= h_hi hits (h_hi <= TM) from the per-read buffer. The
-// tables sit in shared memory, or with GT in the block's slab after the
-// cluster records; FEAT adds the candidate ranker's features.
 template <bool GT, bool FEAT>
-__global__ void k_cluster_bins(ClusterArgs p, uint32_t hmax, size_t slab_bytes) {
+__global__ void __launch_bounds__(1024, 1) k_cluster_bins(ClusterArgs p, uint32_t hmax, size_t slab_bytes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ unsigned long long wtmp64[32];
   __shared__ uint32_t wtmp32[32];
   __shared__ uint32_t sh_n;
-  __shared__ uint32_t sh_sel[BIN_MAX_OUT];
-  __shared__ uint32_t sh_hist[256];
+  __shared__ __align__(8) uint32_t sh_aux[1280];
   unsigned char* slab = p.scratch + (size_t)blockIdx.x * slab_bytes;
-  ClusterRecs S;
-  S.carve(slab, hmax);
-  unsigned char* tab = GT ? slab + cluster_recs_bytes(hmax) : smem_raw;
+  BinScratch X;
+  X.carve(slab, hmax, p.gmax);
+  unsigned char* tab = GT ? slab + bin_scratch_bytes(hmax, p.gmax) : smem_raw;
   for (uint32_t r = blockIdx.x; r < p.nr; r += gridDim.x) {
     const uint32_t H = p.hit_cnt[r];
     if (p.overflow[r]) continue;
@@ -769,23 +814,73 @@ __global__ void k_cluster_bins(ClusterArgs p, uint32_t hmax, size_t slab_bytes) 
           p.feat[(size_t)r * MAX_CAND * RANK_FEATURES + i] = 0.f;
       continue;
     }
-    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, S, wtmp32, wtmp64, sh_n, sh_sel, sh_hist);
+    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, X, wtmp32, sh_n, sh_aux);
   }
 }
 
-size_t cluster_bins_slab_bytes(uint32_t hmax, bool table_in_slab) {
-  return cluster_recs_bytes(hmax) + (table_in_slab ? bin_table_bytes(hmax, true) : 0);
+// Over-capacity reads (list mode): the hits of the reads whose pool offset
+// falls in slice p.slice, clustered in the binned form with the records and
+// tables of each read in global scratch at bytes_per_hit times its pool
+// offset (cluster_list_bytes_per_hit covers every read of more than hcap
+// hits). With the ranker these reads get feature 0 = -1 (no hit-level
+// features), which keeps all their candidates.
+__global__ void __launch_bounds__(1024, 1) k_cluster_list(ClusterArgs p, size_t bytes_per_hit) {
+  __shared__ uint32_t wtmp32[32];
+  __shared__ uint32_t sh_n;
+  __shared__ __align__(8) uint32_t sh_aux[1280];
+  const unsigned int n = *p.list_n;
+  const unsigned long long s_lo = (unsigned long long)p.slice * p.pool_slice;
+  if (s_lo >= *p.list_total) return;
+  for (uint32_t w = blockIdx.x; w < n; w += gridDim.x) {
+    if (p.list_hoff[w] / p.pool_slice != p.slice) continue;
+    const uint32_t r = p.list[w];
+    const uint32_t H = p.need[r];
+    const unsigned long long off = p.list_hoff[w] - s_lo;
+    unsigned char* base = p.scratch + off * bytes_per_hit;
+    BinScratch X;
+    X.carve(base, H, p.gmax);
+    cluster_read_bins<false>(p, r, H, p.hits_pool + off, base + bin_scratch_bytes(H, p.gmax), X, wtmp32, sh_n,
+                             sh_aux);
+    if (p.feat) {
+      const uint32_t nout = p.n_cand[r];
+      for (uint32_t i = threadIdx.x; i < (uint32_t)MAX_CAND * RANK_FEATURES; i += blockDim.x)
+        p.feat[(size_t)r * MAX_CAND * RANK_FEATURES + i] =
+            (i % RANK_FEATURES == 0 && i / RANK_FEATURES < nout) ? -1.f : 0.f;
+      __syncthreads();
+    }
+  }
 }
 
-size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat) { return bin_table_bytes(hmax, feat); }
+// Dynamic shared memory a binned block may take (227 KB less room for the
+// kernel's static arrays).
+constexpr size_t BIN_SMEM_MAX = 220 * 1024;
+
+size_t cluster_bins_slab_bytes(uint32_t hmax, uint32_t gmax, bool table_in_slab) {
+  return bin_scratch_bytes(hmax, gmax) + (table_in_slab ? bin_table_bytes(hmax, gmax, true) : 0);
+}
+
+size_t cluster_bins_smem_bytes(uint32_t hmax, uint32_t gmax, bool feat) { return bin_table_bytes(hmax, gmax, feat); }
 
 // Whether a tier's tables go to the global slab: more than one block's
 // shared memory.
-bool cluster_bins_in_slab(uint32_t hmax, bool feat) { return bin_table_bytes(hmax, feat) > 220 * 1024; }
+bool cluster_bins_in_slab(uint32_t hmax, uint32_t gmax, bool feat) {
+  return bin_table_bytes(hmax, gmax, feat) > BIN_SMEM_MAX;
+}
+
+// Scratch bytes per pooled hit of list mode: scratch plus tables of a read of
+// H > hcap hits, at most 32 T + 16 NP + 28 TG + 255 bytes with T =
+// bin_tsize(H) <= 1.6 H + 32, NP = np2(T) <= 3.2 H + 64 and TG =
+// grp_tsize(H, gmax) <= 4 min(H, gmax) + 16; rounded up to 16 bytes.
+size_t cluster_list_bytes_per_hit(uint32_t hcap, uint32_t gmax) {
+  const double hmin = (double)hcap + 1.0;
+  const double g = (double)gmax < hmin ? (double)gmax / hmin : 1.0;
+  const double per = 102.4 + 112.0 * g + 2751.0 / hmin;
+  return ((size_t)per + 1 + 15) & ~(size_t)15;
+}
 
 template <bool GT, bool FEAT>
-static int bins_blocks_per_sm(uint32_t hmax, int threads) {
-  const size_t sm = GT ? 0 : bin_table_bytes(hmax, FEAT);
+static int bins_blocks_per_sm(uint32_t hmax, uint32_t gmax, int threads) {
+  const size_t sm = GT ? 0 : bin_table_bytes(hmax, gmax, FEAT);
   if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cluster_bins<GT, FEAT>, threads, sm) != cudaSuccess) n = 1;
@@ -795,23 +890,23 @@ static int bins_blocks_per_sm(uint32_t hmax, int threads) {
 // Resident blocks of the binned K2 on num_sms SMs (the kernel loops over
 // reads, so its grid is what fits at once); the table-in-slab tier runs one
 // block per SM.
-int cluster_bins_grid(uint32_t hmax, int threads, bool feat, int num_sms) {
-  if (cluster_bins_in_slab(hmax, feat)) return num_sms;
-  return num_sms * (feat ? bins_blocks_per_sm<false, true>(hmax, threads)
-                         : bins_blocks_per_sm<false, false>(hmax, threads));
+int cluster_bins_grid(uint32_t hmax, uint32_t gmax, int threads, bool feat, int num_sms) {
+  if (cluster_bins_in_slab(hmax, gmax, feat)) return num_sms;
+  return num_sms * (feat ? bins_blocks_per_sm<false, true>(hmax, gmax, threads)
+                         : bins_blocks_per_sm<false, false>(hmax, gmax, threads));
 }
 
 template <bool GT, bool FEAT>
 static void launch_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, size_t slab, cudaStream_t st) {
-  const size_t sm = GT ? 0 : bin_table_bytes(hmax, FEAT);
+  const size_t sm = GT ? 0 : bin_table_bytes(hmax, a.gmax, FEAT);
   if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_cluster_bins<GT, FEAT><<<grid, threads, sm, st>>>(a, hmax, slab);
 }
 
 void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, cudaStream_t st) {
   const bool feat = a.feat != nullptr;
-  const bool gt = cluster_bins_in_slab(hmax, feat);
-  const size_t slab = cluster_bins_slab_bytes(hmax, gt);
+  const bool gt = cluster_bins_in_slab(hmax, a.gmax, feat);
+  const size_t slab = cluster_bins_slab_bytes(hmax, a.gmax, gt);
   if (gt) {
     if (feat) launch_bins<true, true>(a, hmax, threads, grid, slab, st);
     else launch_bins<true, false>(a, hmax, threads, grid, slab, st);
@@ -821,8 +916,8 @@ void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int g
   }
 }
 
-void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st) {
-  k_cluster_list<<<grid, 256, 0, st>>>(a);
+void launch_cluster_list(const ClusterArgs& a, size_t bytes_per_hit, int grid, cudaStream_t st) {
+  k_cluster_list<<<grid, 1024, 0, st>>>(a, bytes_per_hit);
 }
 
 }  // namespace pbw

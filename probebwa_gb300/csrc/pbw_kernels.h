@@ -73,14 +73,15 @@ struct ClusterArgs {
   uint32_t* n_cand;         // nr: kept
   uint32_t* total_cand;     // nr: all clusters (optional)
   uint32_t h_lo, h_hi;      // process reads with h_lo < H <= h_hi
+  uint32_t gmax;            // distinct (contig, strand) keys: 2 * contigs
   int* err;                 // device error word
-  // list mode (overflowed reads): hits in the pool, sort arrays in global scratch
+  // list mode (overflowed reads): hits in the pool, tables in global scratch
   const uint32_t* list;
   const unsigned int* list_n;
   const unsigned long long* list_hoff;
   const unsigned long long* hits_pool;
   const uint32_t* need;
-  unsigned char* scratch;   // 2 * 56 bytes per pooled hit
+  unsigned char* scratch;   // list mode: cluster_list_bytes_per_hit per pooled hit; tiers: the slabs
   unsigned long long pool_slice;  // as SeedArgs: the slice of the pool in use
   uint32_t slice;
   const unsigned long long* list_total;
@@ -91,18 +92,21 @@ struct ClusterArgs {
   const uint16_t* hit_info;         // nr * hcap: read position | log2 bucket << 10 | neighbour << 15
   const uint8_t* quals;             // the reads' Phred scores (at offs)
 };
-void launch_cluster_list(const ClusterArgs& a, int grid, cudaStream_t st);
+// K2 of the over-capacity reads of one pool slice (list mode), tables in
+// a.scratch at bytes_per_hit (cluster_list_bytes_per_hit(hcap, gmax)) per
+// pooled hit.
+size_t cluster_list_bytes_per_hit(uint32_t hcap, uint32_t gmax);
+void launch_cluster_list(const ClusterArgs& a, size_t bytes_per_hit, int grid, cudaStream_t st);
 // K2 by diagonal bins (no sort of the hits; cluster.cu) for reads of
 // h_lo < H <= h_hi <= hmax hits, one block per read: the tables in shared
 // memory, or, when they do not fit (cluster_bins_in_slab), in a.scratch.
-// a.scratch holds grid slabs of cluster_bins_slab_bytes(hmax, in_slab);
+// a.scratch holds grid slabs of cluster_bins_slab_bytes(hmax, gmax, in_slab);
 // the grid is cluster_bins_grid (the blocks that are resident at once).
-size_t cluster_bins_slab_bytes(uint32_t hmax, bool table_in_slab);
-size_t cluster_bins_smem_bytes(uint32_t hmax, bool feat);
-bool cluster_bins_in_slab(uint32_t hmax, bool feat);
-int cluster_bins_grid(uint32_t hmax, int threads, bool feat, int num_sms);
+size_t cluster_bins_slab_bytes(uint32_t hmax, uint32_t gmax, bool table_in_slab);
+size_t cluster_bins_smem_bytes(uint32_t hmax, uint32_t gmax, bool feat);
+bool cluster_bins_in_slab(uint32_t hmax, uint32_t gmax, bool feat);
+int cluster_bins_grid(uint32_t hmax, uint32_t gmax, int threads, bool feat, int num_sms);
 void launch_cluster_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, cudaStream_t st);
-uint32_t next_pow2_host(uint32_t x);
 void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st);
 // Exclusive offsets of the listed (over-capacity) reads' hit counts, their
 // total, and the list length for the list-mode passes; a read needing more

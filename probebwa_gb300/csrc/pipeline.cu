@@ -60,10 +60,10 @@ int pipeline_init(pbw_handle* h) {
 // slice of OVF_SLICE_HITS at a time: the reads whose exclusive offset falls
 // in slice s are seeded again and clustered in the s-th list-mode pass. A
 // read reaches at most one slice past its start, so the pool holds two
-// slices; their clustering scratch takes 112 bytes per pooled hit. A chunk's
+// slices; their clustering scratch takes cluster_list_bytes_per_hit bytes
+// per pooled hit. A chunk's
 // over-capacity reads may hold up to OVF_MAX_SLICES slices of hits.
 constexpr size_t OVF_SLICE_HITS = 16ull << 20;
-constexpr size_t OVF_POOL_HITS = 2 * OVF_SLICE_HITS;
 constexpr uint32_t OVF_MAX_SLICES = 16;
 // Tiers of the binned K2: reads up to hmax hits (0: the per-read buffer's
 // capacity) and threads per block; a tier whose tables do not fit shared
@@ -73,17 +73,19 @@ struct BinTier {
   int threads;
 };
 constexpr BinTier BIN_TIERS[5] = {{512, 128}, {1024, 256}, {2048, 512}, {4096, 1024}, {0, 1024}};
+static uint32_t group_keys(const pbw_handle* h) { return 2u * std::max(h->G.ncontig, 1u); }
 static size_t cluster_scratch_bytes(const pbw_handle* h, uint32_t hcap) {
   size_t need = 0;
   uint32_t lo = 0;
+  const uint32_t gm = group_keys(h);
   for (const BinTier& t : BIN_TIERS) {
     const uint32_t hm = t.hmax ? std::min(t.hmax, hcap) : hcap;
     if (hm <= lo) continue;
     const uint32_t hx = t.hmax ? t.hmax : hcap;
     for (const bool feat : {false, true}) {
-      const bool gt = cluster_bins_in_slab(hx, feat);
-      need = std::max(need, cluster_bins_slab_bytes(hx, gt) * (size_t)cluster_bins_grid(hx, t.threads, feat,
-                                                                                       h->num_sms));
+      const bool gt = cluster_bins_in_slab(hx, gm, feat);
+      need = std::max(need, cluster_bins_slab_bytes(hx, gm, gt) *
+                                (size_t)cluster_bins_grid(hx, gm, t.threads, feat, h->num_sms));
     }
     lo = hm;
   }
@@ -95,6 +97,8 @@ static uint64_t ovf_slice_hits(const pbw_handle* h) {
   const uint64_t s = h->tune.ovf_slice_hits;
   return s && s < OVF_SLICE_HITS ? s : OVF_SLICE_HITS;
 }
+// The pool: two slices.
+static uint64_t ovf_pool_hits(const pbw_handle* h) { return 2 * ovf_slice_hits(h); }
 static uint32_t ovf_max_slices(const pbw_handle* h) {
   return (uint32_t)((OVF_MAX_SLICES * OVF_SLICE_HITS) / ovf_slice_hits(h));
 }
@@ -114,10 +118,11 @@ static ChunkCfg chunk_cfg(pbw_handle* h, uint64_t n, int lmax) {
   c.ch = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(n, 1), h->opt.chunk_reads);
   c.lmax = std::max(lmax, 1);
   c.lmin = std::min(std::max(h->call_lmin, 0), c.lmax);
-  // per-read hit buffer: 4096 hits sort in shared memory; long reads on a
-  // repeat-rich genome have more (a 3.1 Gbp genome with 45% interspersed
-  // repeats gives 250-base reads ~4,100 hits on average, 11,600 at the 99th
-  // percentile), sorted in global slabs up to 16384, the rest in the pool
+  // per-read hit buffer: 4096 hits cluster with shared-memory tables; long
+  // reads on a repeat-rich genome have more (a 3.1 Gbp genome with 45%
+  // interspersed repeats gives 250-base reads ~4,100 hits on average, 11,600
+  // at the 99th percentile), clustered with global-slab tables up to 16384,
+  // the rest through the pool
   c.hcap = c.lmax > 160 ? 16384 : 4096;
   c.wcap = (uint32_t)std::max(c.lmax - KMER + 1, 1);
   const uint64_t rp = std::max<uint64_t>(h->opt.max_indel_len, 10);
@@ -151,8 +156,8 @@ static int ensure_chunk(pbw_handle* h, const ChunkCfg& c) {
   TRY(grow(h, h->d_need, c.ch));
   TRY(grow(h, h->d_ovf_list, c.ch));
   TRY(grow(h, h->d_list_hoff, c.ch));
-  TRY(grow(h, h->d_hits_pool, OVF_POOL_HITS));
-  TRY(grow(h, h->d_cl_scratch, OVF_POOL_HITS * 112));
+  TRY(grow(h, h->d_hits_pool, ovf_pool_hits(h)));
+  TRY(grow(h, h->d_cl_scratch, ovf_pool_hits(h) * cluster_list_bytes_per_hit(c.hcap, group_keys(h))));
   TRY(grow(h, h->d_cl_big, cluster_scratch_bytes(h, c.hcap)));
   if (h->opt.max_indel_len > 31) TRY(ensure_window_slab(h, c.lmax, c.nmax, window_grid(h)));
   else TRY(grow(h, h->d_tb_global, band_tb_slab_bytes(c.lmax, c.nmax, h->num_sms, (int)h->opt.max_indel_len)));
@@ -311,7 +316,7 @@ static int ovf_slice(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* bases, c
     cl.pool_slice = ovf_slice_hits(h);
     cl.slice = s;
     cl.list_total = h->d_cnt64.p + 8;
-    launch_cluster_list(cl, h->num_sms, st);
+    launch_cluster_list(cl, cluster_list_bytes_per_hit(cfg.hcap, ca->gmax), h->num_sms, st);
     h->stats.kernel_launches += 1;
   }
   CK(cudaGetLastError());
@@ -335,6 +340,7 @@ static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* base
   ca.r0 = r0;
   ca.nr = nr;
   ca.group_width = h->opt.group_width;
+  ca.gmax = group_keys(h);
   ca.max_out = max_out;
   ca.cand = cand;
   ca.n_cand = n_cand;
@@ -355,7 +361,8 @@ static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* base
     cb.h_hi = hm;
     cb.scratch = h->d_cl_big.p;
     const uint32_t hx = t.hmax ? t.hmax : cfg.hcap;
-    launch_cluster_bins(cb, hx, t.threads, cluster_bins_grid(hx, t.threads, feat != nullptr, h->num_sms), st);
+    launch_cluster_bins(cb, hx, t.threads, cluster_bins_grid(hx, ca.gmax, t.threads, feat != nullptr, h->num_sms),
+                        st);
     h->stats.kernel_launches += 1;
     lo = hm;
   }
@@ -1567,7 +1574,7 @@ int pbw_seed_batch(pbw_handle* h, const pbw_reads* reads, uint64_t* hit_off, uin
   TRY(ensure_chunk(h, cfg));
   TRY(grow(h, h->d_hit_rpos, (size_t)cfg.ch * cfg.hcap));
   DevBuf<uint16_t> rpos_pool;
-  TRY(grow(h, rpos_pool, OVF_POOL_HITS));
+  TRY(grow(h, rpos_pool, ovf_pool_hits(h)));
   CK(cudaMemsetAsync(h->d_cnt32.p, 0, 16 * 4, h->st));
   std::vector<uint32_t> cnt, need, ovf;
   std::vector<uint8_t> over, rep;
