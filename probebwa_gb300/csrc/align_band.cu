@@ -244,6 +244,11 @@ __device__ __forceinline__ uint32_t band_step(int32_t (&PM)[C], int32_t (&PI)[C]
   return word;
 }
 
+template <bool B>
+struct BoolConst {
+  static constexpr bool value = B;
+};
+
 template <int C, int G, int TSTAR>
 __global__ void __launch_bounds__(32, 16) k_align_band(AlignArgs p, BandLayout LY) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -399,16 +404,19 @@ __global__ void __launch_bounds__(32, 16) k_align_band(AlignArgs p, BandLayout L
     for (int d = 16; d >= 1; d >>= 1) S0 = max(S0, __shfl_xor_sync(FULL, S0, d));
     S0 = min(S0, T);
     unsigned long long bestKey = 0;  // (value + 2^31) << 32 | j << 1 | state; 0 = none
-    for (int s = 0; s < T; s++) {
+    // one step: row i = R0 + s - k of this lane's columns, its traceback
+    // word, and on row R1 the endpoint candidates. The masked steps (s < S0)
+    // and the fast ones run as two loops, so neither carries the other's
+    // selects.
+    auto row = [&](int s, auto general) {
+      constexpr bool GEN = decltype(general)::value;
       const int i = R0 + s - k;
       const int ri = min(max(i - 1, -B_PADR), m - 1 + B_PADR);
       const int32_t rw = rowi[ri];
       const int32_t qsym = rw & 0xFF;
       const int32_t pen = rw >> 16;
       const int jb = min(max(i + base + k * C - 1, -B_PADC), n + B_PADC - C);
-      const uint32_t word =
-          s < S0 ? band_step<C, G, TSTAR, true>(PM, PI, PD, lo, sp, k, i, R0, kstar, qsym, pen, ge, coli + jb)
-                 : band_step<C, G, TSTAR, false>(PM, PI, PD, lo, sp, k, i, R0, kstar, qsym, pen, ge, coli + jb);
+      const uint32_t word = band_step<C, G, TSTAR, GEN>(PM, PI, PD, lo, sp, k, i, R0, kstar, qsym, pen, ge, coli + jb);
       if (i >= R0 && i <= R1) {
         store_tb<C>(tbg + (size_t)(i - R0) * ROWB, k, word);
         if (i == R1) {
@@ -425,7 +433,10 @@ __global__ void __launch_bounds__(32, 16) k_align_band(AlignArgs p, BandLayout L
           }
         }
       }
-    }
+    };
+    int s = 0;
+    for (; s < S0; s++) row(s, BoolConst<true>{});
+    for (; s < T; s++) row(s, BoolConst<false>{});
     for (int d = G / 2; d >= 1; d >>= 1) bestKey = max(bestKey, __shfl_xor_sync(FULL, bestKey, d, G));
     // the traceback rows written above, by every lane, are read back through
     // cp.async by the lanes of the same alignment

@@ -164,18 +164,22 @@ constexpr uint32_t SWISS_WARP_SLOTS = 512;  // buckets of the shared-memory repl
 // swiss_replay by one warp over shared memory (all 32 lanes call it): the
 // same insertions and rehashes (old buckets in bucket order), with each
 // probe group tested by the lanes together. aux holds 1280 words: ord, the
-// group slots in insertion order (<= 256, the input), the groups' keys in
-// that order (<= 256), the buckets (cap2 <= 512, each holding an insertion
-// index) and the rehash copy of the old buckets (<= 256). rank[g] receives
-// each group's iteration position and gk_by_rank[rank] its key.
+// group slots in insertion order (<= 256, the input), the low 32 bits of
+// their hashes (<= 256; tables of <= 512 buckets use no more), the buckets
+// (cap2 <= 512, each holding an insertion index) and the rehash copy of the
+// old buckets (<= 256). rank[g] receives each group's iteration position and
+// gk_by_rank[rank] its key.
 __device__ bool swiss_replay_warp(uint32_t G, const uint32_t* ggk, uint32_t* aux, uint32_t cap2, uint32_t* rank,
                                   uint32_t* gk_by_rank, int W, int lane) {
   constexpr uint32_t EMPTY = 0xFFFFFFFFu;
   const uint32_t* ord = aux;
-  uint32_t* gks = aux + 256;
+  uint32_t* hs = aux + 256;
   uint32_t* slots = aux + 512;
   uint32_t* olds = aux + 512 + SWISS_WARP_SLOTS;
-  for (uint32_t t = lane; t < G; t += 32) gks[t] = ggk[ord[t]];
+  for (uint32_t t = lane; t < G; t += 32) {
+    const uint32_t gk = ggk[ord[t]];
+    hs[t] = (uint32_t)fx_hash_group(gk >> 1, gk & 1u);
+  }
   __syncwarp();
   uint32_t nb = 0, items = 0;
   for (uint32_t t = 0; t < G; t++) {
@@ -190,15 +194,13 @@ __device__ bool swiss_replay_warp(uint32_t G, const uint32_t* ggk, uint32_t* aux
       for (uint32_t s = 0; s < nb; s++) {
         const uint32_t ot = olds[s];
         if (ot == EMPTY) continue;
-        const uint32_t ogk = gks[ot];
-        const uint32_t q = swiss_find_warp(slots, nnb, fx_hash_group(ogk >> 1, ogk & 1u), W, lane);
+        const uint32_t q = swiss_find_warp(slots, nnb, hs[ot], W, lane);
         if (lane == 0) slots[q] = ot;
         __syncwarp();
       }
       nb = nnb;
     }
-    const uint32_t gk = gks[t];
-    const uint32_t q = swiss_find_warp(slots, nb, fx_hash_group(gk >> 1, gk & 1u), W, lane);
+    const uint32_t q = swiss_find_warp(slots, nb, hs[t], W, lane);
     if (q == EMPTY) return false;
     if (lane == 0) slots[q] = t;
     __syncwarp();
@@ -211,10 +213,10 @@ __device__ bool swiss_replay_warp(uint32_t G, const uint32_t* ggk, uint32_t* aux
     const bool occ = s < nb && slots[s] != EMPTY;
     const unsigned b = __ballot_sync(0xffffffffu, occ);
     if (occ) {
-      const uint32_t t = slots[s];
+      const uint32_t g = ord[slots[s]];
       const uint32_t rr = rk + (uint32_t)__popc(b & ((1u << lane) - 1u));
-      rank[ord[t]] = rr;
-      gk_by_rank[rr] = gks[t];
+      rank[g] = rr;
+      gk_by_rank[rr] = ggk[g];
     }
     rk += (uint32_t)__popc(b);
   }
@@ -548,11 +550,16 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     }
   }
   __syncthreads();
-  // B. group iteration ranks: the groups in first-emission order (counting
-  // rank; first-emission indices are distinct) replayed through std's
-  // SwissTable insertion, by one warp in shared memory; more than 256 groups
-  // take the block-wide form in global scratch
+  // B + C. Warp 0 computes the group iteration ranks (B) while the other
+  // warps count the clusters (C) into keys that hold the group's slot; the
+  // ranks then replace the slots. When the group table has more slots than
+  // the key's rank field holds, B runs first and C writes ranks directly.
+  const bool overlap = TG <= KEY_RANK_MAX + 1;
   if (threadIdx.x < 32) {
+    // B: the groups in first-emission order (counting rank; first-emission
+    // indices are distinct) replayed through std's SwissTable insertion in
+    // shared memory; more than 256 groups take the block-wide form in global
+    // scratch
     unsigned long long* pairs = (unsigned long long*)(sh_aux + 512);  // 256 (first emission << 32 | slot)
     uint32_t G = 0;
     for (uint32_t g0 = 0; g0 < TG; g0 += 32) {
@@ -579,27 +586,50 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
         atomicExch(p.err, 1);
     }
   }
-  __syncthreads();
-  const uint32_t G = wtmp32[31];
-  if (G > 256) group_ranks_block(p, TG, gkey, gval, grk, X, sh_n);
-  if (threadIdx.x == 0) sh_n = 0;
-  __syncthreads();
-  // C. clusters: runs of joined bins, each counted from its first bin, its
-  // order key into ck
-  for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
-    const unsigned long long k = B.key[s];
-    if (k == BIN_EMPTY || !B.starts(s, k)) continue;
-    const uint32_t cnt = B.count(s, k);
-    const uint32_t gk = (uint32_t)(k >> 35);
-    const uint32_t rank = gval[find32(gkey, gk, TG)];
-    if (cnt > KEY_CNT_MAX || rank > KEY_RANK_MAX) wtmp32[30] = 1;
-    ck[atomicAdd(&sh_n, 1u)] = cluster_key(cnt, rank, k & M35);
+  if (!overlap) {
+    __syncthreads();
+    if (wtmp32[31] > 256) group_ranks_block(p, TG, gkey, gval, grk, X, sh_n);
+    if (threadIdx.x == 0) sh_n = 0;
+    __syncthreads();
+  }
+  // C: runs of joined bins, each counted from its first bin; T and the
+  // threads taking part are multiples of 32, so each warp claims its round's
+  // key slots with one atomic
+  if (!overlap || threadIdx.x >= 32) {
+    const uint32_t t0 = overlap ? 32u : 0u;
+    for (uint32_t s = threadIdx.x - t0; s < T; s += blockDim.x - t0) {
+      const unsigned long long k = B.key[s];
+      const bool start = k != BIN_EMPTY && B.starts(s, k);
+      uint32_t cnt = 0, field = 0;
+      if (start) {
+        cnt = B.count(s, k);
+        const uint32_t g = find32(gkey, (uint32_t)(k >> 35), TG);
+        field = overlap ? g : gval[g];
+        if (cnt > KEY_CNT_MAX || (!overlap && field > KEY_RANK_MAX)) wtmp32[30] = 1;
+      }
+      const unsigned em = __ballot_sync(0xffffffffu, start);
+      uint32_t kb = 0;
+      if (lane == 0 && em) kb = atomicAdd(&sh_n, (uint32_t)__popc(em));
+      kb = __shfl_sync(0xffffffffu, kb, 0);
+      if (start) ck[kb + (uint32_t)__popc(em & ((1u << lane) - 1u))] = cluster_key(cnt, field, k & M35);
+    }
   }
   __syncthreads();
   const uint32_t C = sh_n;
+  __syncthreads();  // every thread holds C before sh_n is counted again
+  if (overlap) {
+    if (wtmp32[31] > 256) group_ranks_block(p, TG, gkey, gval, grk, X, sh_n);
+    // group slot -> iteration rank in every key
+    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+      const unsigned long long v = ck[c];
+      const uint32_t rank = gval[(uint32_t)(v >> 35) & KEY_RANK_MAX];
+      if (rank > KEY_RANK_MAX) wtmp32[30] = 1;
+      ck[c] = (v & ~((unsigned long long)KEY_RANK_MAX << 35)) | ((unsigned long long)min(rank, KEY_RANK_MAX) << 35);
+    }
+    __syncthreads();
+  }
   const bool exact = wtmp32[30] != 0;
   const uint32_t nout = min(min(C, p.max_out), BIN_MAX_OUT);
-  __syncthreads();  // every thread holds C before sh_n is counted again
   // D. the first nout clusters in order. Fast path: the nout-th smallest key
   // by an MSB-first radix select (8 bits a pass; the keys are unique, so
   // exactly nout keys are <= it), then those keys sorted. Exact path: every
