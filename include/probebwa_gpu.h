@@ -122,6 +122,9 @@ typedef struct {
   uint64_t window_cells;      /* their DP cells (also in dp_cells) */
   double ms_compute;          /* device span of the mapping work, input copy and record copy excluded; the
                                  phases above overlap in paired calls, so their sum can exceed it */
+  double t_compute_begin_ms;  /* that span's ends on the device clock, in ms from an origin event the */
+  double t_compute_end_ms;    /* process records on the device when its first handle opens: the spans of
+                                 calls running at once on several handles merge as max(end) - min(begin) */
 } pbw_stats;
 
 void pbw_default_options(pbw_options* opt);

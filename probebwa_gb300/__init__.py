@@ -96,7 +96,7 @@ class StatsC(C.Structure):
                                            "ms_pair", "ms_d2h")] + \
                [(k, C.c_uint64) for k in ("seed_probes", "seed_entries", "seed_hits", "dp_jobs", "dp_cells",
                                           "kernel_launches", "window_jobs", "window_cells")] + \
-               [("ms_compute", C.c_double)]
+               [("ms_compute", C.c_double), ("t_compute_begin_ms", C.c_double), ("t_compute_end_ms", C.c_double)]
 
 
 _lib = None

@@ -496,7 +496,7 @@ template <int C, int G, int TSTAR>
 static void launch_band_c(const AlignArgs& a, int num_sms, cudaStream_t st) {
   const BandLayout LY = band_layout(a.lmax, a.nmax, G * C / 2);
   const size_t sm = LY.bytes * (32 / G);
-  cudaFuncSetAttribute(k_align_band<C, G, TSTAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_ceiling(k_align_band<C, G, TSTAR>);
   k_align_band<C, G, TSTAR><<<band_grid<C, G>(LY, num_sms), 32, sm, st>>>(a, LY);
 }
 

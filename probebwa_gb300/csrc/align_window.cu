@@ -475,10 +475,10 @@ __global__ void __launch_bounds__(WIN_THREADS, MINB) k_align_window(AlignArgs p,
 void launch_align_window(const AlignArgs& a, int grid, cudaStream_t st, bool wide) {
   const size_t sm = window_smem_bytes(a.lmax, a.nmax);
   if (wide) {
-    cudaFuncSetAttribute(k_align_window<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_ceiling(k_align_window<8, 1>);
     k_align_window<8, 1><<<std::max(1, grid / 2), WIN_THREADS, sm, st>>>(a, (unsigned int)sm);
   } else {
-    cudaFuncSetAttribute(k_align_window<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_ceiling(k_align_window<4, 2>);
     k_align_window<4, 2><<<grid, WIN_THREADS, sm, st>>>(a, (unsigned int)sm);
   }
 }

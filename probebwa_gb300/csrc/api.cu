@@ -390,6 +390,7 @@ int pbw_open(const char* genome_prefix, const char* hash_prefix, const pbw_optio
   h->num_sms = prop.multiProcessorCount;
   h->smem_optin = (size_t)prop.sharedMemPerBlockOptin;
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) { g_open_err = "stream"; return PBW_ERR_CUDA; }
+  if (!pbw::device_epoch(h->device)) { g_open_err = "epoch event"; return PBW_ERR_CUDA; }
   int rc = load_genome(h.get(), genome_prefix);
   if (rc == PBW_OK) rc = load_hash(h.get(), hash_prefix ? hash_prefix : genome_prefix);
   if (rc == PBW_OK) rc = build_tables(h.get());

@@ -911,7 +911,7 @@ size_t cluster_list_bytes_per_hit(uint32_t hcap, uint32_t gmax) {
 template <bool GT, bool FEAT>
 static int bins_blocks_per_sm(uint32_t hmax, uint32_t gmax, int threads) {
   const size_t sm = GT ? 0 : bin_table_bytes(hmax, gmax, FEAT);
-  if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (!GT) smem_ceiling(k_cluster_bins<GT, FEAT>);
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cluster_bins<GT, FEAT>, threads, sm) != cudaSuccess) n = 1;
   return std::max(n, 1);
@@ -929,7 +929,7 @@ int cluster_bins_grid(uint32_t hmax, uint32_t gmax, int threads, bool feat, int 
 template <bool GT, bool FEAT>
 static void launch_bins(const ClusterArgs& a, uint32_t hmax, int threads, int grid, size_t slab, cudaStream_t st) {
   const size_t sm = GT ? 0 : bin_table_bytes(hmax, a.gmax, FEAT);
-  if (!GT) cudaFuncSetAttribute(k_cluster_bins<GT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (!GT) smem_ceiling(k_cluster_bins<GT, FEAT>);
   k_cluster_bins<GT, FEAT><<<grid, threads, sm, st>>>(a, hmax, slab);
 }
 

@@ -17,6 +17,10 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <set>
+#include <utility>
+
 namespace pbw {
 
 constexpr int KMER = 15;
@@ -101,5 +105,28 @@ struct DevTables {
   int32_t ln_n_max;            // entries in ln_n
   int32_t gc_tmax;             // totals covered by gc tables
 };
+
+// Dynamic shared-memory limit of a kernel: once per kernel and device, the
+// device's per-block maximum less the kernel's static shared memory. The
+// limit is only a ceiling (each launch's occupancy follows its own size), and
+// one value for every launch keeps launches from several host threads (one
+// handle each) from lowering it under one another.
+inline void smem_ceiling_impl(const void* fn) {
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> g(mu);
+  if (!done.insert({fn, dev}).second) return;
+  int mx = 0;
+  cudaFuncAttributes a{};
+  if (cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return;
+  if (cudaFuncGetAttributes(&a, fn) != cudaSuccess) return;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - (int)a.sharedSizeBytes);
+}
+template <class K>
+inline void smem_ceiling(K* kernel) {
+  smem_ceiling_impl((const void*)kernel);
+}
 
 }  // namespace pbw

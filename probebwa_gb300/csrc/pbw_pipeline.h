@@ -50,6 +50,10 @@ struct HostBuf {
   }
 };
 
+// The process's origin event on a device (recorded when the first handle
+// on it opens); nullptr if it cannot be created.
+cudaEvent_t device_epoch(int dev);
+
 }  // namespace pbw
 
 struct pbw_handle {

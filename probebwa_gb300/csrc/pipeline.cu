@@ -200,6 +200,33 @@ static double ms_between(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+// The process's origin on each device's clock: an event recorded and
+// completed when the first handle on the device opens. Calls report their
+// compute span against it, so the spans of calls running at once on several
+// handles can be merged.
+cudaEvent_t device_epoch(int dev) {
+  static std::mutex mu;
+  static cudaEvent_t ev[64] = {};
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> g(mu);
+  if (!ev[dev]) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    if (cudaEventRecord(e, 0) != cudaSuccess || cudaEventSynchronize(e) != cudaSuccess) {
+      cudaEventDestroy(e);
+      return nullptr;
+    }
+    ev[dev] = e;
+  }
+  return ev[dev];
+}
+static void set_compute_span(pbw_handle* h, cudaEvent_t a, cudaEvent_t b) {
+  h->stats.ms_compute = ms_between(a, b);
+  cudaEvent_t o = device_epoch(h->device);
+  h->stats.t_compute_begin_ms = o ? ms_between(o, a) : 0.0;
+  h->stats.t_compute_end_ms = o ? ms_between(o, b) : 0.0;
+}
+
 // Buffers receiving one read set's candidates and seeded alignments.
 struct MateBufs {
   Cand* cand;
@@ -747,7 +774,7 @@ static int map_single_dev(pbw_handle* h, const uint8_t* d_bases, const uint8_t* 
   CK(cudaEventRecord(e2, h->st));
   CK(cudaStreamSynchronize(h->st));
   h->stats.ms_d2h = ms_between(e1, e2);
-  h->stats.ms_compute = ms_between(e0, e1);
+  set_compute_span(h, e0, e1);
   return PBW_OK;
 }
 
@@ -1134,7 +1161,7 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
     t_pair += ms_between(evB(s)[0], evB(s)[1]);
     t_fin += ms_between(evB(s)[1], evB(s)[2]);
   }
-  const double t_span = ms_between(E[0], evB((int)((chunks.size() - 1) & 1))[2]);
+  set_compute_span(h, E[0], evB((int)((chunks.size() - 1) & 1))[2]);
   TRY(check_device_errors(h));
   h->stats.ms_seed = t_seed;
   h->stats.ms_cluster = t_cl;
@@ -1184,7 +1211,6 @@ static int map_paired_dev(pbw_handle* h, pbw_insert_model* model, const uint8_t*
   CK(cudaEventRecord(e2, st));
   CK(cudaStreamSynchronize(st));
   h->stats.ms_d2h = ms_between(e1, e2);
-  h->stats.ms_compute = t_span;
   model->mean = pm.mean;
   model->sd = pm.sd;
   model->n_observed = pm.n;

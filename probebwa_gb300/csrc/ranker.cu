@@ -390,7 +390,7 @@ void launch_rank_train_step(const float* feat, const uint8_t* label, uint64_t n,
                             uint64_t stride_mul, const float* norm, const float* w, float* grad, double w_pos,
                             double w_neg, float* loss_acc, cudaStream_t st) {
   const size_t sm = rank_train_smem();
-  cudaFuncSetAttribute(k_rank_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_ceiling(k_rank_train);
   const unsigned blocks = (count + TR_T - 1) / TR_T;
   k_rank_train<<<blocks, TR_T, sm, st>>>(feat, label, n, first, count, stride_mul, norm, w, grad, (float)w_pos,
                                          (float)w_neg, loss_acc);

@@ -387,14 +387,14 @@ void launch_ovf_offsets(const uint32_t* list, const unsigned int* list_n, const 
 void launch_seed_list(const SeedArgs& a, int grid, cudaStream_t st) {
   const int threads = 256;
   size_t sm = seed_smem_per_warp(a.lmax) * (threads / 32);
-  cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_ceiling(k_seed);
   k_seed<<<grid, threads, sm, st>>>(a);
 }
 
 void launch_seed(const SeedArgs& a, int grid, cudaStream_t st) {
   const int threads = 256;
   size_t sm = seed_smem_per_warp(a.lmax) * (threads / 32);
-  cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_ceiling(k_seed);
   k_seed<<<grid, threads, sm, st>>>(a);
 }
 
