@@ -161,6 +161,74 @@ __device__ __forceinline__ uint32_t swiss_find_warp(const uint32_t* t, uint32_t 
 
 constexpr uint32_t SWISS_WARP_SLOTS = 512;  // buckets of the shared-memory replay (groups <= 256)
 
+// swiss_find over a table of nb <= 64 buckets held as an occupancy mask:
+// the first empty bucket of the circular scan (nb <= W) or of the first
+// probe group with one (triangular probing), by bit rotation.
+__device__ __forceinline__ uint32_t swiss_find_mask(unsigned long long occ, uint32_t nb, uint32_t h, int W) {
+  const uint32_t mask = nb - 1;
+  const unsigned long long all = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
+  const unsigned long long fr = ~occ & all;
+  uint32_t pos = h & mask;
+  auto rot = [&](uint32_t p0) -> unsigned long long {  // free buckets from p0 on, circularly
+    return p0 ? ((fr >> p0) | (fr << (nb - p0))) & all : fr;
+  };
+  if (nb <= (uint32_t)W) {
+    const unsigned long long r = rot(pos);
+    return r ? (pos + (uint32_t)__ffsll((long long)r) - 1) & mask : 0u;
+  }
+  const unsigned long long gm = (1ull << W) - 1ull;
+  uint32_t stride = 0;
+  for (uint32_t guard = 0; guard <= nb; guard++) {
+    const unsigned long long r = rot(pos) & gm;
+    if (r) return (pos + (uint32_t)__ffsll((long long)r) - 1) & mask;
+    stride += W;
+    pos = (pos + stride) & mask;
+  }
+  return 0xFFFFFFFFu;
+}
+
+constexpr uint32_t SWISS_MASK_GROUPS = 56;  // the largest table of 56 items has 64 buckets
+
+// swiss_replay of at most 56 groups by one thread: occupancy in a 64-bit
+// mask, bucket contents (insertion indices) in slots[64], the rehash copy in
+// olds[64]; hs[t] the low 32 bits of insertion t's hash, ord[t] its group
+// slot. Same insertions, rehashes (old buckets in bucket order) and ranks as
+// swiss_replay.
+__device__ bool swiss_replay_mask(uint32_t G, const uint32_t* ord, const uint32_t* hs, const uint32_t* ggk,
+                                  uint32_t* slots, uint32_t* olds, uint32_t* rank, uint32_t* gk_by_rank, int W) {
+  unsigned long long occ = 0;
+  uint32_t nb = 0, items = 0;
+  for (uint32_t t = 0; t < G; t++) {
+    if (items + 1 > swiss_cap(nb)) {
+      const uint32_t need = max(items + 1, swiss_cap(nb) + 1);
+      const uint32_t nnb = swiss_buckets(need);
+      if (nnb > 64) return false;
+      const unsigned long long old = occ;
+      for (uint32_t s = 0; s < nb; s++) olds[s] = slots[s];
+      occ = 0;
+      for (unsigned long long m = old; m; m &= m - 1) {
+        const uint32_t ot = olds[__ffsll((long long)m) - 1];
+        const uint32_t q = swiss_find_mask(occ, nnb, hs[ot], W);
+        occ |= 1ull << q;
+        slots[q] = ot;
+      }
+      nb = nnb;
+    }
+    const uint32_t q = swiss_find_mask(occ, nb, hs[t], W);
+    if (q == 0xFFFFFFFFu) return false;
+    occ |= 1ull << q;
+    slots[q] = t;
+    items++;
+  }
+  uint32_t rk = 0;
+  for (unsigned long long m = occ; m; m &= m - 1) {
+    const uint32_t g = ord[slots[__ffsll((long long)m) - 1]];
+    rank[g] = rk;
+    gk_by_rank[rk++] = ggk[g];
+  }
+  return true;
+}
+
 // swiss_replay by one warp over shared memory (all 32 lanes call it): the
 // same insertions and rehashes (old buckets in bucket order), with each
 // probe group tested by the lanes together. aux holds 1280 words: ord, the
@@ -181,6 +249,11 @@ __device__ bool swiss_replay_warp(uint32_t G, const uint32_t* ggk, uint32_t* aux
     hs[t] = (uint32_t)fx_hash_group(gk >> 1, gk & 1u);
   }
   __syncwarp();
+  if (G <= SWISS_MASK_GROUPS) {
+    bool ok = true;
+    if (lane == 0) ok = swiss_replay_mask(G, ord, hs, ggk, slots, olds, rank, gk_by_rank, W);
+    return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+  }
   uint32_t nb = 0, items = 0;
   for (uint32_t t = 0; t < G; t++) {
     if (items + 1 > swiss_cap(nb)) {
@@ -281,11 +354,14 @@ __host__ __device__ inline uint32_t grp_tsize(uint32_t H, uint32_t gmax) {
   return np2(g < 8 ? 16 : 2 * g);
 }
 
+// Slot of a key in a table of T slots (any T): two 32-bit multiplicative
+// mixes (the low word carries the bin, the high word the group and the
+// bin's top bits), the high bits of the product scaled to T.
 __device__ __forceinline__ uint32_t hash_slot(unsigned long long key, uint32_t T) {
-  unsigned long long k = key ^ (key >> 33);
-  k *= 0xff51afd7ed558ccdull;
-  k ^= k >> 33;
-  return (uint32_t)(((k & 0xFFFFFFFFull) * T) >> 32);  // any T
+  uint32_t h = (uint32_t)key * 0x9E3779B1u ^ (uint32_t)(key >> 32) * 0x85EBCA77u;
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  return __umulhi(h, T);
 }
 
 // Slot of key in an open-addressed table of T (a power of two) 64-bit keys,
@@ -527,8 +603,18 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
     const unsigned long long w = hits[i];
     const unsigned long long d = w & M40;
-    const unsigned long long b = d / BIN_W;
-    const uint32_t off = (uint32_t)(d - b * BIN_W);
+    // diagonal / 51 in 32 bits while the diagonal fits (every contig under
+    // 4 Gbp), in 64 bits otherwise
+    unsigned long long b;
+    uint32_t off;
+    if (d < (1ull << 32)) {
+      const uint32_t b32 = (uint32_t)d / (uint32_t)BIN_W;
+      b = b32;
+      off = (uint32_t)d - b32 * (uint32_t)BIN_W;
+    } else {
+      b = d / BIN_W;
+      off = (uint32_t)(d - b * BIN_W);
+    }
     const uint32_t gk = (uint32_t)(w >> 40);
     const uint32_t s = insert64(B.key, ((unsigned long long)gk << 35) | b, T);
     const uint32_t g = insert32(gkey, gk, TG);
