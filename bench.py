@@ -901,10 +901,11 @@ class HgWorkload:
                 pe = S.reads(seed + 1001 + 2 * c, names, lens, codes, args.hg_pairs, 250, paired=True, mean=300.0,
                              sd=80.0, trim=(60, 250), g_dev=g)
                 self.chunks.append({"se": se, "pe": pe})
-            tr_se = S.reads(seed + 99, names, lens, codes, args.train_reads // 2, 250, trim=(60, 250), g_dev=g)
-            tr_pe = S.reads(seed + 98, names, lens, codes, args.train_reads // 4, 250, paired=True, mean=300.0,
-                            sd=80.0, trim=(60, 250), g_dev=g)
-            self.train = {"se": tr_se, "pe": tr_pe}
+            if args.train_reads:
+                tr_se = S.reads(seed + 99, names, lens, codes, args.train_reads // 2, 250, trim=(60, 250), g_dev=g)
+                tr_pe = S.reads(seed + 98, names, lens, codes, args.train_reads // 4, 250, paired=True, mean=300.0,
+                                sd=80.0, trim=(60, 250), g_dev=g)
+                self.train = {"se": tr_se, "pe": tr_pe}
             self.insert = (300.0, 80.0)
         else:
             self.n_chunks = args.hg_chunks
@@ -913,7 +914,9 @@ class HgWorkload:
             for c in range(self.n_chunks):
                 pe = S.reads(seed + 1001 + 2 * c, names, lens, codes, args.stress_pairs, 250, **kw)
                 self.chunks.append({"se": None, "pe": pe})
-            self.train = {"se": None, "pe": S.reads(seed + 98, names, lens, codes, args.train_reads // 2, 250, **kw)}
+            if args.train_reads:
+                self.train = {"se": None, "pe": S.reads(seed + 98, names, lens, codes, args.train_reads // 2, 250,
+                                                        **kw)}
             self.insert = (500.0, 120.0)
         del g
         torch.cuda.empty_cache()
@@ -1308,6 +1311,21 @@ def run_hg(args, rank, world):
     return out
 
 
+def run_stage_hgstep(args):
+    """One step of the 3.1 Gbp workload (chunk 0: the single-end call, then
+    the paired call) and the calls' stats; with --hg-chunks 1 --train-reads 0
+    it generates only that chunk. The profiles of the 3.1 Gbp workload run
+    this under ncu."""
+    import probebwa_gb300 as P
+    W = HgWorkload(args, args.config)
+    inputs = _hg_inputs(P, W)
+    R = HgRunner(P, W, inputs, concurrent=False)
+    reads, dev, e2e, stats = R.step(0)
+    R.close()
+    return {"stage": "hgstep", "config": W.meta(), "reads": int(reads), "device_ms": round(dev, 2),
+            "e2e_ms": round(e2e, 2), "calls": stats}
+
+
 def small_parity(args, cfg):
     """The GPU path against the oracle on the whole single-end configuration
     (cfg 0, 10,000 reads) or on 40,000 pairs of the paired one (cfg 1)."""
@@ -1419,9 +1437,10 @@ def main():
     ap.add_argument("--small-parity", type=int, default=1, help="add configs 0 / 1 parity to the config 2 line")
     ap.add_argument("--ref-se", type=int, default=8_000)
     ap.add_argument("--ref-pairs", type=int, default=4_000)
-    ap.add_argument("--stage", default="map", choices=["map", "index", "sam", "cli", "batch"],
+    ap.add_argument("--stage", default="map", choices=["map", "index", "sam", "cli", "batch", "hgstep"],
                     help="map: the mapping path (default); index / sam / cli: build-hash, SAM output and the "
-                         "command line, each against the oracle")
+                         "command line, each against the oracle; hgstep: one step of configs 2-4 (the single-end "
+                         "and the paired call of chunk 0, once each) and its stats, the case the profiles capture")
     args = ap.parse_args()
     hg = args.config in (2, 3, 4)
     if args.label_cut is None:
@@ -1441,6 +1460,10 @@ def main():
     if args.stage == "batch":
         if rank == 0:
             print(json.dumps(run_stage_batch(args)), flush=True)
+        return
+    if args.stage == "hgstep":
+        if rank == 0:
+            print(json.dumps(run_stage_hgstep(args)), flush=True)
         return
     if args.stage != "map":
         if rank != 0:

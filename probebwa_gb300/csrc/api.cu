@@ -238,8 +238,21 @@ int load_genome(pbw_handle* h, const std::string& prefix) {
   const size_t nwords = std::max<size_t>(words.size(), 1);
   words.resize(nwords, 0);
   nmask.resize(nwords, 0);
+  // one bit per 1024-base block (32 mask words): whether the block holds an
+  // N; ~380 KB for 3.1 Gbp, so it stays in L2 while the seeding kernel skips
+  // the N-mask words of N-free blocks
+  const size_t nblocks = (nwords + 31) / 32;
+  std::vector<uint32_t> nblk((nblocks + 31) / 32, 0u);
+  for (size_t b = 0; b < nblocks; b++) {
+    uint32_t any = 0;
+    const size_t e = std::min(nwords, (b + 1) * 32);
+    for (size_t w = b * 32; w < e; w++) any |= nmask[w];
+    if (any) nblk[b >> 5] |= 1u << (b & 31);
+  }
   TRY(dev_alloc(h, h->d_bits, nwords));
   TRY(dev_alloc(h, h->d_nmask, nwords));
+  TRY(dev_alloc(h, h->d_nblk, nblk.size()));
+  CK(cudaMemcpy(h->d_nblk.p, nblk.data(), nblk.size() * 4, cudaMemcpyHostToDevice));
   TRY(dev_alloc(h, h->d_cbase, std::max<size_t>(nc, 1)));
   TRY(dev_alloc(h, h->d_clen, std::max<size_t>(nc, 1)));
   TRY(dev_alloc(h, h->d_name_class, std::max<size_t>(nc, 1)));
@@ -252,6 +265,7 @@ int load_genome(pbw_handle* h, const std::string& prefix) {
   }
   h->G.bits = h->d_bits.p;
   h->G.nmask = h->d_nmask.p;
+  h->G.nblk = h->d_nblk.p;
   h->G.cbase = h->d_cbase.p;
   h->G.clen = h->d_clen.p;
   h->G.name_class = h->d_name_class.p;

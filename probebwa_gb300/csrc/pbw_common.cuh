@@ -62,6 +62,7 @@ __host__ __device__ __forceinline__ uint8_t comp_ascii(uint8_t b) {
 struct DevGenome {
   const unsigned long long* bits;
   const unsigned int* nmask;
+  const unsigned int* nblk;         // 1 bit per 1024-base block (32 nmask words): the block holds an N
   const unsigned long long* cbase;  // per contig: global base offset
   const unsigned long long* clen;   // per contig: length
   const int* name_class;            // per contig: first contig index with the same name

@@ -72,6 +72,7 @@ struct pbw_handle {
   // index
   pbw::DevBuf<unsigned long long> d_bits;
   pbw::DevBuf<unsigned int> d_nmask;
+  pbw::DevBuf<unsigned int> d_nblk;  // 1 bit per 1024-base block: holds an N
   pbw::DevBuf<unsigned long long> d_cbase, d_clen;
   pbw::DevBuf<int> d_name_class;
   pbw::DevBuf<unsigned int> d_csr;

@@ -51,7 +51,8 @@ __device__ __forceinline__ bool nb_probed(int rp, int L) {
 // hit). Read counts come from the read's prefix counts (pc4: four 16-bit
 // fields A C G T per position), genome counts from the 27-base window
 // [ref_pos - 4, ref_pos + 23) read as 2-bit words, by mask and popcount, N
-// bases (the contig's N runs) counting as none of the four.
+// bases (the contig's N runs) counting as none of the four; the N-mask words
+// are read only for 1024-base blocks that hold an N.
 __device__ __forceinline__ bool similarity_ok(const DevGenome& G, const unsigned long long* pc4, int L, int rp,
                                               bool rev, uint32_t cid, uint64_t ref_pos, bool neighbour) {
   constexpr int k = KMER;
@@ -72,13 +73,17 @@ __device__ __forceinline__ bool similarity_ok(const DevGenome& G, const unsigned
   const uint32_t sh = (uint32_t)(gs & 31);
   const uint64_t wi = gs >> 5;
   unsigned long long X = __ldg(&G.bits[wi]);
-  uint32_t NM = __ldg(&G.nmask[wi]);
+  // the N-mask words only where the window's 1024-base blocks hold an N
+  const uint64_t b0 = wi >> 5, b1 = (wi + 1) >> 5;
+  const bool has_n = ((__ldg(&G.nblk[b0 >> 5]) >> (b0 & 31)) & 1u) != 0 ||
+                     (sh > 5 && ((__ldg(&G.nblk[b1 >> 5]) >> (b1 & 31)) & 1u) != 0);
+  uint32_t NM = has_n ? __ldg(&G.nmask[wi]) : 0u;
   if (sh) {
     X >>= 2 * sh;
     NM >>= sh;
     if (sh > 5) {  // the window reaches into the next word
       X |= __ldg(&G.bits[wi + 1]) << (64 - 2 * sh);
-      NM |= __ldg(&G.nmask[wi + 1]) << (32 - sh);
+      if (has_n) NM |= __ldg(&G.nmask[wi + 1]) << (32 - sh);
     }
   }
   // bases 0-3 and 19-26 of the window, one bit per base at even positions
