@@ -1148,6 +1148,11 @@ def hg_oracle_sample(W, n_se, n_pairs, threads):
     return out, secs, reads, t_open
 
 
+# DRAM traffic of K1 per read on the 3.1 Gbp workload (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of a 131,072-read launch: 133.21 GB)
+SEED_TRAFFIC_PER_READ_HG = 133.212596736e9 / 131072
+
+
 def int32_peak():
     """Measured INT32 add and max throughput of this GPU (independent chains,
     CUDA events): G ops/s."""
@@ -1236,11 +1241,16 @@ def run_hg(args, rank, world):
                 for k in inputs[ci % W.n_chunks])
     n_launch_seed = sum(-(-(len(inputs[ci % W.n_chunks][k].offsets) - 1) // CHUNK_READS)
                         for ci in range(args.steps) for k in inputs[ci % W.n_chunks])
+    bases_reads = sum(len(inputs[ci % W.n_chunks][k].offsets) - 1 for ci in range(args.steps)
+                      for k in inputs[ci % W.n_chunks])
     seed_bytes = (bases + (bases + 3) // 4) + 8 * (s["seed_probes"] + s["seed_entries"] + s["seed_hits"])
     seed_gbs = seed_bytes / (s["ms_seed"] / 1e3) / 1e9 if s["ms_seed"] > 0 else 0.0
+    reads_per_launch = bases_reads / max(n_launch_seed, 1)
     roofline = {"kernel": "k_seed (K1 seeding)", "bound": "hbm", "achieved": round(seed_gbs, 1), "peak": hbm_peak,
-                "unit": "GB/s", "frac": round(seed_gbs / hbm_peak, 4), "traffic": None,
-                "traffic_note": "no ncu capture of this workload's seeding yet",
+                "unit": "GB/s", "frac": round(seed_gbs / hbm_peak, 4),
+                "traffic": int(SEED_TRAFFIC_PER_READ_HG * reads_per_launch),
+                "traffic_note": "DRAM bytes per launch: 1.016 MB per read (ncu dram__bytes_read + dram__bytes_write "
+                                "of a 131,072-read launch of this workload) x the reads of a launch",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst), of measured" if peaks else "fallback 6800 GB/s",
                 "algorithmic_bytes_per_launch": int(seed_bytes / max(n_launch_seed, 1)),
                 "launches_in_timed_region": int(n_launch_seed)}

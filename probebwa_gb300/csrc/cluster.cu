@@ -486,6 +486,10 @@ struct BinTab {
 // bin (35 bits); unique per cluster. Counts above 0xFFFF or ranks above
 // 0x1FFF take the exact path instead.
 constexpr uint32_t KEY_CNT_MAX = 0xFFFFu, KEY_RANK_MAX = 0x1FFFu;
+// Bin links: 16-bit slot indices, so tables of up to 32767 slots
+// (LINK_NONE ends a cluster).
+constexpr uint32_t LINK_MAX_SLOTS = 32767u;
+constexpr uint16_t LINK_NONE = 0xFFFFu;
 __device__ __forceinline__ unsigned long long cluster_key(uint32_t cnt, uint32_t rank, unsigned long long b0) {
   return ((unsigned long long)(KEY_CNT_MAX - min(cnt, KEY_CNT_MAX)) << 48) |
          ((unsigned long long)min(rank, KEY_RANK_MAX) << 35) | b0;
@@ -593,6 +597,10 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
       B.rmx[s] = 0;
     }
   }
+  if (T <= LINK_MAX_SLOTS) {
+    uint32_t* jw = (uint32_t*)((unsigned char*)ck + 5 * (size_t)T);  // the joined bytes, T/4 words
+    for (uint32_t s = threadIdx.x; s < T / 4; s += blockDim.x) jw[s] = 0;
+  }
   if (threadIdx.x == 0) {
     sh_n = 0;
     wtmp32[30] = 0;  // exact-path flag
@@ -636,16 +644,22 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     }
   }
   __syncthreads();
-  // B + C. Warp 0 computes the group iteration ranks (B) while the other
-  // warps count the clusters (C) into keys that hold the group's slot; the
-  // ranks then replace the slots. When the group table has more slots than
-  // the key's rank field holds, B runs first and C writes ranks directly.
-  const bool overlap = TG <= KEY_RANK_MAX + 1;
+  // B + C1. Warp 0 computes the group iteration ranks (B) while the other
+  // warps link the bins (C1): each occupied bin looks up its upper
+  // neighbour once, and when the two join, records the link (a 16-bit slot
+  // index in the cluster-key area's upper quarter) and marks the upper bin
+  // as joined from below (a byte per slot before it). Tables of more than
+  // 32767 slots (list mode only) keep no links: their walks look the
+  // neighbours up. The cluster keys written later take at most 5T of the
+  // area's 8T bytes (a read has at most H <= T / 1.6 clusters).
+  const bool linked = T <= LINK_MAX_SLOTS;
+  uint16_t* nxt = (uint16_t*)((unsigned char*)ck + 6 * (size_t)T);
+  uint8_t* joined = (unsigned char*)ck + 5 * (size_t)T;
   if (threadIdx.x < 32) {
     // B: the groups in first-emission order (counting rank; first-emission
     // indices are distinct) replayed through std's SwissTable insertion in
     // shared memory; more than 256 groups take the block-wide form in global
-    // scratch
+    // scratch after this phase
     unsigned long long* pairs = (unsigned long long*)(sh_aux + 512);  // 256 (first emission << 32 | slot)
     uint32_t G = 0;
     for (uint32_t g0 = 0; g0 < TG; g0 += 32) {
@@ -671,49 +685,47 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
       if (!swiss_replay_warp(G, gkey, sh_aux, max(16u, 2 * np2(G)), gval, grk, p.group_width, lane) && lane == 0)
         atomicExch(p.err, 1);
     }
+  } else if (linked) {
+    for (uint32_t s = threadIdx.x - 32; s < T; s += blockDim.x - 32) {
+      const unsigned long long k = B.key[s];
+      if (k == BIN_EMPTY) continue;
+      const unsigned long long b = k & M35;
+      const uint32_t q = B.next(k, b, b, B.mask(s));
+      nxt[s] = q == NO_SLOT ? LINK_NONE : (uint16_t)q;
+      if (q != NO_SLOT) joined[q] = 1;
+    }
   }
-  if (!overlap) {
-    __syncthreads();
-    if (wtmp32[31] > 256) group_ranks_block(p, TG, gkey, gval, grk, X, sh_n);
+  __syncthreads();
+  if (wtmp32[31] > 256) {
+    group_ranks_block(p, TG, gkey, gval, grk, X, sh_n);
     if (threadIdx.x == 0) sh_n = 0;
     __syncthreads();
   }
-  // C: runs of joined bins, each counted from its first bin; T and the
-  // threads taking part are multiples of 32, so each warp claims its round's
-  // key slots with one atomic
-  if (!overlap || threadIdx.x >= 32) {
-    const uint32_t t0 = overlap ? 32u : 0u;
-    for (uint32_t s = threadIdx.x - t0; s < T; s += blockDim.x - t0) {
-      const unsigned long long k = B.key[s];
-      const bool start = k != BIN_EMPTY && B.starts(s, k);
-      uint32_t cnt = 0, field = 0;
-      if (start) {
+  // C2: each cluster counted along its links from its first bin, its order
+  // key into ck (T and the block are multiples of 32, so each warp claims
+  // its round's key slots with one atomic)
+  for (uint32_t s = threadIdx.x; s < T; s += blockDim.x) {
+    const unsigned long long k = B.key[s];
+    const bool start = k != BIN_EMPTY && (linked ? joined[s] == 0 : B.starts(s, k));
+    uint32_t cnt = 0, rank = 0;
+    if (start) {
+      if (linked) {
+        for (uint32_t cur = s; cur != LINK_NONE; cur = nxt[cur]) cnt += B.cnt[cur];
+      } else {
         cnt = B.count(s, k);
-        const uint32_t g = find32(gkey, (uint32_t)(k >> 35), TG);
-        field = overlap ? g : gval[g];
-        if (cnt > KEY_CNT_MAX || (!overlap && field > KEY_RANK_MAX)) wtmp32[30] = 1;
       }
-      const unsigned em = __ballot_sync(0xffffffffu, start);
-      uint32_t kb = 0;
-      if (lane == 0 && em) kb = atomicAdd(&sh_n, (uint32_t)__popc(em));
-      kb = __shfl_sync(0xffffffffu, kb, 0);
-      if (start) ck[kb + (uint32_t)__popc(em & ((1u << lane) - 1u))] = cluster_key(cnt, field, k & M35);
+      rank = gval[find32(gkey, (uint32_t)(k >> 35), TG)];
+      if (cnt > KEY_CNT_MAX || rank > KEY_RANK_MAX) wtmp32[30] = 1;
     }
+    const unsigned em = __ballot_sync(0xffffffffu, start);
+    uint32_t kb = 0;
+    if (lane == 0 && em) kb = atomicAdd(&sh_n, (uint32_t)__popc(em));
+    kb = __shfl_sync(0xffffffffu, kb, 0);
+    if (start) ck[kb + (uint32_t)__popc(em & ((1u << lane) - 1u))] = cluster_key(cnt, rank, k & M35);
   }
   __syncthreads();
   const uint32_t C = sh_n;
   __syncthreads();  // every thread holds C before sh_n is counted again
-  if (overlap) {
-    if (wtmp32[31] > 256) group_ranks_block(p, TG, gkey, gval, grk, X, sh_n);
-    // group slot -> iteration rank in every key
-    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-      const unsigned long long v = ck[c];
-      const uint32_t rank = gval[(uint32_t)(v >> 35) & KEY_RANK_MAX];
-      if (rank > KEY_RANK_MAX) wtmp32[30] = 1;
-      ck[c] = (v & ~((unsigned long long)KEY_RANK_MAX << 35)) | ((unsigned long long)min(rank, KEY_RANK_MAX) << 35);
-    }
-    __syncthreads();
-  }
   const bool exact = wtmp32[30] != 0;
   const uint32_t nout = min(min(C, p.max_out), BIN_MAX_OUT);
   // D. the first nout clusters in order. Fast path: the nout-th smallest key
@@ -858,7 +870,7 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
         rmn = min(rmn, B.rmn[cur]);
         rmx = max(rmx, B.rmx[cur]);
       }
-      const uint32_t q = B.next(k, b0, cb, m);
+      const uint32_t q = linked ? (nxt[cur] == LINK_NONE ? NO_SLOT : (uint32_t)nxt[cur]) : B.next(k, b0, cb, m);
       if (q == NO_SLOT) break;
       cur = q;
       cb++;

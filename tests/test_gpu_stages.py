@@ -86,6 +86,33 @@ def _overflow_genome(tmp_path):
     return prefix, seqs + s2, quals + q2
 
 
+def _wide_group_genome(tmp_path):
+    """200 contigs, each with a 1 kbp unit forward and reverse-complemented:
+    a read from the unit hits ~400 (contig, strand) groups (the block-wide
+    group order of reads over 256 groups) and tens of thousands of hits
+    (list mode, tables too large for bin links)."""
+    from probebwa_gb300 import synth
+    rng = np.random.default_rng(311)
+    unit = synth.rand_codes(rng, 1000)
+    contigs = []
+    for c in range(200):
+        g = synth.rand_codes(rng, 4000)
+        g[500:1500] = synth.mutate_subs(rng, unit, 0.002)
+        g[2500:3500] = 3 - synth.mutate_subs(rng, unit, 0.002)[::-1]
+        contigs.append((f"w{c}", g))
+    prefix = str(tmp_path / "wide")
+    synth.write_index(prefix, contigs)
+    seqs, quals = [], []
+    for i in range(12):
+        s = int(rng.integers(0, 1000 - 100))
+        frag = unit[s:s + 100].copy()
+        if i % 2:
+            frag = 3 - frag[::-1]
+        seqs.append(synth.ASCII[frag].tobytes())
+        quals.append(bytes(rng.integers(20, 41, size=100).astype(np.uint8)))
+    return prefix, seqs, quals
+
+
 def _edge_reads(seqs, quals):
     """Reads the seeding loop treats specially: empty, shorter than k,
     exactly k, N runs and IUPAC letters inside windows, lower case."""
@@ -200,3 +227,10 @@ def test_overflow_pool_in_slices(P, oracle, tmp_path):
         assert tc[i] == len(e_c2) and cp[i, :k].tolist() == e_p2[:k].tolist(), i
     exp = om.map_single(oracle.Reads(R.bases, R.quals, R.offsets, R.ids))
     compare_records(P, oracle, got, exp, "sliced overflow pool")
+
+
+@pytest.mark.parametrize("group_width", [16, 8])
+def test_candidates_over_256_groups(P, oracle, tmp_path, group_width):
+    prefix, seqs, quals = _wide_group_genome(tmp_path)
+    tc, _ = _check_clusters(P, oracle, prefix, seqs, quals, group_width=group_width, max_per_read=256)
+    assert tc.min() > 256, "every read must have clusters in more than 256 groups"
