@@ -351,6 +351,10 @@ int pbw_build_hash(const char* genome_prefix, const char* out_prefix, uint64_t k
  *   clustering scratch hold two slices, so a smaller slice also takes less
  *   device memory. A chunk's over-capacity reads may hold 16 default slices in
  *   all, and one read one slice.
+ * k2_threads: K2 (clustering) runs each read as one block; for the two
+ *   largest hit-count tiers the autotuner times blocks of 1024, 512 and 256
+ *   threads on the handle's first chunk (same results; smaller blocks put
+ *   more reads in flight per SM) and keeps the fastest per tier.
  * pbw_set_tuning reads the inputs and clears the tuned choices. */
 typedef struct {
   int32_t autotune;
@@ -361,6 +365,10 @@ typedef struct {
   float tuned_ms[3][2];
   uint32_t wait_polls;
   uint32_t ovf_slice_hits;
+  int32_t k2_threads[2];      /* K2 block size for the 2049-4096-hit tier and the 4097-16384-hit tier
+                                 (tables in global slabs): 0 = tuned (or 1024), else 256, 512 or 1024 */
+  int32_t k2_chosen[2];       /* (read) the tuned block sizes, 0 = not tuned yet */
+  float k2_tuned_ms[2][3];    /* (read) the tuning trial's times for 1024, 512 and 256 threads */
 } pbw_tuning;
 int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t);
 int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t);

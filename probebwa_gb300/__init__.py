@@ -84,7 +84,8 @@ class RankerReportC(C.Structure):
 class TuningC(C.Structure):
     _fields_ = [("autotune", C.c_int32), ("band_lanes", C.c_int32), ("length_bins", C.c_int32),
                 ("pair_graphs", C.c_int32), ("chosen_lanes", C.c_int32 * 3), ("tuned_ms", (C.c_float * 2) * 3),
-                ("wait_polls", C.c_uint32), ("ovf_slice_hits", C.c_uint32)]
+                ("wait_polls", C.c_uint32), ("ovf_slice_hits", C.c_uint32), ("k2_threads", C.c_int32 * 2),
+                ("k2_chosen", C.c_int32 * 2), ("k2_tuned_ms", (C.c_float * 3) * 2)]
 
 
 class InsertModelC(C.Structure):
@@ -551,15 +552,20 @@ class Mapper:
         return {"autotune": t.autotune, "band_lanes": t.band_lanes, "length_bins": t.length_bins,
                 "pair_graphs": t.pair_graphs, "chosen_lanes": list(t.chosen_lanes),
                 "tuned_ms": [list(r) for r in t.tuned_ms], "wait_polls": t.wait_polls,
-                "ovf_slice_hits": t.ovf_slice_hits}
+                "ovf_slice_hits": t.ovf_slice_hits, "k2_threads": list(t.k2_threads),
+                "k2_chosen": list(t.k2_chosen), "k2_tuned_ms": [list(r) for r in t.k2_tuned_ms]}
 
     def set_tuning(self, **kw):
         """pbw_set_tuning: autotune, band_lanes (0, 8, 16), length_bins, pair_graphs, wait_polls,
-        ovf_slice_hits."""
+        ovf_slice_hits, k2_threads (two of 0, 256, 512, 1024)."""
         t = TuningC()
         self._check(lib().pbw_get_tuning(self.h, C.byref(t)))
         for k, v in kw.items():
-            setattr(t, k, int(v))
+            if k == "k2_threads":
+                for i, x in enumerate(v):
+                    t.k2_threads[i] = int(x)
+            else:
+                setattr(t, k, int(v))
         self._check(lib().pbw_set_tuning(self.h, C.byref(t)))
 
     def ranker_train(self, r1: Reads, r2: Reads | None = None, **kw) -> dict:

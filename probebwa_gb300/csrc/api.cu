@@ -454,6 +454,11 @@ int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t) {
     t->tuned_ms[c][0] = T.ms[c][0];
     t->tuned_ms[c][1] = T.ms[c][1];
   }
+  for (int i = 0; i < 2; i++) {
+    t->k2_threads[i] = T.k2_threads[i];
+    t->k2_chosen[i] = T.k2_chosen[i];
+    for (int j = 0; j < 3; j++) t->k2_tuned_ms[i][j] = T.k2_ms[i][j];
+  }
   return PBW_OK;
 }
 
@@ -462,6 +467,13 @@ int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t) {
   if (t->band_lanes != 0 && t->band_lanes != 8 && t->band_lanes != 16) {
     h->err = "pbw_set_tuning: band_lanes must be 0, 8 or 16";
     return PBW_ERR_ARG;
+  }
+  for (int i = 0; i < 2; i++) {
+    const int k = t->k2_threads[i];
+    if (k != 0 && k != 256 && k != 512 && k != 1024) {
+      h->err = "pbw_set_tuning: k2_threads must be 0, 256, 512 or 1024";
+      return PBW_ERR_ARG;
+    }
   }
   auto& T = h->tune;
   T.autotune = t->autotune != 0;
@@ -473,6 +485,11 @@ int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t) {
   for (int c = 0; c < 3; c++) {
     T.chosen[c] = 0;
     T.ms[c][0] = T.ms[c][1] = 0.f;
+  }
+  for (int i = 0; i < 2; i++) {
+    T.k2_threads[i] = t->k2_threads[i];
+    T.k2_chosen[i] = 0;
+    for (int j = 0; j < 3; j++) T.k2_ms[i][j] = 0.f;
   }
   return PBW_OK;
 }

@@ -1016,10 +1016,12 @@ static int bins_blocks_per_sm(uint32_t hmax, uint32_t gmax, int threads) {
 }
 
 // Resident blocks of the binned K2 on num_sms SMs (the kernel loops over
-// reads, so its grid is what fits at once); the table-in-slab tier runs one
-// block per SM.
+// reads, so its grid is what fits at once): by shared memory for tables in
+// shared memory, by registers and threads for tables in the global slab.
 int cluster_bins_grid(uint32_t hmax, uint32_t gmax, int threads, bool feat, int num_sms) {
-  if (cluster_bins_in_slab(hmax, gmax, feat)) return num_sms;
+  if (cluster_bins_in_slab(hmax, gmax, feat))
+    return num_sms * (feat ? bins_blocks_per_sm<true, true>(hmax, gmax, threads)
+                           : bins_blocks_per_sm<true, false>(hmax, gmax, threads));
   return num_sms * (feat ? bins_blocks_per_sm<false, true>(hmax, gmax, threads)
                          : bins_blocks_per_sm<false, false>(hmax, gmax, threads));
 }

@@ -155,6 +155,9 @@ struct pbw_handle {
     float ms[3][2] = {{0, 0}, {0, 0}, {0, 0}};
     uint32_t wait_polls = 0;  // window-DP wavefront waits: polls before giving up (0 = the kernel's default)
     uint32_t ovf_slice_hits = 0;  // over-capacity reads: hits per pool slice (0 = the default, 16 M)
+    int k2_threads[2] = {0, 0};   // K2 block size of the 4096-hit and the slab tier: 0 tuned, else forced
+    int k2_chosen[2] = {0, 0};    // tuned block sizes (0: not tuned)
+    float k2_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // the trial: 1024, 512, 256 threads
   } tune;
   int call_lmin = 0;        // shortest read of the current call
   pbw::DevBuf<pbw::AlnJob> d_jobs_b;

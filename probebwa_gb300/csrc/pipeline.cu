@@ -74,6 +74,10 @@ struct BinTier {
 };
 constexpr BinTier BIN_TIERS[5] = {{512, 128}, {1024, 256}, {2048, 512}, {4096, 1024}, {0, 1024}};
 static uint32_t group_keys(const pbw_handle* h) { return 2u * std::max(h->G.ncontig, 1u); }
+// The tiers whose block size the autotuner picks (the 4096-hit tier and the
+// slab tier), and the sizes it tries.
+static int k2_tuned_tier(const BinTier& t) { return t.hmax == 4096 ? 0 : (t.hmax == 0 ? 1 : -1); }
+constexpr int K2_TRIAL_THREADS[3] = {1024, 512, 256};
 static size_t cluster_scratch_bytes(const pbw_handle* h, uint32_t hcap) {
   size_t need = 0;
   uint32_t lo = 0;
@@ -84,8 +88,11 @@ static size_t cluster_scratch_bytes(const pbw_handle* h, uint32_t hcap) {
     const uint32_t hx = t.hmax ? t.hmax : hcap;
     for (const bool feat : {false, true}) {
       const bool gt = cluster_bins_in_slab(hx, gm, feat);
-      need = std::max(need, cluster_bins_slab_bytes(hx, gm, gt) *
-                                (size_t)cluster_bins_grid(hx, gm, t.threads, feat, h->num_sms));
+      for (int i = 0; i < 3; i++) {
+        const int thr = k2_tuned_tier(t) >= 0 ? K2_TRIAL_THREADS[i] : t.threads;
+        need = std::max(need, cluster_bins_slab_bytes(hx, gm, gt) *
+                                  (size_t)cluster_bins_grid(hx, gm, thr, feat, h->num_sms));
+      }
     }
     lo = hm;
   }
@@ -380,6 +387,7 @@ static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* base
   }
   // reads within the per-read buffer, by hit-count tier
   uint32_t lo = 0;
+  auto& T = h->tune;
   for (const BinTier& t : BIN_TIERS) {
     const uint32_t hm = t.hmax ? std::min(t.hmax, cfg.hcap) : cfg.hcap;
     if (hm <= lo) continue;
@@ -388,9 +396,31 @@ static int cluster_phase(pbw_handle* h, const ChunkCfg& cfg, const uint8_t* base
     cb.h_hi = hm;
     cb.scratch = h->d_cl_big.p;
     const uint32_t hx = t.hmax ? t.hmax : cfg.hcap;
-    launch_cluster_bins(cb, hx, t.threads, cluster_bins_grid(hx, ca.gmax, t.threads, feat != nullptr, h->num_sms),
-                        st);
-    h->stats.kernel_launches += 1;
+    const int ti = k2_tuned_tier(t);
+    auto launch = [&](int thr) {
+      launch_cluster_bins(cb, hx, thr, cluster_bins_grid(hx, ca.gmax, thr, feat != nullptr, h->num_sms), st);
+      h->stats.kernel_launches += 1;
+    };
+    if (ti < 0) {
+      launch(t.threads);
+    } else if (T.k2_threads[ti] || T.k2_chosen[ti] || !T.autotune) {
+      launch(T.k2_threads[ti] ? T.k2_threads[ti] : (T.k2_chosen[ti] ? T.k2_chosen[ti] : t.threads));
+    } else {
+      // the tier's first chunk: each block size in turn on the same reads
+      // (the outputs are the same), the fastest kept
+      cudaEvent_t* e = &h->events[28];
+      for (int i = 0; i < 3; i++) {
+        CK(cudaEventRecord(e[0], st));
+        launch(K2_TRIAL_THREADS[i]);
+        CK(cudaEventRecord(e[1], st));
+        CK(cudaEventSynchronize(e[1]));
+        T.k2_ms[ti][i] = (float)ms_between(e[0], e[1]);
+      }
+      int best = 0;
+      for (int i = 1; i < 3; i++)
+        if (T.k2_ms[ti][i] < T.k2_ms[ti][best]) best = i;
+      T.k2_chosen[ti] = K2_TRIAL_THREADS[best];
+    }
     lo = hm;
   }
   const uint32_t ns = ovf_max_slices(h);

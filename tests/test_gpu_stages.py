@@ -234,3 +234,35 @@ def test_candidates_over_256_groups(P, oracle, tmp_path, group_width):
     prefix, seqs, quals = _wide_group_genome(tmp_path)
     tc, _ = _check_clusters(P, oracle, prefix, seqs, quals, group_width=group_width, max_per_read=256)
     assert tc.min() > 256, "every read must have clusters in more than 256 groups"
+
+
+def test_cluster_block_sizes_agree(P, tmp_path):
+    """The K2 block size of the 4096-hit and slab tiers (tuned, or forced with
+    k2_threads) changes no candidate and no record. 200-base reads of a genome
+    with 250 copies of a 2 kbp unit fill both tiers."""
+    from probebwa_gb300 import synth
+    contigs = synth.genome_single(301, length=700_000, n_copies=250, copy_len=2000)
+    prefix = str(tmp_path / "rep250")
+    synth.write_index(prefix, contigs)
+    seqs, quals, _ = synth.reads_single(302, contigs, n=200, L=200, sub=0.01, indel=0.001)
+    R = P.Reads.from_lists(seqs, quals)
+    outs = []
+    for k2 in ((1024, 1024), (512, 512), (256, 256), (0, 0)):
+        with P.Mapper(prefix) as m:
+            m.set_tuning(k2_threads=k2)
+            c = m.cluster_batch(R, max_per_read=64)
+            rec = m.map_single(R)
+            t = m.tuning()
+        outs.append((c, rec))
+        if k2 == (0, 0):
+            assert all(x in (256, 512, 1024) for x in t["k2_chosen"]), t
+    with P.Mapper(prefix) as m:
+        hit_off = m.seed_batch(R)[0]
+    per = np.diff(hit_off.astype(np.int64))
+    assert ((per > 2048) & (per <= 4096)).any() and ((per > 4096) & (per <= 16384)).any(), "both tiers must be used"
+    c0, r0 = outs[0]
+    for c, r in outs[1:]:
+        for a, b in zip(c, c0):
+            assert np.array_equal(a, b)
+        for k in ("contig", "pos", "mapq", "flag", "as_score", "nm", "cigar_off"):
+            assert np.array_equal(r[k], r0[k]), k
