@@ -161,27 +161,20 @@ __device__ __forceinline__ uint32_t swiss_find_warp(const uint32_t* t, uint32_t 
 
 constexpr uint32_t SWISS_WARP_SLOTS = 512;  // buckets of the shared-memory replay (groups <= 256)
 
-// swiss_find over a table of nb <= 64 buckets held as an occupancy mask:
-// the first empty bucket of the circular scan (nb <= W) or of the first
-// probe group with one (triangular probing), by bit rotation.
-__device__ __forceinline__ uint32_t swiss_find_mask(unsigned long long occ, uint32_t nb, uint32_t h, int W) {
-  const uint32_t mask = nb - 1;
-  const unsigned long long all = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
-  const unsigned long long fr = ~occ & all;
-  uint32_t pos = h & mask;
-  auto rot = [&](uint32_t p0) -> unsigned long long {  // free buckets from p0 on, circularly
-    return p0 ? ((fr >> p0) | (fr << (nb - p0))) & all : fr;
-  };
-  if (nb <= (uint32_t)W) {
-    const unsigned long long r = rot(pos);
-    return r ? (pos + (uint32_t)__ffsll((long long)r) - 1) & mask : 0u;
-  }
-  const unsigned long long gm = (1ull << W) - 1ull;
-  uint32_t stride = 0;
+// swiss_find over a table of nb <= 64 buckets (nb a power of two) held as
+// a free-bucket mask in two 32-bit halves, replicated with period nb (bit i
+// is bucket i mod nb), so that every probe window, wrapping or not, is the
+// low bits of one 64-bit rotation: the first free bucket of the circular
+// scan from h (nb <= W; wl = nb) or of the first probe group of W buckets
+// with one (triangular probing; wl = W).
+__device__ __forceinline__ uint32_t swiss_find_free(uint32_t lo, uint32_t hi, uint32_t nb, uint32_t h, uint32_t wl) {
+  const uint32_t mask = nb - 1, gm = (1u << wl) - 1u;
+  uint32_t pos = h & mask, stride = 0;
   for (uint32_t guard = 0; guard <= nb; guard++) {
-    const unsigned long long r = rot(pos) & gm;
-    if (r) return (pos + (uint32_t)__ffsll((long long)r) - 1) & mask;
-    stride += W;
+    const bool low = pos < 32;
+    const uint32_t win = __funnelshift_r(low ? lo : hi, low ? hi : lo, pos) & gm;
+    if (win) return (pos + (uint32_t)__ffs((int)win) - 1) & mask;
+    stride += wl;
     pos = (pos + stride) & mask;
   }
   return 0xFFFFFFFFu;
@@ -189,43 +182,94 @@ __device__ __forceinline__ uint32_t swiss_find_mask(unsigned long long occ, uint
 
 constexpr uint32_t SWISS_MASK_GROUPS = 56;  // the largest table of 56 items has 64 buckets
 
-// swiss_replay of at most 56 groups by one thread: occupancy in a 64-bit
-// mask, bucket contents (insertion indices) in slots[64], the rehash copy in
-// olds[64]; hs[t] the low 32 bits of insertion t's hash, ord[t] its group
-// slot. Same insertions, rehashes (old buckets in bucket order) and ranks as
-// swiss_replay.
-__device__ bool swiss_replay_mask(uint32_t G, const uint32_t* ord, const uint32_t* hs, const uint32_t* ggk,
-                                  uint32_t* slots, uint32_t* olds, uint32_t* rank, uint32_t* gk_by_rank, int W) {
-  unsigned long long occ = 0;
-  uint32_t nb = 0, items = 0;
-  for (uint32_t t = 0; t < G; t++) {
-    if (items + 1 > swiss_cap(nb)) {
-      const uint32_t need = max(items + 1, swiss_cap(nb) + 1);
-      const uint32_t nnb = swiss_buckets(need);
-      if (nnb > 64) return false;
-      const unsigned long long old = occ;
-      for (uint32_t s = 0; s < nb; s++) olds[s] = slots[s];
-      occ = 0;
-      for (unsigned long long m = old; m; m &= m - 1) {
-        const uint32_t ot = olds[__ffsll((long long)m) - 1];
-        const uint32_t q = swiss_find_mask(occ, nnb, hs[ot], W);
-        occ |= 1ull << q;
-        slots[q] = ot;
+// swiss_replay of at most 56 groups by one warp in registers (all 32 lanes
+// call it): the table's free buckets as a replicated mask every lane holds
+// (swiss_find_free), bucket s's insertion index and hash in lane s / 2, and
+// insertion t's hash in lane t % 32, moved between lanes by shuffles; the
+// same insertions and rehashes (old buckets in bucket order) as
+// swiss_replay. The next item's shuffles are issued before the current
+// item's probe, so only the free mask is carried from item to item. The
+// ranks come out in parallel: a bucket's rank is the number of occupied
+// buckets before it.
+__device__ bool swiss_replay_regs(uint32_t G, const uint32_t* ord, const uint32_t* ggk, uint32_t* rank,
+                                  uint32_t* gk_by_rank, int W, int lane) {
+  constexpr uint32_t EMPTY = 0xFFFFFFFFu;
+  constexpr unsigned FULL = 0xffffffffu;
+  uint32_t h0 = 0, h1 = 0;  // hashes of insertions lane and lane + 32
+  if ((uint32_t)lane < G) {
+    const uint32_t gk = ggk[ord[lane]];
+    h0 = (uint32_t)fx_hash_group(gk >> 1, gk & 1u);
+  }
+  if ((uint32_t)lane + 32 < G) {
+    const uint32_t gk = ggk[ord[lane + 32]];
+    h1 = (uint32_t)fx_hash_group(gk >> 1, gk & 1u);
+  }
+  uint32_t b0 = EMPTY, b1 = EMPTY, hb0 = 0, hb1 = 0;  // buckets 2 lane and 2 lane + 1: item, hash
+  uint32_t lo = 0, hi = 0;                            // free mask (no table yet)
+  uint32_t nb = 0, wl = 0, unit = 0;                  // unit: bits at multiples of nb in a half
+  auto put = [&](uint32_t q, uint32_t t, uint32_t h) {
+    if ((uint32_t)lane == (q >> 1)) {
+      if (q & 1) {
+        b1 = t;
+        hb1 = h;
+      } else {
+        b0 = t;
+        hb0 = h;
       }
-      nb = nnb;
     }
-    const uint32_t q = swiss_find_mask(occ, nb, hs[t], W);
-    if (q == 0xFFFFFFFFu) return false;
-    occ |= 1ull << q;
-    slots[q] = t;
-    items++;
+  };
+  auto take = [&](uint32_t q) {  // mark bucket q (every copy of it) occupied
+    const uint32_t c = nb == 64 ? 1u << (q & 31) : unit << q;
+    lo &= (nb < 64 || q < 32) ? ~c : ~0u;
+    hi &= (nb < 64 || q >= 32) ? ~c : ~0u;
+  };
+  uint32_t hn = __shfl_sync(FULL, h0, 0);
+  for (uint32_t t = 0; t < G; t++) {
+    const uint32_t ht = hn;
+    const uint32_t tn = min(t + 1, G - 1);
+    hn = __shfl_sync(FULL, tn < 32 ? h0 : h1, (int)(tn & 31));
+    if (t + 1 > swiss_cap(nb)) {  // t items are in the table
+      const uint32_t nnb = swiss_buckets(max(t + 1, swiss_cap(nb) + 1));
+      if (nnb > 64) return false;
+      unsigned long long m =
+          nb == 0 ? 0ull : ~(((unsigned long long)hi << 32) | lo) & (nb == 64 ? ~0ull : (1ull << nb) - 1ull);
+      const uint32_t o0 = b0, o1 = b1, g0 = hb0, g1 = hb1;
+      b0 = b1 = EMPTY;
+      nb = nnb;
+      wl = min(nb, (uint32_t)W);
+      unit = nb >= 32 ? 1u : 0xFFFFFFFFu / ((1u << nb) - 1u);
+      lo = hi = 0xFFFFFFFFu;
+      uint32_t sb = m ? (uint32_t)__ffsll((long long)m) - 1 : 0;
+      uint32_t ot = __shfl_sync(FULL, (sb & 1) ? o1 : o0, (int)(sb >> 1));
+      uint32_t oh = __shfl_sync(FULL, (sb & 1) ? g1 : g0, (int)(sb >> 1));
+      while (m) {
+        const uint32_t ct = ot, chh = oh;
+        m &= m - 1;
+        sb = m ? (uint32_t)__ffsll((long long)m) - 1 : 0;
+        ot = __shfl_sync(FULL, (sb & 1) ? o1 : o0, (int)(sb >> 1));
+        oh = __shfl_sync(FULL, (sb & 1) ? g1 : g0, (int)(sb >> 1));
+        const uint32_t q = swiss_find_free(lo, hi, nb, chh, wl);
+        take(q);
+        put(q, ct, chh);
+      }
+    }
+    const uint32_t q = swiss_find_free(lo, hi, nb, ht, wl);
+    if (q == EMPTY) return false;
+    take(q);
+    put(q, t, ht);
   }
-  uint32_t rk = 0;
-  for (unsigned long long m = occ; m; m &= m - 1) {
-    const uint32_t g = ord[slots[__ffsll((long long)m) - 1]];
-    rank[g] = rk;
-    gk_by_rank[rk++] = ggk[g];
+  const unsigned long long occ =
+      G == 0 ? 0ull : ~(((unsigned long long)hi << 32) | lo) & (nb == 64 ? ~0ull : (1ull << nb) - 1ull);
+  for (uint32_t hb = 0; hb < 2; hb++) {
+    const uint32_t sb = 2 * (uint32_t)lane + hb;
+    if ((occ >> sb) & 1ull) {
+      const uint32_t g = ord[hb ? b1 : b0];
+      const uint32_t rr = (uint32_t)__popcll(occ & ((1ull << sb) - 1ull));
+      rank[g] = rr;
+      gk_by_rank[rr] = ggk[g];
+    }
   }
+  __syncwarp();
   return true;
 }
 
@@ -244,16 +288,12 @@ __device__ bool swiss_replay_warp(uint32_t G, const uint32_t* ggk, uint32_t* aux
   uint32_t* hs = aux + 256;
   uint32_t* slots = aux + 512;
   uint32_t* olds = aux + 512 + SWISS_WARP_SLOTS;
+  if (G <= SWISS_MASK_GROUPS) return swiss_replay_regs(G, ord, ggk, rank, gk_by_rank, W, lane);
   for (uint32_t t = lane; t < G; t += 32) {
     const uint32_t gk = ggk[ord[t]];
     hs[t] = (uint32_t)fx_hash_group(gk >> 1, gk & 1u);
   }
   __syncwarp();
-  if (G <= SWISS_MASK_GROUPS) {
-    bool ok = true;
-    if (lane == 0) ok = swiss_replay_mask(G, ord, hs, ggk, slots, olds, rank, gk_by_rank, W);
-    return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-  }
   uint32_t nb = 0, items = 0;
   for (uint32_t t = 0; t < G; t++) {
     if (items + 1 > swiss_cap(nb)) {
