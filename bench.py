@@ -327,7 +327,7 @@ def run_gpu(args, prefix, d, meta, rank, world):
     }
     out["_records"] = plain_records
     out["batching"] = {"band_dp_lanes_by_length_class": dict(zip(("<=128", "<=256", ">256"), tuning["chosen_lanes"])),
-                       "band_dp_tuned_ms_8_16": dict(zip(("<=128", "<=256", ">256"), tuning["tuned_ms"])),
+                       "band_dp_tuned_ms_8_16_4": dict(zip(("<=128", "<=256", ">256"), tuning["tuned_ms"])),
                        "length_bins": bool(tuning["length_bins"]), "pair_graphs": bool(tuning["pair_graphs"])}
     if ranked is not None:
         ranked["speedup_vs_plain"] = round(ranked["value"] / value, 3)

@@ -327,19 +327,22 @@ int pbw_build_hash(const char* genome_prefix, const char* out_prefix, uint64_t k
 
 /* Batching settings of a handle (no counterpart in the reference).
  * autotune: the seeded band DP exists with 8 lanes per alignment (8 band
- *   columns each) and 16 lanes (4 each); with autotune the first chunk of
- *   each read-length class (<= 128, <= 256, longer bases) runs both on the
- *   same alignments and the faster form is kept for the class (the results
- *   are the same either way). band_lanes 8 or 16 forces a form; 0 leaves it
- *   to the tuner (8 without it).
+ *   columns each at the default band of 30), 16 lanes (4 each) and, for
+ *   bands of 16 to 31, 4 lanes (16 each); with autotune the first chunk of
+ *   each read-length class (<= 128, <= 256, longer bases) runs every form on
+ *   the same alignments and the fastest is kept for the class (the results
+ *   are the same either way). band_lanes 4, 8 or 16 forces a form (4 runs
+ *   as 8 for bands without a 4-lane form); 0 leaves it to the tuner (8
+ *   without it).
  * length_bins: in a chunk whose reads differ in length, the seeded DP's work
  *   queue is ordered by 16-base length bins, longest first.
  * pair_graphs: each batch of pairs (decide, cross-alignment DP, statistics,
  *   resolve, observation copy) is one CUDA graph launch, captured once per
  *   chunk of pairs.
  * chosen_lanes / tuned_ms are outputs of pbw_get_tuning: the form chosen
- * per read-length class (0 = not tuned yet) and the two timings (8 lanes,
- * 16 lanes, ms) that chose it. All settings are on by default.
+ * per read-length class (0 = not tuned yet) and the timings (8 lanes, 16
+ * lanes, 4 lanes, ms; 0 = not run) that chose it. All settings are on by
+ * default.
  * wait_polls: the whole-window DP's warps wait for the warp to their left
  *   with a bounded spin; after this many polls (0 = the default, 2^22) the
  *   wait gives up, the call discards its results and returns PBW_ERR_DEVICE.
@@ -362,7 +365,7 @@ typedef struct {
   int32_t length_bins;
   int32_t pair_graphs;
   int32_t chosen_lanes[3];
-  float tuned_ms[3][2];
+  float tuned_ms[3][3];
   uint32_t wait_polls;
   uint32_t ovf_slice_hits;
   int32_t k2_threads[2];      /* K2 block size for the 2049-4096-hit tier and the 4097-16384-hit tier

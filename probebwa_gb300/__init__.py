@@ -83,7 +83,7 @@ class RankerReportC(C.Structure):
 
 class TuningC(C.Structure):
     _fields_ = [("autotune", C.c_int32), ("band_lanes", C.c_int32), ("length_bins", C.c_int32),
-                ("pair_graphs", C.c_int32), ("chosen_lanes", C.c_int32 * 3), ("tuned_ms", (C.c_float * 2) * 3),
+                ("pair_graphs", C.c_int32), ("chosen_lanes", C.c_int32 * 3), ("tuned_ms", (C.c_float * 3) * 3),
                 ("wait_polls", C.c_uint32), ("ovf_slice_hits", C.c_uint32), ("k2_threads", C.c_int32 * 2),
                 ("k2_chosen", C.c_int32 * 2), ("k2_tuned_ms", (C.c_float * 3) * 2)]
 
@@ -556,7 +556,7 @@ class Mapper:
                 "k2_chosen": list(t.k2_chosen), "k2_tuned_ms": [list(r) for r in t.k2_tuned_ms]}
 
     def set_tuning(self, **kw):
-        """pbw_set_tuning: autotune, band_lanes (0, 8, 16), length_bins, pair_graphs, wait_polls,
+        """pbw_set_tuning: autotune, band_lanes (0, 4, 8, 16), length_bins, pair_graphs, wait_polls,
         ovf_slice_hits, k2_threads (two of 0, 256, 512, 1024)."""
         t = TuningC()
         self._check(lib().pbw_get_tuning(self.h, C.byref(t)))

@@ -29,6 +29,7 @@
 // NEG_INF exactly as in the reference; rows before R0 hold the initial row
 // (M = 0 at every window column, smith_waterman.rs:174-176).
 #include <algorithm>
+#include <type_traits>
 
 #include "align_finish.cuh"
 #include "pbw_common.cuh"
@@ -76,9 +77,14 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 
+// One lane's traceback nibbles of a row: C cells of 4 bits.
 template <int C>
-__device__ __forceinline__ void store_tb(unsigned char* row, int k, uint32_t word) {
-  if (C == 8) ((uint32_t*)row)[k] = word;
+using TbWord = typename std::conditional<(C > 8), unsigned long long, uint32_t>::type;
+
+template <int C>
+__device__ __forceinline__ void store_tb(unsigned char* row, int k, TbWord<C> word) {
+  if (C == 16) ((unsigned long long*)row)[k] = word;
+  else if (C == 8) ((uint32_t*)row)[k] = (uint32_t)word;
   else if (C == 4) ((uint16_t*)row)[k] = (uint16_t)word;
   else row[k] = (uint8_t)word;
 }
@@ -187,7 +193,7 @@ __device__ void band_traceback(int k, unsigned gmask, int m, int n, int B, int R
 // column 2*band + 1 (M and I; its up value feeds column 2*band), at lane
 // kstar, position TSTAR.
 template <int C, int G, int TSTAR, bool GENERAL>
-__device__ __forceinline__ uint32_t band_step(int32_t (&PM)[C], int32_t (&PI)[C], int32_t (&PD)[C], const int (&lo)[C],
+__device__ __forceinline__ TbWord<C> band_step(int32_t (&PM)[C], int32_t (&PI)[C], int32_t (&PD)[C], const int (&lo)[C],
                                               const int (&sp)[C], int k, int i, int R0, int kstar, int32_t qsym,
                                               int32_t pen, int32_t ge, const int2* cols) {
   constexpr unsigned FULL = 0xffffffffu;
@@ -196,7 +202,7 @@ __device__ __forceinline__ uint32_t band_step(int32_t (&PM)[C], int32_t (&PI)[C]
   int32_t lM = k ? sLM : NEG, lD = k ? sLD : NEG;
   const bool pre = i < R0;
   const bool kill = k == kstar;
-  uint32_t word = 0;
+  TbWord<C> word = 0;
   int32_t upM = NEG, upI = NEG;
 #pragma unroll
   for (int t = 0; t < C; t++) {
@@ -213,7 +219,7 @@ __device__ __forceinline__ uint32_t band_step(int32_t (&PM)[C], int32_t (&PI)[C]
     const int32_t Iv = max(io, ie);
     const int32_t dop = lM + go, dex = lD + ge;
     const int32_t Dv = max(dop, dex);
-    word |= (tm | (io >= ie ? 0u : 4u) | (dop >= dex ? 0u : 8u)) << (4 * t);
+    word |= (TbWord<C>)(tm | (io >= ie ? 0u : 4u) | (dop >= dex ? 0u : 8u)) << (4 * t);
     int32_t nM, nI, nD;
     if (GENERAL) {
       const bool on = (unsigned)(i - lo[t]) <= (unsigned)sp[t];
@@ -250,7 +256,10 @@ struct BoolConst {
 };
 
 template <int C, int G, int TSTAR>
-__global__ void __launch_bounds__(32, 16) k_align_band(AlignArgs p, BandLayout LY) {
+// The 4-lane form keeps 16 columns of state per lane; its shared memory
+// (8 alignments per warp) already holds it to a few blocks per SM, so its
+// register bound is looser.
+__global__ void __launch_bounds__(32, G == 4 ? 4 : 16) k_align_band(AlignArgs p, BandLayout LY) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int BJ = 32 / G;         // alignments per warp
@@ -416,7 +425,7 @@ __global__ void __launch_bounds__(32, 16) k_align_band(AlignArgs p, BandLayout L
       const int32_t qsym = rw & 0xFF;
       const int32_t pen = rw >> 16;
       const int jb = min(max(i + base + k * C - 1, -B_PADC), n + B_PADC - C);
-      const uint32_t word = band_step<C, G, TSTAR, GEN>(PM, PI, PD, lo, sp, k, i, R0, kstar, qsym, pen, ge, coli + jb);
+      const TbWord<C> word = band_step<C, G, TSTAR, GEN>(PM, PI, PD, lo, sp, k, i, R0, kstar, qsym, pen, ge, coli + jb);
       if (i >= R0 && i <= R1) {
         store_tb<C>(tbg + (size_t)(i - R0) * ROWB, k, word);
         if (i == R1) {
@@ -513,21 +522,42 @@ size_t band_tb_slab_bytes(int lmax, int nmax, int num_sms, int band_max) {
     const int g16 = C == 4 ? band_grid<2, 16>(L16, num_sms) : band_grid<4, 16>(L16, num_sms);
     need = std::max(need, (size_t)g16 * 2 * L16.tb_job);
   }
+  if (C == 8) {
+    // 4 lanes with twice the columns per lane
+    const BandLayout L4 = band_layout(lmax, nmax, 4 * 16 / 2);
+    need = std::max(need, (size_t)band_grid<16, 4>(L4, num_sms) * 8 * L4.tb_job);
+  }
   return need;
 }
 
 // Whether a 16-lane form exists for the band (a band of at least 8 columns
 // per 8 lanes, i.e. C >= 4).
 bool band_has_lanes16(int band_max) { return band_c(band_max) >= 4; }
+// Whether a 4-lane form exists for the band (16 columns per lane: bands of
+// 16 to 31).
+bool band_has_lanes4(int band_max) { return band_c(band_max) == 8; }
 
 // lanes lanes per alignment, C columns per lane with lanes*C > 2*band_max + 1;
 // the fast form is compiled for column 2*band_max + 1 at lane position TSTAR
 // (odd, as 2*band + 1 is odd and C even); alignments of other bands in the
 // same launch use the masked form throughout. lanes 16 halves C (bands with
-// C >= 4 only).
+// C >= 4 only); lanes 4 doubles it (C == 8 only).
 void launch_align_band_lanes(const AlignArgs& a, int num_sms, int band_max, int lanes, cudaStream_t st) {
   const int cstar = 2 * band_max + 1;
   const int C = band_c(band_max);
+  if (lanes == 4 && C == 8) {
+    switch (cstar % 16) {
+      case 1: launch_band_c<16, 4, 1>(a, num_sms, st); break;
+      case 3: launch_band_c<16, 4, 3>(a, num_sms, st); break;
+      case 5: launch_band_c<16, 4, 5>(a, num_sms, st); break;
+      case 7: launch_band_c<16, 4, 7>(a, num_sms, st); break;
+      case 9: launch_band_c<16, 4, 9>(a, num_sms, st); break;
+      case 11: launch_band_c<16, 4, 11>(a, num_sms, st); break;
+      case 13: launch_band_c<16, 4, 13>(a, num_sms, st); break;
+      default: launch_band_c<16, 4, 15>(a, num_sms, st); break;
+    }
+    return;
+  }
   if (lanes == 16 && C >= 4) {
     if (C == 4) {
       launch_band_c<2, 16, 1>(a, num_sms, st);

@@ -451,8 +451,7 @@ int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t) {
   t->ovf_slice_hits = T.ovf_slice_hits;
   for (int c = 0; c < 3; c++) {
     t->chosen_lanes[c] = T.chosen[c];
-    t->tuned_ms[c][0] = T.ms[c][0];
-    t->tuned_ms[c][1] = T.ms[c][1];
+    for (int j = 0; j < 3; j++) t->tuned_ms[c][j] = T.ms[c][j];
   }
   for (int i = 0; i < 2; i++) {
     t->k2_threads[i] = T.k2_threads[i];
@@ -464,8 +463,8 @@ int pbw_get_tuning(const pbw_handle* h, pbw_tuning* t) {
 
 int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t) {
   if (!h || !t) return PBW_ERR_ARG;
-  if (t->band_lanes != 0 && t->band_lanes != 8 && t->band_lanes != 16) {
-    h->err = "pbw_set_tuning: band_lanes must be 0, 8 or 16";
+  if (t->band_lanes != 0 && t->band_lanes != 4 && t->band_lanes != 8 && t->band_lanes != 16) {
+    h->err = "pbw_set_tuning: band_lanes must be 0, 4, 8 or 16";
     return PBW_ERR_ARG;
   }
   for (int i = 0; i < 2; i++) {
@@ -484,7 +483,7 @@ int pbw_set_tuning(pbw_handle* h, const pbw_tuning* t) {
   T.ovf_slice_hits = t->ovf_slice_hits;
   for (int c = 0; c < 3; c++) {
     T.chosen[c] = 0;
-    T.ms[c][0] = T.ms[c][1] = 0.f;
+    T.ms[c][0] = T.ms[c][1] = T.ms[c][2] = 0.f;
   }
   for (int i = 0; i < 2; i++) {
     T.k2_threads[i] = t->k2_threads[i];

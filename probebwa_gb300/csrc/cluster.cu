@@ -206,17 +206,13 @@ __device__ bool swiss_replay_regs(uint32_t G, const uint32_t* ord, const uint32_
   }
   uint32_t b0 = EMPTY, b1 = EMPTY, hb0 = 0, hb1 = 0;  // buckets 2 lane and 2 lane + 1: item, hash
   uint32_t lo = 0, hi = 0;                            // free mask (no table yet)
-  uint32_t nb = 0, wl = 0, unit = 0;                  // unit: bits at multiples of nb in a half
+  uint32_t nb = 0, wl = 0, unit = 0, cap = 0;         // unit: bits at multiples of nb in a half
   auto put = [&](uint32_t q, uint32_t t, uint32_t h) {
-    if ((uint32_t)lane == (q >> 1)) {
-      if (q & 1) {
-        b1 = t;
-        hb1 = h;
-      } else {
-        b0 = t;
-        hb0 = h;
-      }
-    }
+    const bool mine = (uint32_t)lane == (q >> 1), odd = (q & 1) != 0;
+    b0 = mine && !odd ? t : b0;
+    hb0 = mine && !odd ? h : hb0;
+    b1 = mine && odd ? t : b1;
+    hb1 = mine && odd ? h : hb1;
   };
   auto take = [&](uint32_t q) {  // mark bucket q (every copy of it) occupied
     const uint32_t c = nb == 64 ? 1u << (q & 31) : unit << q;
@@ -228,14 +224,15 @@ __device__ bool swiss_replay_regs(uint32_t G, const uint32_t* ord, const uint32_
     const uint32_t ht = hn;
     const uint32_t tn = min(t + 1, G - 1);
     hn = __shfl_sync(FULL, tn < 32 ? h0 : h1, (int)(tn & 31));
-    if (t + 1 > swiss_cap(nb)) {  // t items are in the table
-      const uint32_t nnb = swiss_buckets(max(t + 1, swiss_cap(nb) + 1));
+    if (t + 1 > cap) {  // t items are in the table
+      const uint32_t nnb = swiss_buckets(max(t + 1, cap + 1));
       if (nnb > 64) return false;
       unsigned long long m =
           nb == 0 ? 0ull : ~(((unsigned long long)hi << 32) | lo) & (nb == 64 ? ~0ull : (1ull << nb) - 1ull);
       const uint32_t o0 = b0, o1 = b1, g0 = hb0, g1 = hb1;
       b0 = b1 = EMPTY;
       nb = nnb;
+      cap = swiss_cap(nb);
       wl = min(nb, (uint32_t)W);
       unit = nb >= 32 ? 1u : 0xFFFFFFFFu / ((1u << nb) - 1u);
       lo = hi = 0xFFFFFFFFu;
@@ -598,10 +595,20 @@ __device__ void group_ranks_block(const ClusterArgs& p, uint32_t TG, const uint3
   __syncthreads();
 }
 
+// Barrier among the threads of warps 1.. of the block (named barrier 1;
+// __syncthreads is barrier 0).
+__device__ __forceinline__ void sync_upper_warps() {
+  asm volatile("bar.sync 1, %0;" ::"r"(blockDim.x - 32) : "memory");
+}
+
+// early_groups: the groups are collected in a pass of their own before the
+// bins, so that warp 0 ranks them (B) while the other warps bin the hits (A)
+// and link the bins (C1); otherwise A collects both and B runs beside C1
+// only.
 template <bool FEAT>
 __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
                                   unsigned char* tab, const BinScratch& X, uint32_t* wtmp32, uint32_t& sh_n,
-                                  uint32_t* sh_aux) {
+                                  uint32_t* sh_aux, bool early_groups) {
   const uint32_t T = bin_tsize(H);            // bin slots (the bins and clusters of the read <= H)
   const uint32_t TG = grp_tsize(H, p.gmax);   // group slots
   const int lane = threadIdx.x & 31;
@@ -646,9 +653,24 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     wtmp32[30] = 0;  // exact-path flag
   }
   __syncthreads();
-  // A. bins and groups (32-bit counters: same-address 32-bit adds from one
-  // warp combine in the shared-memory unit, 64-bit ones serialise)
-  for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+  if (early_groups) {
+    // A0. the groups and their first-emission indices
+    for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+      const uint32_t g = insert32(gkey, (uint32_t)(hits[i] >> 40), TG);
+      if (g == NO_SLOT) {
+        atomicExch(p.err, 1);
+        continue;
+      }
+      if (gval[g] > i) atomicMin(&gval[g], i);
+    }
+    __syncthreads();
+  }
+  // A. bins (and groups unless collected in A0) by warps 1.. with
+  // early_groups, else by the whole block (32-bit counters: same-address
+  // 32-bit adds from one warp combine in the shared-memory unit, 64-bit ones
+  // serialise)
+  const uint32_t a0 = early_groups ? 32 : 0;
+  for (uint32_t i = threadIdx.x - a0; threadIdx.x >= a0 && i < H; i += blockDim.x - a0) {
     const unsigned long long w = hits[i];
     const unsigned long long d = w & M40;
     // diagonal / 51 in 32 bits while the diagonal fits (every contig under
@@ -665,15 +687,21 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     }
     const uint32_t gk = (uint32_t)(w >> 40);
     const uint32_t s = insert64(B.key, ((unsigned long long)gk << 35) | b, T);
-    const uint32_t g = insert32(gkey, gk, TG);
-    if (s == NO_SLOT || g == NO_SLOT) {
+    if (!early_groups) {
+      const uint32_t g = insert32(gkey, gk, TG);
+      if (g == NO_SLOT) {
+        atomicExch(p.err, 1);
+        continue;
+      }
+      if (gval[g] > i) atomicMin(&gval[g], i);
+    }
+    if (s == NO_SLOT) {
       atomicExch(p.err, 1);
       continue;
     }
     atomicAdd(&B.cnt[s], 1u);
     atomicAdd(&B.sum[s], off);
     atomicOr(off < 32 ? &B.mlo[s] : &B.mhi[s], 1u << (off & 31u));
-    if (gval[g] > i) atomicMin(&gval[g], i);
     if (FEAT) {
       // hit info: read position | log2 exact bucket size << 10 | neighbour << 15
       const uint32_t info = p.hit_info[(size_t)r * p.hcap + i];
@@ -683,7 +711,8 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
       atomicMax(&B.rmx[s], info & 0x3FFu);
     }
   }
-  __syncthreads();
+  if (!early_groups) __syncthreads();
+  else if (threadIdx.x >= 32) sync_upper_warps();
   // B + C1. Warp 0 computes the group iteration ranks (B) while the other
   // warps link the bins (C1): each occupied bin looks up its upper
   // neighbour once, and when the two join, records the link (a 16-bit slot
@@ -982,7 +1011,7 @@ __global__ void __launch_bounds__(1024, 1) k_cluster_bins(ClusterArgs p, uint32_
           p.feat[(size_t)r * MAX_CAND * RANK_FEATURES + i] = 0.f;
       continue;
     }
-    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, X, wtmp32, sh_n, sh_aux);
+    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, X, wtmp32, sh_n, sh_aux, !GT);
   }
 }
 
@@ -1008,7 +1037,7 @@ __global__ void __launch_bounds__(1024, 1) k_cluster_list(ClusterArgs p, size_t 
     BinScratch X;
     X.carve(base, H, p.gmax);
     cluster_read_bins<false>(p, r, H, p.hits_pool + off, base + bin_scratch_bytes(H, p.gmax), X, wtmp32, sh_n,
-                             sh_aux);
+                             sh_aux, false);
     if (p.feat) {
       const uint32_t nout = p.n_cand[r];
       for (uint32_t i = threadIdx.x; i < (uint32_t)MAX_CAND * RANK_FEATURES; i += blockDim.x)

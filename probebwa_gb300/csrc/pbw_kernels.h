@@ -178,9 +178,11 @@ struct AlignArgs {
 // AlignArgs::tb_global must hold band_tb_slab_bytes(lmax, nmax, num_sms,
 // band_max) bytes (the per-alignment traceback rows).
 void launch_align_band(const AlignArgs& a, int num_sms, int band_max, cudaStream_t st);
-// The same with 8 or 16 lanes per alignment (16: bands with band_has_lanes16).
+// The same with 4, 8 or 16 lanes per alignment (16: bands with
+// band_has_lanes16; 4: bands with band_has_lanes4).
 void launch_align_band_lanes(const AlignArgs& a, int num_sms, int band_max, int lanes, cudaStream_t st);
 bool band_has_lanes16(int band_max);
+bool band_has_lanes4(int band_max);
 size_t band_tb_slab_bytes(int lmax, int nmax, int num_sms, int band_max);
 // K3w, one job per block of 8 warps; tb_global_per_warp is the global slab of
 // one block (window_slab_bytes), used by windows that do not fit the block's

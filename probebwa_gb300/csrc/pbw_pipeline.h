@@ -147,12 +147,12 @@ struct pbw_handle {
   } rk;
   // batching: seeded-DP form per read-length class, length bins, graphs
   struct Tuning {
-    int autotune = 1;       // time the 8- and 16-lane band DP on a class's first chunk, keep the faster
-    int band_lanes = 0;     // 0: the tuned (or 8) form; 8 or 16: forced
+    int autotune = 1;       // time the 8-, 16- and 4-lane band DP on a class's first chunk, keep the fastest
+    int band_lanes = 0;     // 0: the tuned (or 8) form; 4, 8 or 16: forced
     int length_bins = 1;    // order the seeded DP queue by read length in mixed-length chunks
     int pair_graphs = 1;    // one CUDA graph launch per batch of pairs
     int chosen[3] = {0, 0, 0};  // lanes per read-length class (<= 128, <= 256, longer); 0: not tuned
-    float ms[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    float ms[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // the trial: 8, 16, 4 lanes
     uint32_t wait_polls = 0;  // window-DP wavefront waits: polls before giving up (0 = the kernel's default)
     uint32_t ovf_slice_hits = 0;  // over-capacity reads: hits per pool slice (0 = the default, 16 M)
     int k2_threads[2] = {0, 0};   // K2 block size of the 4096-hit and the slab tier: 0 tuned, else forced

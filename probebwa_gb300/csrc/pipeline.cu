@@ -480,8 +480,9 @@ static int length_class(int lmax) { return lmax <= 128 ? 0 : (lmax <= 256 ? 1 : 
 // The seeded band DP in the form chosen for this read-length class: forced
 // by pbw_set_tuning, or timed once per class on the class's first chunk --
 // the 8-lane form runs, the queue and the counters it moved are put back,
-// the 16-lane form runs on the same jobs (same results: the DP is exact),
-// and the faster one is kept for the class's later chunks.
+// the 16-lane form (and, for bands of 16 to 31, the 4-lane one) runs on the
+// same jobs (same results: the DP is exact), and the fastest is kept for the
+// class's later chunks.
 static int band_dp(pbw_handle* h, const AlignArgs& aa, const ChunkCfg& cfg) {
   cudaStream_t st = h->st;
   const int band = (int)h->opt.max_indel_len;
@@ -491,7 +492,7 @@ static int band_dp(pbw_handle* h, const AlignArgs& aa, const ChunkCfg& cfg) {
     launch_align_band_lanes(aa, h->num_sms, band, 8, st);
     return PBW_OK;
   }
-  if (T.band_lanes == 8 || T.band_lanes == 16) {
+  if (T.band_lanes == 4 || T.band_lanes == 8 || T.band_lanes == 16) {
     launch_align_band_lanes(aa, h->num_sms, band, T.band_lanes, st);
     return PBW_OK;
   }
@@ -518,8 +519,22 @@ static int band_dp(pbw_handle* h, const AlignArgs& aa, const ChunkCfg& cfg) {
   CK(cudaEventSynchronize(e[3]));
   T.ms[cls][0] = (float)ms_between(e[0], e[1]);
   T.ms[cls][1] = (float)ms_between(e[2], e[3]);
+  T.ms[cls][2] = 0.f;
   T.chosen[cls] = T.ms[cls][1] < T.ms[cls][0] ? 16 : 8;
   h->stats.kernel_launches += 1;
+  if (band_has_lanes4(band)) {
+    CK(cudaMemsetAsync(aa.next_job, 0, sizeof(unsigned int), st));
+    CK(cudaMemcpyAsync(aa.cig_pool_used, c32 + 12, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(c64 + 3, c64 + 12, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+    CK(cudaEventRecord(e[0], st));
+    launch_align_band_lanes(aa, h->num_sms, band, 4, st);
+    CK(cudaEventRecord(e[1], st));
+    CK(cudaGetLastError());
+    CK(cudaEventSynchronize(e[1]));
+    T.ms[cls][2] = (float)ms_between(e[0], e[1]);
+    if (T.ms[cls][2] < std::min(T.ms[cls][0], T.ms[cls][1])) T.chosen[cls] = 4;
+    h->stats.kernel_launches += 1;
+  }
   return PBW_OK;
 }
 

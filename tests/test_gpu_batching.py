@@ -57,6 +57,28 @@ def test_band_dp_16_lanes_matches_oracle(P, oracle, tmp_path):
     _same(got16, got8)
 
 
+@pytest.mark.parametrize("band", [30, 20, 17, 10])
+def test_band_dp_4_lanes_matches_oracle(P, oracle, tmp_path, band):
+    """4 lanes of 16 columns (bands 16-31; the last band column 2*band + 1
+    sits at lane position 13, 9 and 3 for bands 30, 20 and 17); band 10 has
+    no 4-lane form and runs the 8-lane one."""
+    from probebwa_gb300 import synth
+    contigs = synth.genome_single(105 + band, length=300_000, n_copies=20, copy_len=1000)
+    prefix = str(tmp_path / "g")
+    synth.write_index(prefix, contigs)
+    R = _mixed_reads(P, contigs, 106 + band, n_per=120)
+    with P.Mapper(prefix, options=P.MapperOptions(max_indel_len=band)) as m:
+        m.set_tuning(band_lanes=4, autotune=0)
+        got4 = m.map_single(R)
+        m.set_tuning(band_lanes=8, autotune=0)
+        got8 = m.map_single(R)
+    om = oracle.Mapper(prefix, max_indel_len=band)
+    exp = om.map_single(to_oracle_reads(oracle, R))
+    om.close()
+    compare_records(P, oracle, got4, exp, f"4 lanes, band {band}")
+    _same(got4, got8)
+
+
 def test_length_bins_and_autotune_keep_records(P, tmp_path):
     from probebwa_gb300 import synth
     contigs = synth.genome_single(103, length=500_000, n_copies=30, copy_len=1500)
@@ -73,7 +95,8 @@ def test_length_bins_and_autotune_keep_records(P, tmp_path):
     _same(base, tuned)
     _same(base, again)
     # reads of 60-250 bases: the <= 256 class (and the <= 128 one) got a form
-    assert t["chosen_lanes"][1] in (8, 16) and t["tuned_ms"][1][0] > 0 and t["tuned_ms"][1][1] > 0, t
+    # (the default band, 30, has all three forms)
+    assert t["chosen_lanes"][1] in (4, 8, 16) and min(t["tuned_ms"][1]) > 0, t
 
 
 def test_pair_graphs_keep_records(P, oracle, tmp_path):
