@@ -605,10 +605,14 @@ __device__ __forceinline__ void sync_upper_warps() {
 // bins, so that warp 0 ranks them (B) while the other warps bin the hits (A)
 // and link the bins (C1); otherwise A collects both and B runs beside C1
 // only.
+// grp_sh: when not null, a shared-memory home for the group table (gkey,
+// gval, grk: 3 * GRP_SH_SLOTS words), used when the read's group table fits
+// (tables in global memory: each hit's group probe then stays on the SM).
+constexpr uint32_t GRP_SH_SLOTS = 1024;
 template <bool FEAT>
 __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, const unsigned long long* hits,
                                   unsigned char* tab, const BinScratch& X, uint32_t* wtmp32, uint32_t& sh_n,
-                                  uint32_t* sh_aux, bool early_groups) {
+                                  uint32_t* sh_aux, bool early_groups, uint32_t* grp_sh) {
   const uint32_t T = bin_tsize(H);            // bin slots (the bins and clusters of the read <= H)
   const uint32_t TG = grp_tsize(H, p.gmax);   // group slots
   const int lane = threadIdx.x & 31;
@@ -624,7 +628,7 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   B.rmn = B.cnt + 6 * T;  // FEAT
   B.rmx = B.cnt + 7 * T;  // FEAT
   unsigned long long* ck = (unsigned long long*)(B.cnt + (FEAT ? 8 : 4) * T);  // cluster keys
-  uint32_t* gkey = (uint32_t*)(ck + T);
+  uint32_t* gkey = grp_sh && TG <= GRP_SH_SLOTS ? grp_sh : (uint32_t*)(ck + T);
   uint32_t* gval = gkey + TG;  // first emission index, then iteration rank
   uint32_t* grk = gval + TG;   // group key by rank
   for (uint32_t s = threadIdx.x; s < TG; s += blockDim.x) {
@@ -669,9 +673,20 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
   // early_groups, else by the whole block (32-bit counters: same-address
   // 32-bit adds from one warp combine in the shared-memory unit, 64-bit ones
   // serialise)
-  const uint32_t a0 = early_groups ? 32 : 0;
-  for (uint32_t i = threadIdx.x - a0; threadIdx.x >= a0 && i < H; i += blockDim.x - a0) {
-    const unsigned long long w = hits[i];
+  // (each thread loads its next hit, and its info, before binning the
+  // current one, so that the load's latency overlaps the insert's)
+  const uint32_t a0 = early_groups ? 32 : 0, astep = blockDim.x - a0;
+  const bool abin = threadIdx.x >= a0;
+  uint32_t i = threadIdx.x - a0;
+  unsigned long long w_next = abin && i < H ? hits[i] : 0ull;
+  uint32_t info_next = FEAT && abin && i < H ? p.hit_info[(size_t)r * p.hcap + i] : 0u;
+  for (; abin && i < H; i += astep) {
+    const unsigned long long w = w_next;
+    const uint32_t info = info_next;
+    if (i + astep < H) {
+      w_next = hits[i + astep];
+      if (FEAT) info_next = p.hit_info[(size_t)r * p.hcap + i + astep];
+    }
     const unsigned long long d = w & M40;
     // diagonal / 51 in 32 bits while the diagonal fits (every contig under
     // 4 Gbp), in 64 bits otherwise
@@ -704,7 +719,6 @@ __device__ void cluster_read_bins(const ClusterArgs& p, uint32_t r, uint32_t H, 
     atomicOr(off < 32 ? &B.mlo[s] : &B.mhi[s], 1u << (off & 31u));
     if (FEAT) {
       // hit info: read position | log2 exact bucket size << 10 | neighbour << 15
-      const uint32_t info = p.hit_info[(size_t)r * p.hcap + i];
       atomicAdd(&B.ne[s], (info >> 15) ? 0u : 1u);
       atomicAdd(&B.l2s[s], (info >> 10) & 31u);
       atomicMin(&B.rmn[s], info & 0x3FFu);
@@ -993,6 +1007,7 @@ __global__ void __launch_bounds__(1024, 1) k_cluster_bins(ClusterArgs p, uint32_
   __shared__ uint32_t wtmp32[32];
   __shared__ uint32_t sh_n;
   __shared__ __align__(8) uint32_t sh_aux[1280];
+  __shared__ uint32_t sh_grp[GT ? 3 * GRP_SH_SLOTS : 1];  // the group table of a slab-tier read
   unsigned char* slab = p.scratch + (size_t)blockIdx.x * slab_bytes;
   BinScratch X;
   X.carve(slab, hmax, p.gmax);
@@ -1011,7 +1026,8 @@ __global__ void __launch_bounds__(1024, 1) k_cluster_bins(ClusterArgs p, uint32_
           p.feat[(size_t)r * MAX_CAND * RANK_FEATURES + i] = 0.f;
       continue;
     }
-    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, X, wtmp32, sh_n, sh_aux, !GT);
+    cluster_read_bins<FEAT>(p, r, H, p.hits + (size_t)r * p.hcap, tab, X, wtmp32, sh_n, sh_aux, !GT,
+                            GT ? sh_grp : nullptr);
   }
 }
 
@@ -1037,7 +1053,7 @@ __global__ void __launch_bounds__(1024, 1) k_cluster_list(ClusterArgs p, size_t 
     BinScratch X;
     X.carve(base, H, p.gmax);
     cluster_read_bins<false>(p, r, H, p.hits_pool + off, base + bin_scratch_bytes(H, p.gmax), X, wtmp32, sh_n,
-                             sh_aux, false);
+                             sh_aux, false, nullptr);
     if (p.feat) {
       const uint32_t nout = p.n_cand[r];
       for (uint32_t i = threadIdx.x; i < (uint32_t)MAX_CAND * RANK_FEATURES; i += blockDim.x)
