@@ -86,30 +86,34 @@ def _overflow_genome(tmp_path):
     return prefix, seqs + s2, quals + q2
 
 
-def _wide_group_genome(tmp_path):
-    """200 contigs, each with a 1 kbp unit forward and reverse-complemented:
-    a read from the unit hits ~400 (contig, strand) groups (the block-wide
-    group order of reads over 256 groups) and tens of thousands of hits
-    (list mode, tables too large for bin links)."""
+def _wide_group_genome(tmp_path, n_contigs=200, L=100, copies=1):
+    """n_contigs contigs, each with copies of a 1 kbp unit forward and as
+    many reverse-complemented: a read of L bases from the unit hits
+    2 * n_contigs (contig, strand) groups. With 200 contigs that is ~310
+    groups after the bucket cap (the block-wide group order of reads over
+    256 groups) and ~5,100-5,400 hits, over the 4096-hit buffer of 100-base
+    reads (list mode)."""
     from probebwa_gb300 import synth
     rng = np.random.default_rng(311)
     unit = synth.rand_codes(rng, 1000)
     contigs = []
-    for c in range(200):
-        g = synth.rand_codes(rng, 4000)
-        g[500:1500] = synth.mutate_subs(rng, unit, 0.002)
-        g[2500:3500] = 3 - synth.mutate_subs(rng, unit, 0.002)[::-1]
+    for c in range(n_contigs):
+        g = synth.rand_codes(rng, 4000 * copies)
+        for j in range(copies):
+            o = 4000 * j
+            g[o + 500:o + 1500] = synth.mutate_subs(rng, unit, 0.002)
+            g[o + 2500:o + 3500] = 3 - synth.mutate_subs(rng, unit, 0.002)[::-1]
         contigs.append((f"w{c}", g))
     prefix = str(tmp_path / "wide")
     synth.write_index(prefix, contigs)
     seqs, quals = [], []
     for i in range(12):
-        s = int(rng.integers(0, 1000 - 100))
-        frag = unit[s:s + 100].copy()
+        s = int(rng.integers(0, 1000 - L))
+        frag = unit[s:s + L].copy()
         if i % 2:
             frag = 3 - frag[::-1]
         seqs.append(synth.ASCII[frag].tobytes())
-        quals.append(bytes(rng.integers(20, 41, size=100).astype(np.uint8)))
+        quals.append(bytes(rng.integers(20, 41, size=L).astype(np.uint8)))
     return prefix, seqs, quals
 
 
@@ -234,6 +238,24 @@ def test_candidates_over_256_groups(P, oracle, tmp_path, group_width):
     prefix, seqs, quals = _wide_group_genome(tmp_path)
     tc, _ = _check_clusters(P, oracle, prefix, seqs, quals, group_width=group_width, max_per_read=256)
     assert tc.min() > 256, "every read must have clusters in more than 256 groups"
+
+
+@pytest.mark.parametrize("n_contigs,L,copies,group_width", [(22, 100, 1, 16), (28, 100, 1, 8), (28, 170, 4, 16),
+                                                            (26, 170, 4, 8)])
+def test_candidates_near_register_replay_limit(P, oracle, tmp_path, n_contigs, L, copies, group_width):
+    """44 to 56 (contig, strand) groups per read, the top of the one-warp
+    register replay of the group order (up to 56 groups: a 64-bucket table).
+    100-base reads (~730-990 hits) take the shared-memory tiers, where the
+    groups are collected before the bins; 170-base reads of the 4-copy
+    genome (~6,200-7,000 hits) take the global-slab tier, whose group table
+    then sits in shared memory."""
+    prefix, seqs, quals = _wide_group_genome(tmp_path, n_contigs, L, copies)
+    tc, _ = _check_clusters(P, oracle, prefix, seqs, quals, group_width=group_width, max_per_read=256)
+    assert tc.min() >= 2 * n_contigs, "every read must have clusters in all of its groups"
+    with P.Mapper(prefix) as m:
+        per = np.diff(m.seed_batch(P.Reads.from_lists(seqs, quals))[0].astype(np.int64))
+    lo, hi = (0, 4096) if L == 100 else (4096, 16384)
+    assert ((per > lo) & (per <= hi)).all(), (per.min(), per.max())
 
 
 def test_cluster_block_sizes_agree(P, tmp_path):
